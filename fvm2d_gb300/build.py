@@ -1,0 +1,109 @@
+"""Build the C-ABI shared library ``_build/libfvm2d_gb300.so`` in-tree.
+
+Every translation unit is compiled in parallel:
+  * CUDA kernels for sm_103a only (``-gencode arch=compute_103a,code=sm_103a``);
+    the FP64 kernels and the set-up kernels with ``--fmad=false`` so their
+    arithmetic is rounded exactly as written, the FP32 kernels with
+    contraction allowed;
+  * host C++ with ``-ffp-contract=off`` (the driver-side geometry must equal
+    the serial FP64 arithmetic on x86 and on Arm alike).
+No CPU fallback is built: without this library the package refuses to run.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import hashlib
+import os
+import platform
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "csrc")
+INC = os.path.join(os.path.dirname(HERE), "include")
+OUT = os.path.join(HERE, "_build", platform.machine())
+LIB = os.path.join(OUT, "libfvm2d_gb300.so")
+
+CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+                      "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr",
+                      f"-I{INC}", f"-I{SRC}"]
+CXX_COMMON = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wextra",
+              "-Wno-unused-parameter", f"-I{CUDA_HOME}/include", f"-I{INC}", f"-I{SRC}"]
+
+UNITS = [
+    ("fvm_kernels_fp64.cu", "nvcc", ["--fmad=false"]),
+    ("fvm_kernels_fp32.cu", "nvcc", []),
+    ("fvm_setup.cu", "nvcc", ["--fmad=false"]),
+    ("fvm_api.cpp", "cxx", []),
+    ("fvm_layout.cpp", "cxx", []),
+    ("fvm_geometry.cpp", "cxx", []),
+]
+
+
+def _headers_digest() -> str:
+    h = hashlib.sha256()
+    for d in (SRC, INC):
+        for n in sorted(os.listdir(d)):
+            if n.endswith((".h", ".cuh")):
+                with open(os.path.join(d, n), "rb") as f:
+                    h.update(n.encode() + f.read())
+    return h.hexdigest()
+
+
+def _compile(unit, kind, extra, digest, verbose):
+    src = os.path.join(SRC, unit)
+    obj = os.path.join(OUT, unit + ".o")
+    stamp = obj + ".stamp"
+    with open(src, "rb") as f:
+        key = hashlib.sha256(f.read() + digest.encode() + " ".join(extra).encode()).hexdigest()
+    if os.path.exists(obj) and os.path.exists(stamp) and open(stamp).read() == key:
+        return obj, ""
+    if kind == "nvcc":
+        cmd = [NVCC] + NVCC_COMMON + extra + ["-c", src, "-o", obj]
+    else:
+        cmd = [os.environ.get("CXX", "g++")] + CXX_COMMON + extra + ["-c", src, "-o", obj]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    with open(stamp, "w") as f:
+        f.write(key)
+    return obj, (r.stderr if verbose else "")
+
+
+def build(verbose: bool = False, ptxas_info: bool = False) -> str:
+    """Compile and link the library; returns its path."""
+    if not os.path.exists(NVCC):
+        raise RuntimeError(f"nvcc not found at {NVCC}")
+    os.makedirs(OUT, exist_ok=True)
+    digest = _headers_digest()
+    units = []
+    for unit, kind, extra in UNITS:
+        e = list(extra)
+        if ptxas_info and kind == "nvcc":
+            e += ["-Xptxas", "-v"]
+        units.append((unit, kind, e))
+    with cf.ThreadPoolExecutor(max_workers=len(units)) as ex:
+        futs = [ex.submit(_compile, u, k, e, digest, verbose or ptxas_info) for u, k, e in units]
+        objs = []
+        for f in futs:
+            obj, log = f.result()
+            objs.append(obj)
+            if log:
+                sys.stderr.write(log)
+    newest = max(os.path.getmtime(o) for o in objs)
+    if not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
+        tmp = LIB + ".tmp"
+        cmd = [NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+        shutil.move(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose=True, ptxas_info="--ptxas" in sys.argv))

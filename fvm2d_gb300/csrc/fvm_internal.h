@@ -1,0 +1,157 @@
+// fvm_internal.h -- device data layout shared by the host runtime and the
+// kernels of the GB300 fvm2d hot path.
+//
+// Layout in HBM ("arena"): every mesh of a batch owns contiguous ranges of
+// the vertex, block, block-edge, block-boundary, block-triangle and
+// incidence arrays.  Vertices are renumbered so that each block of at most
+// kBlockVerts consecutive vertices is a compact patch of the mesh graph
+// (recursive BFS bisection).  One CTA processes one block:
+//
+//   gradient pass (green_gauss.f:23-39, tri_visc :132-194):
+//     phase 1  each triangle touching the block -> dxt,dyt (+ viscous terms)
+//              into shared memory, computed once per block
+//     phase 2  each vertex sums its triangles in original triangle order
+//   flux pass (residu.f:37-88 + update.f:17-35):
+//     phase 1  each edge touching the block -> recon + Riemann flux into
+//              shared memory (edges cut by the block boundary are computed
+//              by both blocks: no atomics, no global flux buffer)
+//     phase 2  each vertex sums its edge fluxes in original iedge order,
+//              then solid and farfield contributions in beindx order, then
+//              applies the RK stage and writes the next state buffer.
+//
+// Summation order per vertex equals the Fortran serial order, so the FP64
+// build (no FMA contraction) reproduces the reference arithmetic exactly.
+#pragma once
+
+#include <stdint.h>
+
+namespace fvm {
+
+constexpr int kBlockVerts = 256;      // vertices (and threads) per block
+constexpr int kMaxMeshes = 4096;
+
+// incidence-list entry bits (uint16)
+constexpr uint16_t kSlotMask = 0x1fff;     // slot in the block's list
+constexpr uint16_t kNegBit = 0x8000;       // edge entry: subtract (vertex is n2)
+constexpr uint16_t kSolidBit = 0x4000;     // boundary entry: components 2,3 only
+constexpr uint16_t kFarBit = 0x2000;       // boundary entry: farfield
+constexpr int kTriPosShift = 14;           // triangle entry: vertex position 0..2
+
+// per-vertex flag bits
+constexpr uint8_t kVtxSolid = 1;
+constexpr uint8_t kVtxFarfield = 2;
+
+struct BlockInfo {          // 16 ints, one per CTA
+  int mesh;                 // mesh slot
+  int v0, nv;               // arena vertex range
+  int e0, ne;               // interior edge entries (be_* arrays)
+  int b0, nb;               // boundary edges (bb_* arrays); 2 slots each
+  int t0, nt;               // triangle entries (bt_* arrays)
+  int part;                 // index of this block's partial-sum record
+  int pad[6];
+};
+
+// Per-mesh constants (read-only during a solve).  Mirrors fvm_params plus
+// arena placement.
+struct MeshConst {
+  int iflow, iflux, ilimit, vortex, bugcompat, precision;
+  int v0, nv;                       // vertex range
+  int blk0, nblk;                   // range in the block table
+  int sw0, nsw;                     // solid edges (sw_nodes)
+  int orig123[3];                   // arena ids of driver vertices 1,2,3
+  int pad0;
+  double gamma, gamma1, gas_const, pi, prandtl, prandtl_turb;
+  double albada11, albada12, albada21, albada22, epsilon;
+  double cb1, cb2, sigma_sa, kolm, cw1, cw2, cw3, cv1, cv2;
+  double cv11, cw31, cw32, kolm2, cb2sig1, cb2sig2;
+  double mach_inf, aoa, rey, cfl;
+  double q_inf, r_inf, p_inf, t_inf, u_inf, v_inf, a_inf, sconst, nut_inf;
+  double xref, yref;
+  double airk[3], birk[3];
+  double sin_aoa, cos_aoa;          // host libm values (clcd.f:45-46)
+};
+
+// Per-mesh mutable control block.
+struct MeshCtl {
+  int active;        // 1 while iterating
+  int phase;         // state buffer holding the current solution (0..2)
+  int nphase;        // nut buffer holding the current nu~ (0..1)
+  int iter;          // iteration counter (main.f iter)
+  int iterlast;      // iteration whose residual sets fres1
+  int n_done;        // iterations completed in this iterate call
+  int n_max;         // iterations allowed in this iterate call
+  int err;           // FVM_ERR_* (0 = none)
+  int err_point;     // min driver index (1-based) of a non-positive point
+  int hist_off;      // offset of this mesh's history rows
+  int hist_cap;      // rows available
+  int pad;
+  double minres, fres1, fres, fresi, cl, cd;
+  int iresi, pad2;
+};
+
+struct BlockPartial {       // conres.f:14-22 partials of one block
+  double sumsq;
+  double maxabs;
+  int argmax;               // driver index (1-based); INT_MAX if none
+  int pad;
+};
+
+template <typename R>
+struct alignas(4 * sizeof(R)) R4 {
+  R x, y, z, w;
+};
+template <typename R>
+struct alignas(8 * sizeof(R) > 32 ? 32 : 8 * sizeof(R)) Grad {
+  R qx[4];
+  R qy[4];
+};
+struct alignas(32) D4 {
+  double x, y, z, w;
+};
+
+// Device pointers of an arena (all arena-global indices).
+template <typename R>
+struct ArenaPtrs {
+  // vertices
+  R4<R> *st[3];          // state buffers (rho, u, v, p)
+  Grad<R> *grad;         // qx, qy of the last gradient pass
+  R4<R> *resv;           // viscous residual part (components 1..3 = res 2..4)
+  R4<R> *res;            // residual (per-routine calls)
+  R *dt, *mu, *mul;
+  R *nut[2];
+  const double2 *coord;
+  const double *ais;     // (1/6)/mcarea
+  const double *cvarea, *drmin, *wd;
+  const int *orig;       // driver index (1-based) of each vertex
+  const uint8_t *vflag;
+  // incidence
+  const int *ve_ptr;      // [V+1] absolute offsets into ve_list
+  const uint16_t *ve_list;
+  const int *vt_ptr;
+  const uint16_t *vt_list;
+  // block entries
+  const BlockInfo *blocks;
+  const int2 *be_nodes;   // interior edge entries (n1, n2)
+  const double2 *be_ds;   // ds of the edge (flength.f:38-39)
+  const D4 *be_csl;       // (ct, st, length) precomputed in FP64
+  const int4 *bb_nodes;   // boundary entries (n1, n2, type, -)
+  const int4 *bt_nodes;   // triangle entries (n1, n2, n3, arena triangle)
+  const double *elarea;   // per arena triangle
+  // solid edges per mesh for clcd (n1, n2) in beindx order
+  const int2 *sw_nodes;
+  // all-edge incidence (limitgrad.f loops over netot edges)
+  const int *va_ptr;
+  const int *va_list;     // other vertex | (is n2) << 31
+  // per mesh
+  const MeshConst *mc;
+  MeshCtl *ctl;
+  BlockPartial *part;
+  // history rows
+  double *h_fres, *h_fresi, *h_cl, *h_cd;
+  int *h_iresi;
+  // block work list (indices into blocks[]) and its length
+  const int *work;
+  const int *nwork;
+};
+
+}  // namespace fvm

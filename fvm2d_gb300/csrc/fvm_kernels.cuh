@@ -1,0 +1,872 @@
+// fvm_kernels.cuh -- CUDA kernels of the fvm2d hot path, templated on the
+// state type R.  Included by fvm_kernels_fp64.cu (compiled without FMA
+// contraction) and fvm_kernels_fp32.cu.
+//
+// Every per-block kernel walks the work list (a persistent grid-stride loop
+// over blocks of every active mesh in the arena), skips meshes whose control
+// block is inactive, and picks the state buffers from the mesh's phase:
+//   iterate mode, stage s = 1,2,3 (old = buffer p):
+//     s1: p -> p+1      s2: p+1 -> p+2      s3: p+2 -> p+1   (mod 3)
+//   routine mode (stage 0): state = p, prim_old = p+2, updates in place.
+#pragma once
+
+#include <climits>
+
+#include "fvm_device.cuh"
+
+namespace fvm {
+
+enum { MODE_RESIDUAL = 0, MODE_UPDATE = 1 };
+
+__device__ __forceinline__ int cur_buf(int p, int stage) {
+  return stage <= 1 ? p : (p + stage - 1) % 3;
+}
+__device__ __forceinline__ int out_buf(int p, int stage) {
+  return stage == 2 ? (p + 2) % 3 : (p + 1) % 3;
+}
+__device__ __forceinline__ int old_buf(int p, int stage) {
+  return stage == 0 ? (p + 2) % 3 : p;
+}
+
+template <typename R>
+__device__ __forceinline__ R4<R> ld4(const R4<R> *p) { return *p; }
+
+// ---------------------------------------------------------------------------
+// Viscosity (viscosity.f:2-55) and, at stage 1, the viscous time step
+// (time_step.f:13-20) from the previous mu.  One thread per vertex.
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(kBlockVerts) k_visc(ArenaPtrs<R> A, int stage, int do_dt,
+                                                      int routine) {
+  const int nwork = *A.nwork;
+  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+    const BlockInfo bi = A.blocks[A.work[w]];
+    const MeshCtl &ctl = A.ctl[bi.mesh];
+    if (!routine && !ctl.active) continue;
+    const MeshConst &mc = A.mc[bi.mesh];
+    if (threadIdx.x >= bi.nv) continue;
+    const int v = bi.v0 + threadIdx.x;
+    const R4<R> P = A.st[cur_buf(ctl.phase, stage)][v];
+    if (do_dt) A.dt[v] = time_step<R>(mc, P, A.mu[v], A.drmin[v]);
+    R mul = sutherland_viscosity<R>(mc, P.x, P.w);
+    A.mul[v] = mul;
+    if (mc.iflow == 2) {
+      A.mu[v] = mul;
+    } else {
+      R mut = mu_turb<R>(mc, mul, P.x, A.nut[ctl.nphase][v]);
+      A.mu[v] = mul + mut;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Gradient pass: green_gauss_euler / green_gauss_visc (green_gauss.f:2-92)
+// with tri_gg and tri_visc; at stage 1 of an inviscid iteration also the
+// local time step (time_step.f:22-27).
+// ---------------------------------------------------------------------------
+template <typename R>
+struct TriSmem {
+  R dxt[4];
+  R dyt[4];
+};
+
+template <typename R>
+__global__ void __launch_bounds__(kBlockVerts) k_grad(ArenaPtrs<R> A, int stage, int do_dt,
+                                                      int routine, int max_tri) {
+  extern __shared__ __align__(32) unsigned char smem_raw[];
+  TriSmem<R> *s_tri = reinterpret_cast<TriSmem<R> *>(smem_raw);
+  R *s_vis = reinterpret_cast<R *>(s_tri + max_tri);   // [max_tri][3 pos][3 comp]
+  const int nwork = *A.nwork;
+  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+    const BlockInfo bi = A.blocks[A.work[w]];
+    const MeshCtl &ctl = A.ctl[bi.mesh];
+    if (!routine && !ctl.active) continue;
+    const MeshConst &mc = A.mc[bi.mesh];
+    const bool visc = mc.iflow != 1;
+    const R4<R> *P = A.st[cur_buf(ctl.phase, stage)];
+    // phase 1: one thread per triangle touching the block
+    for (int k = threadIdx.x; k < bi.nt; k += blockDim.x) {
+      const int4 t = A.bt_nodes[bi.t0 + k];
+      const double2 c1 = A.coord[t.x], c2 = A.coord[t.y], c3 = A.coord[t.z];
+      const R4<R> p1 = P[t.x], p2 = P[t.y], p3 = P[t.z];
+      const R dbxx[3] = {R(c2.y - c3.y), R(c3.y - c1.y), R(c1.y - c2.y)};
+      const R dbyy[3] = {R(c3.x - c2.x), R(c1.x - c3.x), R(c2.x - c1.x)};
+      TriSmem<R> ts;
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const R a1 = comp(p1, q), a2 = comp(p2, q), a3 = comp(p3, q);
+        ts.dxt[q] = a1 * dbxx[0] + a2 * dbxx[1] + a3 * dbxx[2];
+        ts.dyt[q] = a1 * dbyy[0] + a2 * dbyy[1] + a3 * dbyy[2];
+      }
+      s_tri[k] = ts;
+      if (visc) {
+        // tri_visc (green_gauss.f:132-194)
+        const R n2b3 = R(2) / R(3);
+        const R en1 = p1.w / p1.x, en2 = p2.w / p2.x, en3 = p3.w / p3.x;
+        const R ext = en1 * dbxx[0] + en2 * dbxx[1] + en3 * dbxx[2];
+        const R eyt = en1 * dbyy[0] + en2 * dbyy[1] + en3 * dbyy[2];
+        const R um = (p1.y + p2.y + p3.y) / R(3);
+        const R vm = (p1.z + p2.z + p3.z) / R(3);
+        const int nb = ctl.nphase;
+        const R mut = (A.mu[t.x] + A.mu[t.y] + A.mu[t.z]) / R(3);
+        const R mult = (A.mul[t.x] + A.mul[t.y] + A.mul[t.z]) / R(3);
+        const R prim5t = (A.nut[nb][t.x] + A.nut[nb][t.y] + A.nut[nb][t.z]) / R(3);
+        const R rhot = (p1.x + p2.x + p3.x) / R(3);
+        const R chi = prim5t * rhot / mult;
+        const R chi3 = cube(chi);
+        const R fv1 = chi3 / (chi3 + R(mc.cv11));
+        const R txx = n2b3 * mut * (R(2) * ts.dxt[1] - ts.dyt[2]);
+        const R txy = mut * (ts.dyt[1] + ts.dxt[2]);
+        const R tyy = n2b3 * mut * (R(2) * ts.dyt[2] - ts.dxt[1]);
+        const R gpr = R(mc.gamma) * (mult / R(mc.prandtl) + rhot * prim5t * fv1 / R(mc.prandtl_turb)) /
+                      R(mc.gamma1);
+        const R efx = txx * um + txy * vm + gpr * ext;
+        const R efy = txy * um + tyy * vm + gpr * eyt;
+        const R areat = R(0.25 / A.elarea[t.w]);
+        R *sv = s_vis + 9 * k;
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+          sv[3 * j + 0] = (txx * dbxx[j] + txy * dbyy[j]) * areat;
+          sv[3 * j + 1] = (txy * dbxx[j] + tyy * dbyy[j]) * areat;
+          sv[3 * j + 2] = (efx * dbxx[j] + efy * dbyy[j]) * areat;
+        }
+      }
+    }
+    __syncthreads();
+    // phase 2: one thread per vertex, triangles in original order
+    if (threadIdx.x < bi.nv) {
+      const int v = bi.v0 + threadIdx.x;
+      R qx[4] = {R(0), R(0), R(0), R(0)}, qy[4] = {R(0), R(0), R(0), R(0)};
+      R rv[3] = {R(0), R(0), R(0)};
+      const int j0 = A.vt_ptr[v], j1 = A.vt_ptr[v + 1];
+      for (int j = j0; j < j1; j++) {
+        const uint16_t e = A.vt_list[j];
+        const int slot = e & 0x3fff;
+        const TriSmem<R> ts = s_tri[slot];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          qx[q] = qx[q] + ts.dxt[q];
+          qy[q] = qy[q] + ts.dyt[q];
+        }
+        if (visc) {
+          const R *sv = s_vis + 9 * slot + 3 * (e >> kTriPosShift);
+          rv[0] = rv[0] + sv[0];
+          rv[1] = rv[1] + sv[1];
+          rv[2] = rv[2] + sv[2];
+        }
+      }
+      const R ais = R(A.ais[v]);
+      Grad<R> g;
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        g.qx[q] = qx[q] * ais;
+        g.qy[q] = qy[q] * ais;
+      }
+      A.grad[v] = g;
+      if (visc) {
+        R4<R> r;
+        r.x = R(0);
+        r.y = rv[0];
+        r.z = rv[1];
+        r.w = rv[2];
+        A.resv[v] = r;
+      } else if (do_dt) {
+        A.dt[v] = time_step<R>(mc, P[v], R(0), A.drmin[v]);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Flux pass: residu.f:37-88 (recon + roe/kfvs/hllc over iedge, solid_flux,
+// farfield_flux) gathered per vertex in Fortran order, then either the
+// residual is written (MODE_RESIDUAL) or the RK stage of update.f:17-35 is
+// applied (MODE_UPDATE).  At stage 3 of an iteration it also produces the
+// conres.f partials and the density/pressure positivity check.
+// ---------------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ void edge_flux(const ArenaPtrs<R> &A, const MeshConst &mc,
+                                          const R4<R> *P, int e, R f[4], int &err) {
+  const int2 nn = A.be_nodes[e];
+  const R4<R> p1 = P[nn.x], p2 = P[nn.y];
+  const Grad<R> g1 = A.grad[nn.x], g2 = A.grad[nn.y];
+  const double2 c1 = A.coord[nn.x], c2 = A.coord[nn.y];
+  const R dx = R(c2.x - c1.x), dy = R(c2.y - c1.y);
+  R pl[4], pr[4];
+  const R a11 = R(mc.albada11), a12 = R(mc.albada12), a21 = R(mc.albada21), a22 = R(mc.albada22);
+  const R eps = R(mc.epsilon);
+#pragma unroll
+  for (int q = 0; q < 4; q++)
+    recon1<R>(comp(p1, q), comp(p2, q), g1.qx[q], g1.qy[q], g2.qx[q], g2.qy[q], dx, dy,
+              mc.ilimit, a11, a12, a21, a22, eps, pl[q], pr[q]);
+  R ct, st, len;
+  if (sizeof(R) == 8) {
+    const D4 csl = A.be_csl[e];
+    ct = R(csl.x);
+    st = R(csl.y);
+    len = R(csl.z);
+  } else {
+    const double2 ds = A.be_ds[e];
+    const R d1 = R(ds.x), d2 = R(ds.y);
+    len = msqrt(d1 * d1 + d2 * d2);
+    ct = d1 / len;
+    st = d2 / len;
+  }
+  if (mc.iflux == 1) {
+    if (!roe_flux<R>(ct, st, len, pl, pr, R(mc.gamma), R(mc.gamma1), f)) err = 1;
+  } else if (mc.iflux == 2) {
+    kfvs_flux<R>(ct, st, len, pl, pr, R(mc.gamma1), R(mc.pi), f);
+  } else {
+    hllc_flux<R>(ct, st, len, pl, pr, R(mc.gamma), R(mc.gamma1), mc.bugcompat ? 0 : 1, f);
+  }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kBlockVerts) k_flux(ArenaPtrs<R> A, int stage, int mode,
+                                                      int irk, int routine) {
+  extern __shared__ __align__(32) unsigned char smem_raw[];
+  R4<R> *s_flux = reinterpret_cast<R4<R> *>(smem_raw);
+  __shared__ double s_red[kBlockVerts / 32];
+  __shared__ double s_max[kBlockVerts / 32];
+  __shared__ int s_arg[kBlockVerts / 32];
+  const int nwork = *A.nwork;
+  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+    const BlockInfo bi = A.blocks[A.work[w]];
+    MeshCtl &ctl = A.ctl[bi.mesh];
+    if (!routine && !ctl.active) continue;
+    const MeshConst &mc = A.mc[bi.mesh];
+    const int p = ctl.phase;
+    const R4<R> *P = A.st[cur_buf(p, stage)];
+    int err = 0;
+    // phase 1a: interior edges
+    for (int k = threadIdx.x; k < bi.ne; k += blockDim.x) {
+      R f[4];
+      edge_flux<R>(A, mc, P, bi.e0 + k, f, err);
+      R4<R> o;
+      o.x = f[0];
+      o.y = f[1];
+      o.z = f[2];
+      o.w = f[3];
+      s_flux[k] = o;
+    }
+    // phase 1b: boundary edges, two slots each (contribution to n1, to n2)
+    for (int k = threadIdx.x; k < bi.nb; k += blockDim.x) {
+      const int4 b = A.bb_nodes[bi.b0 + k];
+      const double2 x1 = A.coord[b.x], x2 = A.coord[b.y];
+      const R4<R> p1 = P[b.x], p2 = P[b.y];
+      R4<R> o1, o2;
+      if (b.z == 1) {
+        // solid_flux.f:10-17
+        const R sx = R(0.5) * R(x2.y - x1.y);
+        const R sy = -R(0.5) * R(x2.x - x1.x);
+        const R pp1 = R(0.75) * p1.w + R(0.25) * p2.w;
+        const R pp2 = R(0.25) * p1.w + R(0.75) * p2.w;
+        o1.x = R(0);
+        o1.y = pp1 * sx;
+        o1.z = pp1 * sy;
+        o1.w = R(0);
+        o2.x = R(0);
+        o2.y = pp2 * sx;
+        o2.z = pp2 * sy;
+        o2.w = R(0);
+      } else {
+        R f1[4], f2[4];
+        farfield_flux<R>(mc, ctl.cl, x1, x2, p1, p2, f1, f2);
+        o1.x = f1[0];
+        o1.y = f1[1];
+        o1.z = f1[2];
+        o1.w = f1[3];
+        o2.x = f2[0];
+        o2.y = f2[1];
+        o2.z = f2[2];
+        o2.w = f2[3];
+      }
+      s_flux[bi.ne + 2 * k] = o1;
+      s_flux[bi.ne + 2 * k + 1] = o2;
+    }
+    if (err) atomicCAS(&ctl.err, 0, 4 /* FVM_ERR_ROE_SONIC */);
+    __syncthreads();
+    // phase 2: gather per vertex in Fortran order
+    double d2 = 0.0, dabs = 0.0;
+    int darg = INT_MAX;
+    if (threadIdx.x < bi.nv) {
+      const int v = bi.v0 + threadIdx.x;
+      R acc[4];
+      if (mc.iflow != 1) {
+        const R4<R> rv = A.resv[v];
+        acc[0] = R(0);
+        acc[1] = rv.y;
+        acc[2] = rv.z;
+        acc[3] = rv.w;
+      } else {
+        acc[0] = acc[1] = acc[2] = acc[3] = R(0);
+      }
+      const int j0 = A.ve_ptr[v], j1 = A.ve_ptr[v + 1];
+      for (int j = j0; j < j1; j++) {
+        const uint16_t e = A.ve_list[j];
+        const R4<R> f = s_flux[e & kSlotMask];
+        if (e & kSolidBit) {
+          acc[1] = acc[1] + f.y;
+          acc[2] = acc[2] + f.z;
+        } else if (e & kNegBit) {
+          acc[0] = acc[0] - f.x;
+          acc[1] = acc[1] - f.y;
+          acc[2] = acc[2] - f.z;
+          acc[3] = acc[3] - f.w;
+        } else {
+          acc[0] = acc[0] + f.x;
+          acc[1] = acc[1] + f.y;
+          acc[2] = acc[2] + f.z;
+          acc[3] = acc[3] + f.w;
+        }
+      }
+      if (mode == MODE_RESIDUAL) {
+        R4<R> r;
+        r.x = acc[0];
+        r.y = acc[1];
+        r.z = acc[2];
+        r.w = acc[3];
+        A.res[v] = r;
+      } else {
+        const R4<R> po = A.st[old_buf(p, stage)][v];
+        const R4<R> pc = P[v];
+        const bool noslip = (mc.iflow != 1) && (A.vflag[v] & kVtxSolid);
+        const R4<R> pn = rk_update<R>(mc, irk, po, pc, A.dt[v], A.cvarea[v], acc, noslip);
+        A.st[out_buf(p, stage)][v] = pn;
+        if (stage == 3) {
+          // conres.f:14-22 partials and check_positivity.f:13-14 (rho, p)
+          const double gra = double(pn.x) - double(po.x);
+          d2 = gra * gra;
+          dabs = fabs(gra);
+          if (dabs > 0.0) darg = A.orig[v];
+          if (pn.x <= R(0) || pn.w <= R(0)) atomicMin(&ctl.err_point, A.orig[v]);
+        }
+      }
+    }
+    if (mode == MODE_UPDATE && stage == 3) {
+      // deterministic block reduction: warp shuffles then warp 0
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        const double o2 = __shfl_down_sync(0xffffffffu, d2, off);
+        const double om = __shfl_down_sync(0xffffffffu, dabs, off);
+        const int oa = __shfl_down_sync(0xffffffffu, darg, off);
+        d2 += o2;
+        if (om > dabs || (om == dabs && oa < darg)) {
+          dabs = om;
+          darg = oa;
+        }
+      }
+      const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+      if (lane == 0) {
+        s_red[wid] = d2;
+        s_max[wid] = dabs;
+        s_arg[wid] = darg;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double s = 0.0, m = 0.0;
+        int a = INT_MAX;
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++) {
+          s += s_red[i];
+          if (s_max[i] > m || (s_max[i] == m && s_arg[i] < a)) {
+            m = s_max[i];
+            a = s_arg[i];
+          }
+        }
+        BlockPartial bp;
+        bp.sumsq = s;
+        bp.maxabs = m;
+        bp.argmax = a;
+        bp.pad = 0;
+        A.part[bi.part] = bp;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Spalart-Allmaras step (sa_model.f:3-201): viscous_sa over triangles,
+// divergence_sa over iedge, outer_flux_sa over farfield edges, then
+// update_sa; nu~ is zero at solid points.  Reads nut[nphase], writes
+// nut[1-nphase].  Uses the state buffer that holds the new solution.
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(kBlockVerts) k_sa(ArenaPtrs<R> A, int stage, int routine,
+                                                    int max_tri) {
+  extern __shared__ __align__(32) unsigned char smem_raw[];
+  R *s_t = reinterpret_cast<R *>(smem_raw);   // [max_tri][3]
+  R *s_e = s_t + 3 * max_tri;                  // [slots]
+  const int nwork = *A.nwork;
+  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+    const BlockInfo bi = A.blocks[A.work[w]];
+    MeshCtl &ctl = A.ctl[bi.mesh];
+    if (!routine && !ctl.active) continue;
+    const MeshConst &mc = A.mc[bi.mesh];
+    if (mc.iflow != 3) continue;
+    // the solution after the RK stages: out of stage 3, or the state itself
+    const int p = ctl.phase;
+    const R4<R> *P = A.st[stage == 3 ? out_buf(p, 3) : p];
+    const R *nut = A.nut[ctl.nphase];
+    R *nut_new = A.nut[1 - ctl.nphase];
+    for (int k = threadIdx.x; k < bi.nt; k += blockDim.x) {
+      const int4 t = A.bt_nodes[bi.t0 + k];
+      const double2 c1 = A.coord[t.x], c2 = A.coord[t.y], c3 = A.coord[t.z];
+      const R areat = R(0.25 / A.elarea[t.w]);
+      const R dbxx[3] = {R(c2.y - c3.y), R(c3.y - c1.y), R(c1.y - c2.y)};
+      const R dbyy[3] = {R(c3.x - c2.x), R(c1.x - c3.x), R(c2.x - c1.x)};
+      int a1 = t.x, a2 = t.y, a3 = t.z;
+      if (mc.bugcompat) {
+        a1 = mc.orig123[0];
+        a2 = mc.orig123[1];
+        a3 = mc.orig123[2];
+      }
+      const R nux = nut[a1] * dbxx[0] + nut[a2] * dbxx[1] + nut[a3] * dbxx[2];
+      const R nuy = nut[a1] * dbyy[0] + nut[a2] * dbyy[1] + nut[a3] * dbyy[2];
+      const R mul1 = A.mul[t.x], mul2 = A.mul[t.y], mul3 = A.mul[t.z];
+      const R n1 = nut[t.x], n2 = nut[t.y], n3 = nut[t.z];
+      const R r1 = P[t.x].x, r2 = P[t.y].x, r3 = P[t.z].x;
+      const R mult = (mul1 + mul2 + mul3) / R(3);
+      const R prim5t = (n1 + n2 + n3) / R(3);
+      const R rhot = (r1 + r2 + r3) / R(3);
+      const R mutb = mult / rhot + prim5t;
+      const R cs1 = R(mc.cb2sig1), cs2 = R(mc.cb2sig2);
+      s_t[3 * k + 0] = (cs1 * mutb - cs2 * (mul1 / r1 + n1)) * (nux * dbxx[0] + nuy * dbyy[0]) * areat;
+      s_t[3 * k + 1] = (cs1 * mutb - cs2 * (mul2 / r2 + n2)) * (nux * dbxx[1] + nuy * dbyy[1]) * areat;
+      s_t[3 * k + 2] = (cs1 * mutb - cs2 * (mul3 / r3 + n3)) * (nux * dbxx[2] + nuy * dbyy[2]) * areat;
+    }
+    for (int k = threadIdx.x; k < bi.ne; k += blockDim.x) {
+      const int e = bi.e0 + k;
+      const int2 nn = A.be_nodes[e];
+      const double2 ds = A.be_ds[e];
+      const R4<R> p1 = P[nn.x], p2 = P[nn.y];
+      const R d1 = R(ds.x), d2 = R(ds.y);
+      const R unl = p1.y * d1 + p1.z * d2;
+      const R unr = p2.y * d1 + p2.z * d2;
+      const R una = R(0.5) * (unl + unr);
+      s_e[k] = (una > R(0)) ? una * nut[nn.x] : una * nut[nn.y];
+    }
+    for (int k = threadIdx.x; k < bi.nb; k += blockDim.x) {
+      const int4 b = A.bb_nodes[bi.b0 + k];
+      R f1 = R(0), f2 = R(0);
+      if (b.z == 2) {
+        const double2 x1 = A.coord[b.x], x2 = A.coord[b.y];
+        const R dx = R(x2.x - x1.x), dy = R(x2.y - x1.y);
+        const R sx = dy, sy = -dx;
+        const R4<R> p1 = P[b.x], p2 = P[b.y];
+        const R u = R(0.5) * (p1.y + p2.y);
+        const R vv = R(0.5) * (p1.z + p2.z);
+        const R un = u * sx + vv * sy;
+        if (un > R(0)) {
+          f1 = un * nut[b.x];
+          f2 = un * nut[b.y];
+        } else {
+          f1 = un * R(mc.nut_inf);
+          f2 = un * R(mc.nut_inf);
+        }
+        f1 = R(0.5) * f1;
+        f2 = R(0.5) * f2;
+      }
+      s_e[bi.ne + 2 * k] = f1;
+      s_e[bi.ne + 2 * k + 1] = f2;
+    }
+    __syncthreads();
+    if (threadIdx.x < bi.nv) {
+      const int v = bi.v0 + threadIdx.x;
+      R divf = R(0);
+      for (int j = A.vt_ptr[v]; j < A.vt_ptr[v + 1]; j++) {
+        const uint16_t e = A.vt_list[j];
+        divf = divf + s_t[3 * (e & 0x3fff) + (e >> kTriPosShift)];
+      }
+      for (int j = A.ve_ptr[v]; j < A.ve_ptr[v + 1]; j++) {
+        const uint16_t e = A.ve_list[j];
+        if (e & kSolidBit) continue;
+        const R f = s_e[e & kSlotMask];
+        divf = (e & kNegBit) ? divf - f : divf + f;
+      }
+      R nn;
+      if (A.vflag[v] & kVtxSolid) {
+        nn = R(0);
+      } else {
+        const Grad<R> g = A.grad[v];
+        const R omega = g.qy[1] - g.qx[2];
+        nn = update_sa<R>(mc, nut[v], P[v].x, A.mul[v], A.wd[v], A.dt[v], A.cvarea[v], divf, omega);
+      }
+      nut_new[v] = nn;
+      if (nn < R(0)) atomicMin(&ctl.err_point, A.orig[v]);
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// End-of-iteration monitor, one CTA per mesh: conres.f (from the block
+// partials), clcd.f, the positivity verdict, RES.DAT history row and the
+// stop test of main.f:42.  FP64 arithmetic; the clcd sum is the serial
+// Fortran chain when serial_clcd is set.
+// ---------------------------------------------------------------------------
+template <typename R>
+__device__ void clcd_block(const ArenaPtrs<R> &A, const MeshConst &mc, int mesh_phase,
+                           int serial, double &cl, double &cd) {
+  __shared__ double s_x[256], s_y[256];
+  const R4<R> *P = A.st[mesh_phase];
+  double xf = 0.0, yf = 0.0;
+  if (serial) {
+    if (threadIdx.x == 0) {
+      for (int i = 0; i < mc.nsw; i++) {
+        const int2 nn = A.sw_nodes[mc.sw0 + i];
+        const double2 c1 = A.coord[nn.x], c2 = A.coord[nn.y];
+        const double dx = c2.x - c1.x, dy = c2.y - c1.y;
+        const double sx = dy, sy = -dx;
+        const double mu1 = double(A.mu[nn.x]), mu2 = double(A.mu[nn.y]);
+        const Grad<R> g1 = A.grad[nn.x], g2 = A.grad[nn.y];
+        const double p1 = double(P[nn.x].w), p2 = double(P[nn.y].w);
+        const double txx1 = 2.0 / 3.0 * mu1 * (2.0 * double(g1.qx[1]) - double(g1.qy[2]));
+        const double txy1 = mu1 * (double(g1.qy[1]) + double(g1.qx[2]));
+        const double tyy1 = 2.0 / 3.0 * mu1 * (2.0 * double(g1.qy[2]) - double(g1.qx[1]));
+        const double txx2 = 2.0 / 3.0 * mu2 * (2.0 * double(g2.qx[1]) - double(g2.qy[2]));
+        const double txy2 = mu2 * (double(g2.qy[1]) + double(g2.qx[2]));
+        const double tyy2 = 2.0 / 3.0 * mu2 * (2.0 * double(g2.qy[2]) - double(g2.qx[1]));
+        const double pp = 0.5 * (p1 + p2);
+        const double txx = 0.5 * (txx1 + txx2);
+        const double txy = 0.5 * (txy1 + txy2);
+        const double tyy = 0.5 * (tyy1 + tyy2);
+        xf = xf + pp * sx - txx * sx - txy * sy;
+        yf = yf + pp * sy - txy * sx - tyy * sy;
+      }
+    }
+  } else {
+    for (int i = threadIdx.x; i < mc.nsw; i += blockDim.x) {
+      const int2 nn = A.sw_nodes[mc.sw0 + i];
+      const double2 c1 = A.coord[nn.x], c2 = A.coord[nn.y];
+      const double dx = c2.x - c1.x, dy = c2.y - c1.y;
+      const double sx = dy, sy = -dx;
+      const double mu1 = double(A.mu[nn.x]), mu2 = double(A.mu[nn.y]);
+      const Grad<R> g1 = A.grad[nn.x], g2 = A.grad[nn.y];
+      const double p1 = double(P[nn.x].w), p2 = double(P[nn.y].w);
+      const double txx = 0.5 * (2.0 / 3.0 * mu1 * (2.0 * double(g1.qx[1]) - double(g1.qy[2])) +
+                                2.0 / 3.0 * mu2 * (2.0 * double(g2.qx[1]) - double(g2.qy[2])));
+      const double txy = 0.5 * (mu1 * (double(g1.qy[1]) + double(g1.qx[2])) +
+                                mu2 * (double(g2.qy[1]) + double(g2.qx[2])));
+      const double tyy = 0.5 * (2.0 / 3.0 * mu1 * (2.0 * double(g1.qy[2]) - double(g1.qx[1])) +
+                                2.0 / 3.0 * mu2 * (2.0 * double(g2.qy[2]) - double(g2.qx[1])));
+      const double pp = 0.5 * (p1 + p2);
+      xf += pp * sx - txx * sx - txy * sy;
+      yf += pp * sy - txy * sx - tyy * sy;
+    }
+    s_x[threadIdx.x] = xf;
+    s_y[threadIdx.x] = yf;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+      if (threadIdx.x < s) {
+        s_x[threadIdx.x] += s_x[threadIdx.x + s];
+        s_y[threadIdx.x] += s_y[threadIdx.x + s];
+      }
+      __syncthreads();
+    }
+    xf = s_x[0];
+    yf = s_y[0];
+  }
+  const double q = 0.5 * mc.r_inf * (mc.q_inf * mc.q_inf);
+  cl = (-mc.sin_aoa * xf + mc.cos_aoa * yf) / q;
+  cd = (mc.cos_aoa * xf + mc.sin_aoa * yf) / q;
+}
+
+template <typename R>
+__device__ void conres_block(const ArenaPtrs<R> &A, const MeshConst &mc, double &sum,
+                             double &mx, int &arg) {
+  __shared__ double s_s[256], s_m[256];
+  __shared__ int s_a[256];
+  double s = 0.0, m = 0.0;
+  int a = INT_MAX;
+  for (int i = threadIdx.x; i < mc.nblk; i += blockDim.x) {
+    const BlockPartial bp = A.part[A.blocks[mc.blk0 + i].part];
+    s += bp.sumsq;
+    if (bp.maxabs > m || (bp.maxabs == m && bp.argmax < a)) {
+      m = bp.maxabs;
+      a = bp.argmax;
+    }
+  }
+  s_s[threadIdx.x] = s;
+  s_m[threadIdx.x] = m;
+  s_a[threadIdx.x] = a;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st) {
+      s_s[threadIdx.x] += s_s[threadIdx.x + st];
+      const double om = s_m[threadIdx.x + st];
+      const int oa = s_a[threadIdx.x + st];
+      if (om > s_m[threadIdx.x] || (om == s_m[threadIdx.x] && oa < s_a[threadIdx.x])) {
+        s_m[threadIdx.x] = om;
+        s_a[threadIdx.x] = oa;
+      }
+    }
+    __syncthreads();
+  }
+  sum = s_s[0];
+  mx = s_m[0];
+  arg = s_a[0];
+}
+
+// One CTA (256 threads) per mesh slot listed in mesh_list.
+template <typename R>
+__global__ void __launch_bounds__(256) k_monitor(ArenaPtrs<R> A, const int *mesh_list,
+                                                 int serial_clcd) {
+  const int m = mesh_list[blockIdx.x];
+  MeshCtl &ctl = A.ctl[m];
+  if (!ctl.active) return;
+  const MeshConst &mc = A.mc[m];
+  double sum, mx;
+  int arg;
+  conres_block<R>(A, mc, sum, mx, arg);
+  const int newp = (ctl.phase + 1) % 3;
+  double cl, cd;
+  clcd_block<R>(A, mc, newp, serial_clcd, cl, cd);
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  ctl.phase = newp;
+  if (mc.iflow == 3) ctl.nphase = 1 - ctl.nphase;
+  if (ctl.err) {                            // roe_flux.f stop, inside residu
+    ctl.active = 0;
+    return;
+  }
+  if (ctl.err_point != INT_MAX) {          // check_positivity.f stop
+    ctl.err = 3;
+    ctl.active = 0;
+    return;
+  }
+  ctl.cl = cl;
+  ctl.cd = cd;
+  double fres = sqrt(sum / double(mc.nv));
+  ctl.fresi = mx;
+  ctl.iresi = (mx > 0.0) ? arg : 0;
+  if (ctl.iter == ctl.iterlast) {
+    ctl.fres1 = fres;
+    if (fres == 0.0) {
+      ctl.fres = fres;
+      ctl.err = 5;
+      ctl.active = 0;
+      return;
+    }
+  }
+  fres = fres / ctl.fres1;
+  ctl.fres = fres;
+  if (ctl.n_done < ctl.hist_cap) {
+    const int row = ctl.hist_off + ctl.n_done;
+    A.h_fres[row] = fres;
+    A.h_iresi[row] = ctl.iresi;
+    A.h_fresi[row] = ctl.fresi;
+    A.h_cl[row] = cl;
+    A.h_cd[row] = cd;
+  }
+  ctl.iter += 1;
+  ctl.n_done += 1;
+  if (fres <= ctl.minres || ctl.n_done >= ctl.n_max) ctl.active = 0;
+}
+
+// ---------------------------------------------------------------------------
+// Per-routine kernels (routine mode: state = buffer p, prim_old = p+2).
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(kBlockVerts) k_update(ArenaPtrs<R> A, int irk) {
+  const int nwork = *A.nwork;
+  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+    const BlockInfo bi = A.blocks[A.work[w]];
+    if (threadIdx.x >= bi.nv) continue;
+    const MeshCtl &ctl = A.ctl[bi.mesh];
+    const MeshConst &mc = A.mc[bi.mesh];
+    const int v = bi.v0 + threadIdx.x;
+    const int p = ctl.phase;
+    const R4<R> r4 = A.res[v];
+    const R res[4] = {r4.x, r4.y, r4.z, r4.w};
+    const bool noslip = (mc.iflow != 1) && (A.vflag[v] & kVtxSolid);
+    A.st[p][v] = rk_update<R>(mc, irk, A.st[(p + 2) % 3][v], A.st[p][v], A.dt[v], A.cvarea[v],
+                              res, noslip);
+  }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kBlockVerts) k_time_step(ArenaPtrs<R> A) {
+  const int nwork = *A.nwork;
+  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+    const BlockInfo bi = A.blocks[A.work[w]];
+    if (threadIdx.x >= bi.nv) continue;
+    const MeshCtl &ctl = A.ctl[bi.mesh];
+    const int v = bi.v0 + threadIdx.x;
+    A.dt[v] = time_step<R>(A.mc[bi.mesh], A.st[ctl.phase][v], A.mu[v], A.drmin[v]);
+  }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kBlockVerts) k_positivity(ArenaPtrs<R> A) {
+  const int nwork = *A.nwork;
+  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+    const BlockInfo bi = A.blocks[A.work[w]];
+    if (threadIdx.x >= bi.nv) continue;
+    MeshCtl &ctl = A.ctl[bi.mesh];
+    const int v = bi.v0 + threadIdx.x;
+    const R4<R> P = A.st[ctl.phase][v];
+    if (P.x <= R(0) || P.w <= R(0) || A.nut[ctl.nphase][v] < R(0))
+      atomicMin(&ctl.err_point, A.orig[v]);
+  }
+}
+
+// conres.f:14-22 partials between buffer p and prim_old = p+2
+template <typename R>
+__global__ void __launch_bounds__(kBlockVerts) k_conres_part(ArenaPtrs<R> A) {
+  __shared__ double s_red[kBlockVerts / 32], s_max[kBlockVerts / 32];
+  __shared__ int s_arg[kBlockVerts / 32];
+  const int nwork = *A.nwork;
+  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+    const BlockInfo bi = A.blocks[A.work[w]];
+    const MeshCtl &ctl = A.ctl[bi.mesh];
+    double d2 = 0.0, dabs = 0.0;
+    int darg = INT_MAX;
+    if (threadIdx.x < bi.nv) {
+      const int v = bi.v0 + threadIdx.x;
+      const double gra = double(A.st[ctl.phase][v].x) - double(A.st[(ctl.phase + 2) % 3][v].x);
+      d2 = gra * gra;
+      dabs = fabs(gra);
+      if (dabs > 0.0) darg = A.orig[v];
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const double o2 = __shfl_down_sync(0xffffffffu, d2, off);
+      const double om = __shfl_down_sync(0xffffffffu, dabs, off);
+      const int oa = __shfl_down_sync(0xffffffffu, darg, off);
+      d2 += o2;
+      if (om > dabs || (om == dabs && oa < darg)) {
+        dabs = om;
+        darg = oa;
+      }
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) {
+      s_red[wid] = d2;
+      s_max[wid] = dabs;
+      s_arg[wid] = darg;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double s = 0.0, m = 0.0;
+      int a = INT_MAX;
+      for (int i = 0; i < (int)(blockDim.x >> 5); i++) {
+        s += s_red[i];
+        if (s_max[i] > m || (s_max[i] == m && s_arg[i] < a)) {
+          m = s_max[i];
+          a = s_arg[i];
+        }
+      }
+      BlockPartial bp;
+      bp.sumsq = s;
+      bp.maxabs = m;
+      bp.argmax = a;
+      bp.pad = 0;
+      A.part[bi.part] = bp;
+    }
+    __syncthreads();
+  }
+}
+
+// conres (first: set fres1) or clcd for one mesh, routine mode.
+template <typename R>
+__global__ void __launch_bounds__(256) k_routine_monitor(ArenaPtrs<R> A, int mesh, int what,
+                                                         int first, int serial_clcd) {
+  MeshCtl &ctl = A.ctl[mesh];
+  const MeshConst &mc = A.mc[mesh];
+  if (what == 0) {
+    double sum, mx;
+    int arg;
+    conres_block<R>(A, mc, sum, mx, arg);
+    if (threadIdx.x != 0) return;
+    double fres = sqrt(sum / double(mc.nv));
+    ctl.fresi = mx;
+    ctl.iresi = (mx > 0.0) ? arg : 0;
+    if (first) {
+      ctl.fres1 = fres;
+      if (fres == 0.0) {
+        ctl.fres = fres;
+        ctl.err = 5;
+        return;
+      }
+    }
+    ctl.fres = fres / ctl.fres1;
+  } else {
+    double cl, cd;
+    clcd_block<R>(A, mc, ctl.phase, serial_clcd, cl, cd);
+    if (threadIdx.x != 0) return;
+    ctl.cl = cl;
+    ctl.cd = cd;
+  }
+}
+
+// limitgrad.f:14-75 on the current gradients, one thread per vertex over
+// all of its edges in edge order.
+template <typename R>
+__global__ void __launch_bounds__(kBlockVerts) k_limitgrad(ArenaPtrs<R> A) {
+  const int nwork = *A.nwork;
+  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+    const BlockInfo bi = A.blocks[A.work[w]];
+    if (threadIdx.x >= bi.nv) continue;
+    const MeshCtl &ctl = A.ctl[bi.mesh];
+    const MeshConst &mc = A.mc[bi.mesh];
+    const int v = bi.v0 + threadIdx.x;
+    const R4<R> *P = A.st[ctl.phase];
+    const R4<R> pv = P[v];
+    const double2 cv = A.coord[v];
+    Grad<R> g = A.grad[v];
+    R qmin[4], qmax[4], phi[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      qmin[q] = R(1.0e10);
+      qmax[q] = R(-1.0e10);
+      phi[q] = R(1);
+    }
+    const int j0 = A.va_ptr[v], j1 = A.va_ptr[v + 1];
+    for (int j = j0; j < j1; j++) {
+      const int o = A.va_list[j] & 0x7fffffff;
+      const R4<R> po = P[o];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        if (!mc.bugcompat) {
+          qmin[q] = dmin1(qmin[q], comp(pv, q));
+          qmax[q] = dmax1(qmax[q], comp(pv, q));
+          qmin[q] = dmin1(qmin[q], comp(po, q));
+          qmax[q] = dmax1(qmax[q], comp(po, q));
+        } else {
+          qmin[q] = dmin1(qmin[q], comp(pv, q));
+          qmax[q] = dmax1(qmax[q], comp(pv, q));
+        }
+      }
+    }
+    for (int j = j0; j < j1; j++) {
+      const int raw = A.va_list[j];
+      const int o = raw & 0x7fffffff;
+      const bool is_n2 = raw < 0;
+      const double2 co = A.coord[o];
+      // dx, dy always from edge(1) to edge(2)
+      const R dx = is_n2 ? R(cv.x - co.x) : R(co.x - cv.x);
+      const R dy = is_n2 ? R(cv.y - co.y) : R(co.y - cv.y);
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        R dq = g.qx[q] * dx + g.qy[q] * dy;
+        if (is_n2) dq = -dq;
+        const R dqmax = qmax[q] - comp(pv, q);
+        const R dqmin = qmin[q] - comp(pv, q);
+        if (dq != R(0)) {
+          const R ppp = (dq > R(0)) ? dqmax / dq : dqmin / dq;
+          phi[q] = dmin1(phi[q], ppp);
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      g.qx[q] = phi[q] * g.qx[q];
+      g.qy[q] = phi[q] * g.qy[q];
+    }
+    A.grad[v] = g;
+  }
+}
+
+}  // namespace fvm

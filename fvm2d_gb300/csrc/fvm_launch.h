@@ -1,0 +1,52 @@
+// fvm_launch.h -- host-callable launchers of the hot-path kernels, one set
+// per state precision (definitions in fvm_kernels_fp64.cu / _fp32.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "fvm_internal.h"
+
+namespace fvm {
+
+constexpr size_t kMaxSmem = 227 * 1024;   // dynamic shared memory per CTA
+
+struct LaunchCfg {
+  int grid;          // CTAs of the per-block kernels (persistent loop)
+  int max_tri;       // max triangle entries of any block
+  int max_slots;     // max edge slots (interior + 2 x boundary) of any block
+  bool viscous;      // any mesh viscous (gradient-pass shared memory)
+  cudaStream_t stream;
+};
+
+#define FVM_DECLARE_LAUNCHERS(R)                                                          \
+  cudaError_t launch_visc(const ArenaPtrs<R> &A, const LaunchCfg &c, int stage, int do_dt, \
+                          int routine);                                                   \
+  cudaError_t launch_grad(const ArenaPtrs<R> &A, const LaunchCfg &c, int stage, int do_dt, \
+                          int routine);                                                   \
+  cudaError_t launch_flux(const ArenaPtrs<R> &A, const LaunchCfg &c, int stage, int mode,  \
+                          int irk, int routine);                                          \
+  cudaError_t launch_sa(const ArenaPtrs<R> &A, const LaunchCfg &c, int stage, int routine);\
+  cudaError_t launch_monitor(const ArenaPtrs<R> &A, const LaunchCfg &c,                    \
+                             const int *mesh_list, int nmesh, int serial_clcd);            \
+  cudaError_t launch_update(const ArenaPtrs<R> &A, const LaunchCfg &c, int irk);           \
+  cudaError_t launch_time_step(const ArenaPtrs<R> &A, const LaunchCfg &c);                 \
+  cudaError_t launch_positivity(const ArenaPtrs<R> &A, const LaunchCfg &c);                \
+  cudaError_t launch_conres(const ArenaPtrs<R> &A, const LaunchCfg &c, int mesh, int first);\
+  cudaError_t launch_clcd(const ArenaPtrs<R> &A, const LaunchCfg &c, int mesh, int serial);\
+  cudaError_t launch_limitgrad(const ArenaPtrs<R> &A, const LaunchCfg &c);                 \
+  size_t smem_grad(const LaunchCfg &c, R *);                                              \
+  size_t smem_flux(const LaunchCfg &c, R *);                                              \
+  size_t smem_sa(const LaunchCfg &c, R *);                                                \
+  cudaError_t prepare_attributes(const LaunchCfg &c, R *);
+
+FVM_DECLARE_LAUNCHERS(double)
+FVM_DECLARE_LAUNCHERS(float)
+
+// set-up kernels (FP64)
+cudaError_t launch_edge_csl(const double2 *ds, D4 *csl, int n, cudaStream_t s);
+cudaError_t launch_dtlength(int np, int nt, const double2 *coord, const int *elem,
+                            const double *elarea, double *drmin, cudaStream_t s);
+cudaError_t launch_wall_dist(int np, int nsedge, const double2 *coord, const int2 *sedge,
+                             const int *ptype, int bugcompat, double *wd, cudaStream_t s);
+
+}  // namespace fvm

@@ -1,0 +1,260 @@
+// fvm_layout.cpp -- vertex renumbering and block tables of one mesh.
+//
+// Renumbering: recursive bisection of the vertex graph.  A part is split by
+// a breadth-first sweep from a pseudo-peripheral vertex (the last vertex
+// reached by a sweep from an arbitrary one); the first ceil(k/2) blocks'
+// worth of vertices in sweep order form one half.  Splits alternate
+// direction by themselves, so the leaves (blocks of <= block_verts
+// vertices, consecutive in the new numbering) are compact patches and few
+// edges cross block boundaries.
+//
+// Block tables: the interior edges of iedge (residu.f:38-66) touching a
+// block, in iedge order; the solid then farfield edges of beindx
+// (residu.f:73-88) touching it; the triangles touching it in triangle
+// order (green_gauss.f:23-31).  Each vertex lists its slots in exactly the
+// order the Fortran loops visit them, so gathering the per-slot values in
+// list order reproduces the serial sums.
+#include "fvm_layout.h"
+
+#include <algorithm>
+#include <cstring>
+
+namespace fvm {
+
+namespace {
+
+struct Bfs {
+  std::vector<int> seen;   // stamp of the last sweep that reached a vertex
+  std::vector<int> inset;  // stamp of the part a vertex belongs to
+  int stamp = 0;
+};
+
+// Breadth-first sweep over the vertices of the current part (inset ==
+// part_stamp) starting at root; visits every component.  Returns order.
+void sweep(const std::vector<int> &adj_ptr, const std::vector<int> &adj,
+           const std::vector<int> &verts, int root, int part_stamp, Bfs &B,
+           std::vector<int> &order) {
+  const int s = ++B.stamp;
+  order.clear();
+  order.reserve(verts.size());
+  size_t head = 0;
+  auto visit_from = [&](int r) {
+    B.seen[r] = s;
+    order.push_back(r);
+    while (head < order.size()) {
+      const int v = order[head++];
+      for (int j = adj_ptr[v]; j < adj_ptr[v + 1]; j++) {
+        const int w = adj[j];
+        if (B.inset[w] == part_stamp && B.seen[w] != s) {
+          B.seen[w] = s;
+          order.push_back(w);
+        }
+      }
+    }
+  };
+  visit_from(root);
+  if (order.size() < verts.size())
+    for (int v : verts)
+      if (B.seen[v] != s) visit_from(v);
+}
+
+void bisect(const std::vector<int> &adj_ptr, const std::vector<int> &adj, std::vector<int> verts,
+            int bv, Bfs &B, std::vector<int> &perm, std::vector<int> &block_start) {
+  // explicit stack to bound recursion depth
+  std::vector<std::vector<int>> stack;
+  stack.push_back(std::move(verts));
+  std::vector<int> order;
+  while (!stack.empty()) {
+    std::vector<int> part = std::move(stack.back());
+    stack.pop_back();
+    const int part_stamp = ++B.stamp;
+    for (int v : part) B.inset[v] = part_stamp;
+    sweep(adj_ptr, adj, part, part[part.size() / 2], part_stamp, B, order);
+    const int root = order.back();
+    sweep(adj_ptr, adj, part, root, part_stamp, B, order);
+    if ((int)part.size() <= bv) {
+      block_start.push_back((int)perm.size());
+      perm.insert(perm.end(), order.begin(), order.end());
+      continue;
+    }
+    const int nblocks = ((int)part.size() + bv - 1) / bv;
+    const size_t nleft = size_t((nblocks + 1) / 2) * bv;
+    std::vector<int> left(order.begin(), order.begin() + nleft);
+    std::vector<int> right(order.begin() + nleft, order.end());
+    // right is processed after left: push right first
+    stack.push_back(std::move(right));
+    stack.push_back(std::move(left));
+  }
+}
+
+}  // namespace
+
+void order_vertices(int np, const std::vector<int> &adj_ptr, const std::vector<int> &adj,
+                    int block_verts, std::vector<int> &perm, std::vector<int> &block_start) {
+  perm.clear();
+  block_start.clear();
+  if (np <= 0) return;
+  Bfs B;
+  B.seen.assign(np, 0);
+  B.inset.assign(np, 0);
+  std::vector<int> all(np);
+  for (int i = 0; i < np; i++) all[i] = i;
+  bisect(adj_ptr, adj, std::move(all), block_verts, B, perm, block_start);
+}
+
+int32_t build_layout(const fvm_mesh &m, int bv, MeshLayout &L) {
+  const int np = m.np, nt = m.nt, netot = m.netot;
+  if (np < 3 || nt < 1 || m.ne < 1 || m.ne > netot) return FVM_ERR_ARG;
+  L = MeshLayout();
+  L.np = np;
+  L.nt = nt;
+  // adjacency over all edges
+  std::vector<int> deg(np + 1, 0);
+  for (int e = 0; e < netot; e++) {
+    const int a = m.edge[2 * e] - 1, b = m.edge[2 * e + 1] - 1;
+    if (a < 0 || a >= np || b < 0 || b >= np || a == b) return FVM_ERR_ARG;
+    deg[a + 1]++;
+    deg[b + 1]++;
+  }
+  for (int i = 0; i < np; i++) deg[i + 1] += deg[i];
+  std::vector<int> adj(deg[np]);
+  {
+    std::vector<int> fill(deg.begin(), deg.end() - 1);
+    for (int e = 0; e < netot; e++) {
+      const int a = m.edge[2 * e] - 1, b = m.edge[2 * e + 1] - 1;
+      adj[fill[a]++] = b;
+      adj[fill[b]++] = a;
+    }
+  }
+  std::vector<int> block_start;
+  order_vertices(np, deg, adj, bv, L.perm, block_start);
+  L.iperm.assign(np, -1);
+  for (int i = 0; i < np; i++) L.iperm[L.perm[i]] = i;
+  const int nblk = (int)block_start.size();
+  L.nblk = nblk;
+  std::vector<int> blk_of(np);
+  L.blocks.assign(nblk, BlockInfo());
+  for (int b = 0; b < nblk; b++) {
+    const int v0 = block_start[b];
+    const int v1 = (b + 1 < nblk) ? block_start[b + 1] : np;
+    std::memset(&L.blocks[b], 0, sizeof(BlockInfo));
+    L.blocks[b].v0 = v0;
+    L.blocks[b].nv = v1 - v0;
+    for (int v = v0; v < v1; v++) blk_of[v] = b;
+  }
+  L.vflag.assign(np, 0);
+  for (int i = 0; i < np; i++) {
+    const int t = m.ptype[i];
+    if (t == FVM_PT_SOLID) L.vflag[L.iperm[i]] |= kVtxSolid;
+    if (t == FVM_PT_FARFIELD) L.vflag[L.iperm[i]] |= kVtxFarfield;
+  }
+  // interior edges, iedge order, per block
+  std::vector<std::vector<int>> bedges(nblk);
+  for (int i = 0; i < m.ne; i++) {
+    const int e = m.iedge[i] - 1;
+    if (e < 0 || e >= netot) return FVM_ERR_ARG;
+    const int a = L.iperm[m.edge[2 * e] - 1], b = L.iperm[m.edge[2 * e + 1] - 1];
+    const int ba = blk_of[a], bb = blk_of[b];
+    bedges[ba].push_back(e);
+    if (bb != ba) bedges[bb].push_back(e);
+  }
+  // boundary edges, beindx order (solid, then farfield)
+  std::vector<std::vector<int4>> bbnd(nblk);
+  auto add_bnd = [&](int pos1, int pos2, int type) -> int32_t {
+    for (int i = pos1; i <= pos2; i++) {
+      const int e = m.beindx[i - 1] - 1;
+      if (e < 0 || e >= netot) return FVM_ERR_ARG;
+      const int a = L.iperm[m.edge[2 * e] - 1], b = L.iperm[m.edge[2 * e + 1] - 1];
+      const int ba = blk_of[a], bb = blk_of[b];
+      bbnd[ba].push_back(make_int4(a, b, type, 0));
+      if (bb != ba) bbnd[bb].push_back(make_int4(a, b, type, 0));
+      if (type == 1) L.sw_nodes.push_back(make_int2(a, b));
+    }
+    return FVM_OK;
+  };
+  if (m.nswe2 >= m.nswe1)
+    if (add_bnd(m.nswe1, m.nswe2, 1)) return FVM_ERR_ARG;
+  if (m.nffe2 >= m.nffe1)
+    if (add_bnd(m.nffe1, m.nffe2, 2)) return FVM_ERR_ARG;
+  // triangles, triangle order, per block
+  std::vector<std::vector<int>> btris(nblk);
+  for (int t = 0; t < nt; t++) {
+    int bl[3];
+    for (int k = 0; k < 3; k++) {
+      const int n = m.elem[3 * t + k] - 1;
+      if (n < 0 || n >= np) return FVM_ERR_ARG;
+      bl[k] = blk_of[L.iperm[n]];
+    }
+    btris[bl[0]].push_back(t);
+    if (bl[1] != bl[0]) btris[bl[1]].push_back(t);
+    if (bl[2] != bl[0] && bl[2] != bl[1]) btris[bl[2]].push_back(t);
+  }
+  // per-vertex lists
+  std::vector<std::vector<uint16_t>> vint(np), vbnd(np), vtri(np);
+  for (int b = 0; b < nblk; b++) {
+    BlockInfo &bi = L.blocks[b];
+    const int v0 = bi.v0, v1 = bi.v0 + bi.nv;
+    auto inblk = [&](int v) { return v >= v0 && v < v1; };
+    bi.e0 = (int)L.be_nodes.size();
+    bi.ne = (int)bedges[b].size();
+    for (int k = 0; k < bi.ne; k++) {
+      const int e = bedges[b][k];
+      const int a = L.iperm[m.edge[2 * e] - 1], c = L.iperm[m.edge[2 * e + 1] - 1];
+      L.be_nodes.push_back(make_int2(a, c));
+      L.be_edge.push_back(e);
+      if (inblk(a)) vint[a].push_back((uint16_t)k);
+      if (inblk(c)) vint[c].push_back((uint16_t)(k | kNegBit));
+    }
+    bi.b0 = (int)L.bb_nodes.size();
+    bi.nb = (int)bbnd[b].size();
+    for (int k = 0; k < bi.nb; k++) {
+      const int4 q = bbnd[b][k];
+      L.bb_nodes.push_back(q);
+      const uint16_t flag = (q.z == 1) ? kSolidBit : kFarBit;
+      if (inblk(q.x)) vbnd[q.x].push_back((uint16_t)((bi.ne + 2 * k) | flag));
+      if (inblk(q.y)) vbnd[q.y].push_back((uint16_t)((bi.ne + 2 * k + 1) | flag));
+    }
+    const int slots = bi.ne + 2 * bi.nb;
+    if (slots > kSlotMask) return FVM_ERR_CAPACITY;
+    L.max_slots = std::max(L.max_slots, slots);
+    bi.t0 = (int)L.bt_nodes.size();
+    bi.nt = (int)btris[b].size();
+    if (bi.nt > 0x3fff) return FVM_ERR_CAPACITY;
+    L.max_tri = std::max(L.max_tri, bi.nt);
+    for (int k = 0; k < bi.nt; k++) {
+      const int t = btris[b][k];
+      int n[3];
+      for (int q = 0; q < 3; q++) n[q] = L.iperm[m.elem[3 * t + q] - 1];
+      L.bt_nodes.push_back(make_int4(n[0], n[1], n[2], t));
+      for (int q = 0; q < 3; q++)
+        if (inblk(n[q])) vtri[n[q]].push_back((uint16_t)(k | (q << kTriPosShift)));
+    }
+  }
+  L.ve_ptr.assign(np + 1, 0);
+  L.vt_ptr.assign(np + 1, 0);
+  for (int v = 0; v < np; v++) {
+    L.ve_ptr[v + 1] = L.ve_ptr[v] + (int)(vint[v].size() + vbnd[v].size());
+    L.vt_ptr[v + 1] = L.vt_ptr[v] + (int)vtri[v].size();
+  }
+  L.ve_list.reserve(L.ve_ptr[np]);
+  L.vt_list.reserve(L.vt_ptr[np]);
+  for (int v = 0; v < np; v++) {
+    L.ve_list.insert(L.ve_list.end(), vint[v].begin(), vint[v].end());
+    L.ve_list.insert(L.ve_list.end(), vbnd[v].begin(), vbnd[v].end());
+    L.vt_list.insert(L.vt_list.end(), vtri[v].begin(), vtri[v].end());
+  }
+  // all-edge incidence in edge order (limitgrad.f:22-68)
+  std::vector<std::vector<int>> vall(np);
+  for (int e = 0; e < netot; e++) {
+    const int a = L.iperm[m.edge[2 * e] - 1], b = L.iperm[m.edge[2 * e + 1] - 1];
+    vall[a].push_back(b);
+    vall[b].push_back(int(uint32_t(a) | 0x80000000u));
+  }
+  L.va_ptr.assign(np + 1, 0);
+  for (int v = 0; v < np; v++) L.va_ptr[v + 1] = L.va_ptr[v] + (int)vall[v].size();
+  L.va_list.reserve(L.va_ptr[np]);
+  for (int v = 0; v < np; v++) L.va_list.insert(L.va_list.end(), vall[v].begin(), vall[v].end());
+  return FVM_OK;
+}
+
+}  // namespace fvm

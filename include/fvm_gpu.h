@@ -1,0 +1,234 @@
+/*
+ * fvm_gpu.h -- C ABI of the GB300 implementation of fvm2d's per-iteration
+ * hot path (cell-vertex, edge-based finite volumes on triangles).
+ *
+ * The reference is one serial Fortran 77 program.  Its hot path is the body
+ * of the iteration loop in src/main.f:44-62:
+ *
+ *     save_old -> time_step -> 3 x { residu -> update } -> [sa_model]
+ *              -> check_positivity -> clcd -> conres
+ *
+ * The routines take arrays by reference and read scalars from COMMON blocks
+ * (src/param.h:36-142, src/gdata.h:1-6).  This header is the drop-in
+ * boundary for that loop: a Fortran driver binds every function below with
+ * ISO_C_BINDING (`bind(C, name="...")`), keeps its own input, grid, geometry
+ * and output path, and calls these entry points in place of the loop body.
+ *
+ * Conventions
+ *   - All functions return int32 status: FVM_OK (0) or an FVM_ERR_* code.
+ *   - Arrays are the Fortran ones, column-major: prim(4,np) is the C array
+ *     double[np][4]; coord(2,np) is double[np][2]; ds(2,netot) is
+ *     double[netot][2]; elem(3,nt), edge(2,netot), edneigh(2,netot) are
+ *     int32[..][3|2].  Connectivity values are 1-based as in Fortran.
+ *   - Host arrays stay owned by the caller and are only read (or written,
+ *     for outputs) during the call.  The library owns all device memory.
+ *   - One handle per host thread; calls are synchronous from the caller's
+ *     point of view; each handle has its own CUDA stream.
+ *   - Errors mirror the reference's `stop` sites; the driver prints and
+ *     stops as before.  fvm_gpu_strerror() gives the text.
+ */
+#ifndef FVM_GPU_H
+#define FVM_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- codes, as in src/param.h:97-142 ---------------------------------- */
+#define FVM_INVISCID   1
+#define FVM_LAMINAR    2
+#define FVM_TURBULENT  3
+
+#define FVM_FLUX_ROE   1
+#define FVM_FLUX_KFVS  2
+#define FVM_FLUX_HLLC  3
+
+#define FVM_CELL_MEDIAN 1
+#define FVM_CELL_BARTH  2
+
+#define FVM_PT_INTERIOR 0
+#define FVM_PT_SOLID    3
+#define FVM_PT_OUTFLOW  4
+#define FVM_PT_FARFIELD 5
+
+/* arithmetic of the state, reconstruction, fluxes and RK stages */
+#define FVM_PREC_FP64  0   /* plain method, FP64 throughout               */
+#define FVM_PREC_FP32  1   /* FP32 state/flux, FP64 geometry and monitors */
+
+/* ---- status codes ------------------------------------------------------ */
+#define FVM_OK                  0
+#define FVM_ERR_ARG             1  /* bad argument / size                       */
+#define FVM_ERR_CUDA            2  /* CUDA runtime error                        */
+#define FVM_ERR_NONPOSITIVE     3  /* check_positivity.f:13-24                  */
+#define FVM_ERR_ROE_SONIC       4  /* roe_flux.f:60-65 (Roe-average a^2 <= 0)   */
+#define FVM_ERR_ZERO_FIRST_RES  5  /* conres.f:28                               */
+#define FVM_ERR_TIMEOUT         6  /* a bounded device wait ran out             */
+#define FVM_ERR_NOMEM           7  /* device allocation failed                  */
+#define FVM_ERR_STATE           8  /* call out of order (e.g. no state set)     */
+#define FVM_ERR_GEOMETRY        9  /* tri_orient.f:28-31, geom_stat.f:18-37,
+                                      flength.f:20-27, areas.f:145-150          */
+#define FVM_ERR_CAPACITY       10  /* a batch arena has no room                 */
+
+/*
+ * Scalars of the COMMON blocks that the hot path reads.  Fill with
+ * fvm_params_init() (which restates src/math.f:8-40 and
+ * src/initialize.f:14-34,52-58) or copy from the driver's COMMON blocks.
+ */
+typedef struct fvm_params {
+  /* switches: /flowtype/ /fluxtype/ /lim/ /farfieldbc/ /celltypes/ */
+  int32_t iflow;        /* FVM_INVISCID | FVM_LAMINAR | FVM_TURBULENT     */
+  int32_t iflux;        /* FVM_FLUX_ROE | FVM_FLUX_KFVS | FVM_FLUX_HLLC   */
+  int32_t ilimit;       /* 0 = unlimited MUSCL, 1 = van Albada limiter    */
+  int32_t vortex;       /* farfield point-vortex correction 0/1           */
+  int32_t cell_type;    /* FVM_CELL_MEDIAN | FVM_CELL_BARTH               */
+  int32_t precision;    /* FVM_PREC_FP64 | FVM_PREC_FP32                  */
+  int32_t bugcompat;    /* 1: reproduce sa_model.f:57-62 (nut(1..3)),
+                           wall_dist.f:46 (dy3 from x) and the
+                           limitgrad.f:26-29 bounds; 0: corrected forms    */
+  int32_t reserved;
+  /* /const/ /viscparam/ (math.f:8-14) */
+  double gamma, gamma1, gas_const, pi;
+  double prandtl, prandtl_turb;
+  /* /lim/ (math.f:16-20), EPSILON (param.h:105) */
+  double albada11, albada12, albada21, albada22, epsilon;
+  /* /samodel/ (math.f:25-40) */
+  double cb1, cb2, sigma_sa, kolm, cw1, cw2, cw3, cv1, cv2;
+  double cv11, cw31, cw32, kolm2, cb2sig1, cb2sig2;
+  /* /itparam/ /inf/ (read_input.f:20-66, initialize.f:14-34) */
+  double mach_inf, aoa_deg, aoa, rey, cfl;
+  double q_inf, r_inf, p_inf, t_inf, u_inf, v_inf, a_inf, sconst, nut_inf;
+  double xref, yref;
+  /* /timeintegration/ (initialize.f:52-58) */
+  double airk[3], birk[3];
+} fvm_params;
+
+/*
+ * Mesh arrays produced by the driver's geometric() (src/geometric.f:15-60).
+ * ne <= netot: the interior-flux loop runs over iedge(1..ne)
+ * (flength.f:84-98 drops zero-length Barth faces).  beindx(nswe1..nswe2)
+ * are the solid edges and beindx(nffe1..nffe2) the farfield edges
+ * (make_bdedges.f:29-44), all 1-based positions.
+ */
+typedef struct fvm_mesh {
+  int32_t np, nt, ne, netot, nsp, nbe;
+  int32_t nswe1, nswe2, nffe1, nffe2;
+  const double  *coord;    /* [np][2]                                     */
+  const int32_t *elem;     /* [nt][3]   counter-clockwise (tri_orient.f)  */
+  const int32_t *ptype;    /* [np]                                        */
+  const int32_t *spts;     /* [nsp]     solid points, ascending           */
+  const int32_t *edge;     /* [netot][2]                                  */
+  const int32_t *iedge;    /* [ne]                                        */
+  const int32_t *beindx;   /* [nbe]                                       */
+  const double  *ds;       /* [netot][2] dual-face normal (flength.f)     */
+  const double  *elarea;   /* [nt]                                        */
+  const double  *cvarea;   /* [np]      control-volume area               */
+  const double  *mcarea;   /* [np]      median-cell area (gradients)      */
+  const double  *drmin;    /* [np]      dtlength.f                        */
+  const double  *wd;       /* [np]      wall distance (turbulent only;
+                                        may be NULL otherwise)            */
+} fvm_mesh;
+
+typedef struct fvm_handle fvm_handle;
+
+/* ---- set-up ------------------------------------------------------------ */
+
+/* Restates math.f:8-40 and initialize.f:14-34,52-58: fills every constant
+ * and freestream value of `p` from the fvm.inp inputs (read_input.f:20-66).
+ * nut_ratio is the freestream nu~/nu of a turbulent start: nut_inf =
+ * nut_ratio*mul_inf/r_inf (initialize.f:69-74 hard-codes 0.1). */
+int32_t fvm_params_init(fvm_params *p, int32_t iflow, double mach_inf,
+                        double aoa_deg, double rey, double cfl,
+                        int32_t iflux, int32_t ilimit, int32_t vortex,
+                        double xref, double yref, int32_t cell_type,
+                        double nut_ratio, int32_t precision,
+                        int32_t bugcompat);
+
+/* Copies params and mesh to the device, reorders vertices for locality,
+ * builds the gather structures and allocates all device state.  Replaces
+ * nothing in the reference (it is the device-side half of geometric.f).
+ * The state is the freestream until fvm_gpu_set_state() is called. */
+int32_t fvm_gpu_create(const fvm_params *params, const fvm_mesh *mesh,
+                       fvm_handle **out);
+int32_t fvm_gpu_destroy(fvm_handle *h);
+const char *fvm_gpu_strerror(int32_t status);
+
+/* State transfer in the driver's vertex order (initialize.f / finalize.f
+ * arrays).  iterlast is the iteration counter of the first iteration to run
+ * (main.f:32); the residual is normalised by the first iteration after a
+ * set_state (conres.f:25-31).  Any pointer except prim may be NULL. */
+int32_t fvm_gpu_set_state(fvm_handle *h, const double *prim,
+                          const double *nut, const double *mul,
+                          const double *mu, int32_t iterlast);
+int32_t fvm_gpu_get_state(fvm_handle *h, double *prim, double *nut,
+                          double *mul, double *mu, double *qx, double *qy);
+
+/* ---- whole iterations: replaces main.f:44-62 ---------------------------- */
+
+/* Runs up to nmax iterations of the loop body, stopping after the first
+ * iteration whose normalised residual is <= minres (main.f:42).  Writes the
+ * RES.DAT columns of every iteration run (main.f:63) to the hist_* arrays
+ * (each of length >= nmax; any may be NULL) and the count to *niter.  On a
+ * positivity failure returns FVM_ERR_NONPOSITIVE with *bad_point set to the
+ * first offending vertex (1-based, check_positivity.f:11-24). */
+int32_t fvm_gpu_iterate(fvm_handle *h, int32_t nmax, double minres,
+                        int32_t *niter, double *hist_fres,
+                        int32_t *hist_iresi, double *hist_fresi,
+                        double *hist_cl, double *hist_cd,
+                        int32_t *bad_point);
+
+/* ---- per-routine entry points (incremental adoption, parity) ----------- */
+int32_t fvm_gpu_save_old(fvm_handle *h);                 /* save_old.f:4-18   */
+int32_t fvm_gpu_time_step(fvm_handle *h);                /* time_step.f:4-37  */
+int32_t fvm_gpu_residu(fvm_handle *h);                   /* residu.f:2-91     */
+int32_t fvm_gpu_update(fvm_handle *h, int32_t irk);      /* update.f:5-38     */
+int32_t fvm_gpu_sa_model(fvm_handle *h);                 /* sa_model.f:3-25   */
+int32_t fvm_gpu_limitgrad(fvm_handle *h);                /* limitgrad.f:1-78  */
+int32_t fvm_gpu_check_positivity(fvm_handle *h,
+                                 int32_t *bad_point);    /* check_positivity.f */
+int32_t fvm_gpu_clcd(fvm_handle *h, double *cl, double *cd);   /* clcd.f:4-49 */
+/* conres.f:3-34; first != 0 sets fres1 from this call (iter == iterlast). */
+int32_t fvm_gpu_conres(fvm_handle *h, int32_t first, double *fres,
+                       double *fresi, int32_t *iresi);
+/* Arrays the per-routine calls produce, in the driver's vertex order. */
+int32_t fvm_gpu_get_residual(fvm_handle *h, double *res);     /* res(4,np) */
+int32_t fvm_gpu_get_dt(fvm_handle *h, double *dt);            /* dt(np)    */
+int32_t fvm_gpu_get_prim_old(fvm_handle *h, double *prim_old);
+
+/* ---- set-up kernels (FP64), each a whole-array pass ---------------------- */
+/* dtlength.f:6-47: drmin(np) = min altitude of the triangles around each
+ * point.  elem is 1-based and counter-clockwise; elarea from tri_area. */
+int32_t fvm_gpu_dtlength(int32_t np, int32_t nt, const double *coord,
+                         const int32_t *elem, const double *elarea,
+                         double *drmin);
+/* wall_dist.f:3-95 (the wd part, lines 16-61 and 87-92): distance from
+ * every point to the nearest solid edge (edges with both ends solid among
+ * edge(1..ne)); wd = 1 at solid points.  bugcompat reproduces line 46. */
+int32_t fvm_gpu_wall_dist(int32_t np, int32_t ne, const double *coord,
+                          const int32_t *edge, const int32_t *ptype,
+                          int32_t bugcompat, double *wd);
+
+/* Driver-side geometry on the host: restates the chain of
+ * src/geometric.f:15-60 (tri_orient, el_surr_point, pt_surr_pt,
+ * create_edge, el_surr_edge, tri_coord, areas, flength, reorder_edges,
+ * make_bdedges, geom_stat) for callers that have no Fortran geometric().
+ * elem is modified in place (orientation, tri_orient.f:33-37).  drmin and
+ * wd are left zero: fill them with fvm_gpu_dtlength / fvm_gpu_wall_dist.
+ * Output arrays are owned by the library; release with fvm_geom_free().
+ * Runs on the host only (no GPU needed). */
+typedef struct fvm_geom {
+  fvm_mesh mesh;            /* points into the arrays below               */
+  int32_t *edge, *edneigh, *iedge, *beindx, *spts;
+  double *ds, *dsb, *elarea, *cvarea, *mcarea, *drmin, *wd;
+} fvm_geom;
+int32_t fvm_geom_build(int32_t np, int32_t nt, const double *coord,
+                       int32_t *elem, const int32_t *ptype,
+                       int32_t cell_type, fvm_geom **out);
+int32_t fvm_geom_free(fvm_geom *g);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FVM_GPU_H */

@@ -1,0 +1,230 @@
+"""FP64 GPU path vs the CPU oracle, through the C ABI.
+
+The FP64 kernels are compiled without FMA contraction and gather every sum
+in the Fortran loop order, so wherever the arithmetic uses only + - * /
+and sqrt the GPU result must equal the oracle bit for bit.  Routines that
+call pow/erf/exp/atan2/sin/cos (Sutherland viscosity, KFVS, the HLLC
+two-rarefaction branch, the farfield vortex, SA) differ from glibc by a
+few ulp; their tolerance is stated where it is used.
+Acceptance for whole iterations: residual history within 1e-10 relative
+after 100 iterations, cl/cd within 1e-8.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+from fvm2d_gb300 import _lib as L  # noqa: E402
+from fvm2d_gb300.ogrid import naca_ogrid, workload_grid  # noqa: E402
+
+TRANSCENDENTAL_RTOL = 1e-12   # few-ulp libm differences, amplified by one residual
+
+
+def make_pair(oracle_lib, fvm_lib, grid, precision=L.FP64, warm=0, **kw):
+    o = oracle_lib.Oracle(grid.coord, grid.elem, grid.ptype, **kw)
+    if warm:
+        st, _ = o.iterate(warm)
+        assert st == 0
+    p = fvm_lib.make_params(precision=precision, **{k: v for k, v in kw.items()})
+    s = fvm_lib.Solver(p, o.mesh_arrays())
+    sc = o.scalars()
+    s.set_state(o.d("prim"), o.d("nut"), o.d("mul"), o.d("mu"), iterlast=sc["iter"])
+    return o, s
+
+
+def rel_err(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    scale = max(np.abs(b).max(), 1e-300)
+    return float(np.abs(a - b).max() / scale)
+
+
+@pytest.fixture(scope="module")
+def grid1():
+    return workload_grid("euler_160x48")
+
+
+@pytest.fixture(scope="module")
+def small():
+    return naca_ogrid(64, 24, radius=20.0, first_spacing=2e-3)
+
+
+@pytest.mark.parametrize("ilimit", [0, 1])
+def test_residu_roe_bitwise(oracle_lib, fvm_lib, grid1, ilimit):
+    o, s = make_pair(oracle_lib, fvm_lib, grid1, warm=5, ilimit=ilimit)
+    o.residu()
+    s.residu()
+    st = s.get_state()
+    np.testing.assert_array_equal(st["qx"], o.d("qx"))
+    np.testing.assert_array_equal(st["qy"], o.d("qy"))
+    np.testing.assert_array_equal(s.residual(), o.d("res"))
+
+
+@pytest.mark.parametrize("iflux", [L.KFVS, L.HLLC])
+def test_residu_kfvs_hllc(oracle_lib, fvm_lib, grid1, iflux):
+    o, s = make_pair(oracle_lib, fvm_lib, grid1, warm=5, iflux=iflux, bugcompat=0)
+    o.residu()
+    s.residu()
+    assert rel_err(s.residual(), o.d("res")) < TRANSCENDENTAL_RTOL
+
+
+def test_hllc_reference_form(oracle_lib, fvm_lib, grid1):
+    """bugcompat=1: the HLLC momentum flux is not rotated back
+    (hllc_flux.f:149-154), on both sides."""
+    o, s = make_pair(oracle_lib, fvm_lib, grid1, iflux=L.HLLC, bugcompat=1)
+    o.residu()
+    s.residu()
+    assert rel_err(s.residual(), o.d("res")) < TRANSCENDENTAL_RTOL
+
+
+def test_routines_bitwise(oracle_lib, fvm_lib, grid1):
+    o, s = make_pair(oracle_lib, fvm_lib, grid1, warm=3)
+    for so, oo in ((s.save_old, o.save_old), (s.time_step, o.time_step)):
+        so()
+        oo()
+    np.testing.assert_array_equal(s.dt(), o.d("dt"))
+    np.testing.assert_array_equal(s.prim_old(), o.d("prim_old"))
+    for irk in (1, 2, 3):
+        o.residu()
+        s.residu()
+        o.update(irk)
+        s.update(irk)
+        np.testing.assert_array_equal(s.get_state()["prim"], o.d("prim"))
+    assert s.check_positivity() == o.check_positivity() == 0
+    cl, cd = s.clcd()
+    ocl, ocd = o.clcd()
+    assert cl == ocl and cd == ocd
+    f, fi, ir = s.conres(first=True)
+    st, of, ofi, oir = o.conres()
+    assert ir == oir and fi == ofi
+    assert abs(f - of) <= 1e-14 * abs(of)
+
+
+def test_iterate_100_fp64(oracle_lib, fvm_lib, grid1):
+    """160x48 NACA 0012, M 0.8, 1.25 deg, Roe + limiter, CFL 1."""
+    o, s = make_pair(oracle_lib, fvm_lib, grid1)
+    st, h = s.iterate(100)
+    ost, oh = o.iterate(100)
+    assert st == 0 and ost == 0
+    assert len(h["fres"]) == 100
+    assert rel_err(h["fres"], oh["fres"]) <= 1e-10
+    np.testing.assert_array_equal(h["iresi"], oh["iresi"])
+    assert abs(h["cl"][-1] - oh["cl"][-1]) <= 1e-8 * max(1.0, abs(oh["cl"][-1]))
+    assert abs(h["cd"][-1] - oh["cd"][-1]) <= 1e-8 * max(1.0, abs(oh["cd"][-1]))
+    np.testing.assert_array_equal(s.get_state()["prim"], o.d("prim"))
+
+
+def test_iterate_minres_stop(oracle_lib, fvm_lib, small):
+    o, s = make_pair(oracle_lib, fvm_lib, small)
+    st, h = s.iterate(400, minres=0.2)
+    ost, oh = o.iterate(400, minres=0.2)
+    assert len(h["fres"]) == len(oh["fres"]) < 400
+    assert h["fres"][-1] <= 0.2
+
+
+@pytest.mark.parametrize("case", ["barth", "vortex", "kfvs", "hllc"])
+def test_iterate_variants(oracle_lib, fvm_lib, small, case):
+    kw = {"barth": dict(cell_type=L.BARTH), "vortex": dict(vortex=1, mach=0.5, aoa_deg=2.0),
+          "kfvs": dict(iflux=L.KFVS), "hllc": dict(iflux=L.HLLC, bugcompat=0)}[case]
+    o, s = make_pair(oracle_lib, fvm_lib, small, **kw)
+    st, h = s.iterate(50)
+    ost, oh = o.iterate(50)
+    assert st == ost == 0
+    tol = 1e-14 if case == "barth" else 1e-9
+    assert rel_err(h["fres"], oh["fres"]) <= max(tol, 1e-10)
+    assert abs(h["cl"][-1] - oh["cl"][-1]) <= 1e-8
+
+
+def test_laminar(oracle_lib, fvm_lib, small):
+    kw = dict(iflow=L.LAMINAR, mach=0.5, aoa_deg=0.0, rey=5000.0, cfl=0.8)
+    o, s = make_pair(oracle_lib, fvm_lib, small, warm=3, **kw)
+    o.residu()
+    s.residu()
+    assert rel_err(s.residual(), o.d("res")) < TRANSCENDENTAL_RTOL
+    st = s.get_state()
+    assert rel_err(st["mu"], o.d("mu")) < 1e-14
+    o2, s2 = make_pair(oracle_lib, fvm_lib, small, **kw)
+    st, h = s2.iterate(50)
+    ost, oh = o2.iterate(50)
+    assert st == ost == 0
+    assert rel_err(h["fres"], oh["fres"]) <= 1e-10
+    assert abs(h["cd"][-1] - oh["cd"][-1]) <= 1e-8
+
+
+@pytest.mark.parametrize("bugcompat", [0, 1])
+def test_turbulent_sa(oracle_lib, fvm_lib, small, bugcompat):
+    kw = dict(iflow=L.TURBULENT, mach=0.7, aoa_deg=2.0, rey=6.5e6, cfl=0.5, nut_ratio=3.0,
+              bugcompat=bugcompat)
+    o, s = make_pair(oracle_lib, fvm_lib, small, warm=2, **kw)
+    o.time_step()
+    s.time_step()
+    o.residu()
+    s.residu()
+    o.sa_model()
+    s.sa_model()
+    assert rel_err(s.get_state()["nut"], o.d("nut")) < 1e-11
+    o2, s2 = make_pair(oracle_lib, fvm_lib, small, **kw)
+    st, h = s2.iterate(30)
+    ost, oh = o2.iterate(30)
+    assert st == ost == 0
+    assert rel_err(h["fres"], oh["fres"]) <= 1e-10
+    assert abs(h["cl"][-1] - oh["cl"][-1]) <= 1e-8
+
+
+def test_setup_kernels_bitwise(oracle_lib, fvm_lib, grid1):
+    o = oracle_lib.Oracle(grid1.coord, grid1.elem, grid1.ptype)
+    m = o.mesh_arrays()
+    dr = fvm_lib.dtlength(m["coord"], m["elem"], m["elarea"])
+    np.testing.assert_array_equal(dr, o.d("drmin"))
+    for bc in (0, 1):
+        wd = fvm_lib.wall_dist(m["coord"], m["edge"], m["ptype"], bc)
+        owd = oracle_lib.wall_dist(m["coord"], m["edge"], m["ptype"], bc)
+        np.testing.assert_array_equal(wd, owd)
+
+
+@pytest.mark.parametrize("bugcompat", [0, 1])
+def test_limitgrad(oracle_lib, fvm_lib, grid1, bugcompat):
+    o, s = make_pair(oracle_lib, fvm_lib, grid1, warm=5, bugcompat=bugcompat)
+    o.residu()
+    s.residu()
+    o.limitgrad()
+    s.limitgrad()
+    st = s.get_state()
+    np.testing.assert_array_equal(st["qx"], o.d("qx"))
+    np.testing.assert_array_equal(st["qy"], o.d("qy"))
+
+
+def test_positivity_stop(oracle_lib, fvm_lib, small):
+    """A non-positive pressure planted in the host state is reported at the
+    first offending point (check_positivity.f:11-24), like the oracle."""
+    o, s = make_pair(oracle_lib, fvm_lib, small)
+    prim = o.d("prim").copy()
+    prim[[100, 37], 3] = -1.0
+    s.set_state(prim, o.d("nut"), o.d("mul"), o.d("mu"))
+    assert s.check_positivity() == 38
+    # the oracle sees the same state and stops the same way
+    o.d("prim")[:] = prim
+    assert o.check_positivity() == 38
+    st, h = s.iterate(5, raise_on_error=False)
+    ost, oh = o.iterate(5)
+    assert st == ost != 0 and len(h["fres"]) == len(oh["fres"]) == 0
+
+
+def test_zero_first_residual(oracle_lib, fvm_lib, small):
+    o, s = make_pair(oracle_lib, fvm_lib, small)
+    s.save_old()
+    with pytest.raises(L.FvmError) as e:
+        s.conres(first=True)
+    assert e.value.status == L.ERR_ZERO_FIRST_RES
+
+
+def test_host_geometry_drives_gpu(oracle_lib, fvm_lib, grid1):
+    """The library's own driver-side geometry (host chain + GPU dtlength)
+    gives the same iteration history as the oracle's geometry."""
+    m = fvm_lib.build_geometry(grid1.coord, grid1.elem, grid1.ptype)
+    p = fvm_lib.make_params()
+    s = fvm_lib.Solver(p, m)
+    o = oracle_lib.Oracle(grid1.coord, grid1.elem, grid1.ptype)
+    st, h = s.iterate(20)
+    ost, oh = o.iterate(20)
+    assert rel_err(h["fres"], oh["fres"]) <= 1e-14
