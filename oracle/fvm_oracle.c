@@ -1484,3 +1484,20 @@ int32_t *orc_iarray(orc_t *o, const char *name, int64_t *len) {
   if (len) *len = 0;
   return NULL;
 }
+
+/* ------------------------------------------------------------------ */
+/* Test hooks: one interior flux or one limiter value in isolation.     */
+/* ------------------------------------------------------------------ */
+int32_t orc_eval_flux(orc_t *o, int32_t iflux, const double *ds, const double *priml,
+                      const double *primr, double *flux) {
+  int32_t err0 = o->s.err;
+  o->s.err = 0;
+  if (iflux == IROE) roe_flux(o, ds, priml, primr, flux);
+  else if (iflux == IKFVS) kfvs_flux(o, ds, priml, primr, flux);
+  else hllc_flux(o, ds, priml, primr, flux);
+  int32_t e = o->s.err;
+  o->s.err = err0;
+  return e;
+}
+
+double orc_limit_albada(double ul, double ur) { return limit_albada(ul, ur); }

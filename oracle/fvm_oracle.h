@@ -104,6 +104,13 @@ void orc_wall_dist(int32_t np, int32_t ne, const double *coord,
                    const int32_t *edge, const int32_t *ptype,
                    int32_t bugcompat, double *wd);
 
+/* Test hooks: the interior flux of one face (roe/kfvs/hllc_flux.f) with
+ * this instance's constants and bugcompat switch; the van Albada limiter
+ * (recon.f:55-71). */
+int32_t orc_eval_flux(orc_t *o, int32_t iflux, const double *ds, const double *priml,
+                      const double *primr, double *flux);
+double orc_limit_albada(double ul, double ur);
+
 #ifdef __cplusplus
 }
 #endif

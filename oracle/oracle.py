@@ -87,6 +87,10 @@ def lib():
         L.orc_iterate.restype = i32
         L.orc_dtlength.argtypes = [i32, i32, pd, pi, pd, pd]
         L.orc_wall_dist.argtypes = [i32, i32, pd, pi, pi, i32, pd]
+        L.orc_eval_flux.argtypes = [vp, i32, pd, pd, pd, pd]
+        L.orc_eval_flux.restype = i32
+        L.orc_limit_albada.argtypes = [dbl, dbl]
+        L.orc_limit_albada.restype = dbl
         _lib = L
     return _lib
 
@@ -197,6 +201,15 @@ class Oracle:
         s = self.scalars()
         return st, s["fres"], s["fresi"], s["iresi"]
 
+    def flux(self, iflux: int, ds, priml, primr):
+        """One interior face flux; returns (status, flux[4])."""
+        ds = np.ascontiguousarray(ds, dtype=np.float64)
+        pl = np.ascontiguousarray(priml, dtype=np.float64)
+        pr = np.ascontiguousarray(primr, dtype=np.float64)
+        out = np.zeros(4)
+        st = lib().orc_eval_flux(self.h, iflux, _dp(ds), _dp(pl), _dp(pr), _dp(out))
+        return st, out
+
     def set_cl(self, cl: float):
         lib().orc_set_cl(self.h, cl)
 
@@ -231,3 +244,7 @@ def wall_dist(coord, edge, ptype, bugcompat=1):
     lib().orc_wall_dist(coord.shape[0], edge.shape[0], _dp(coord), _ip(edge), _ip(ptype),
                         bugcompat, _dp(out))
     return out
+
+
+def limit_albada(ul: float, ur: float) -> float:
+    return lib().orc_limit_albada(ul, ur)

@@ -1,0 +1,143 @@
+"""Pins for the CPU oracle (no GPU).
+
+The reference ships no tests, golden vectors or grids, and cannot be
+compiled here (no Fortran compiler), so the oracle is pinned by answers
+derived from the equations, plus the committed golden fixtures of
+tests/golden/ (which the oracle must keep reproducing):
+  * Roe and KFVS return the exact Euler flux for equal states; so does
+    HLLC once its momentum flux is rotated back (bugcompat=0);
+  * every flux is rotationally invariant;
+  * a uniform freestream gives a zero residual at interior points;
+  * Green-Gauss reproduces linear fields exactly at every point;
+  * the van Albada limiter is 0 on a sign change;
+  * the residual history falls on the 160x48 workload.
+"""
+import numpy as np
+import pytest
+
+from fvm2d_gb300.ogrid import naca_ogrid, workload_grid
+
+
+@pytest.fixture(scope="module")
+def small_grid():
+    return naca_ogrid(64, 24, radius=20.0, first_spacing=2e-3)
+
+
+def euler_flux(prim, ds, gamma=1.4):
+    r, u, v, p = prim
+    length = np.hypot(*ds)
+    nx, ny = ds[0] / length, ds[1] / length
+    un = u * nx + v * ny
+    E = p / (gamma - 1) + 0.5 * r * (u * u + v * v)
+    return np.array([r * un, p * nx + r * u * un, p * ny + r * v * un, (E + p) * un]) * length
+
+
+def random_state(rng):
+    return np.array([rng.uniform(0.5, 2.0), rng.uniform(-1, 1), rng.uniform(-1, 1),
+                     rng.uniform(0.3, 3.0)])
+
+
+@pytest.mark.parametrize("iflux,bugcompat", [(1, 1), (2, 1), (3, 0)])
+def test_flux_consistency(oracle_lib, small_grid, iflux, bugcompat):
+    o = oracle_lib.Oracle(small_grid.coord, small_grid.elem, small_grid.ptype,
+                          bugcompat=bugcompat)
+    rng = np.random.default_rng(1)
+    for _ in range(50):
+        q = random_state(rng)
+        ds = rng.normal(size=2)
+        st, f = o.flux(iflux, ds, q, q)
+        assert st == 0
+        np.testing.assert_allclose(f, euler_flux(q, ds), rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize("iflux,bugcompat", [(1, 1), (2, 1), (3, 0)])
+def test_flux_rotational_invariance(oracle_lib, small_grid, iflux, bugcompat):
+    o = oracle_lib.Oracle(small_grid.coord, small_grid.elem, small_grid.ptype,
+                          bugcompat=bugcompat)
+    rng = np.random.default_rng(2)
+    for _ in range(50):
+        ql, qr = random_state(rng), random_state(rng)
+        ds = rng.normal(size=2)
+        th = rng.uniform(0, 2 * np.pi)
+        c, s = np.cos(th), np.sin(th)
+        R = np.array([[c, -s], [s, c]])
+
+        def rot(q):
+            out = q.copy()
+            out[1:3] = R @ q[1:3]
+            return out
+        _, f = o.flux(iflux, ds, ql, qr)
+        _, fr = o.flux(iflux, R @ ds, rot(ql), rot(qr))
+        np.testing.assert_allclose(fr, rot(f), rtol=1e-10, atol=1e-11)
+
+
+def test_hllc_reference_form_differs(oracle_lib, small_grid):
+    """hllc_flux.f:149-154 returns the normal/tangential momentum flux."""
+    o = oracle_lib.Oracle(small_grid.coord, small_grid.elem, small_grid.ptype, bugcompat=1)
+    q = np.array([1.0, 0.3, 0.4, 1.0])
+    ds = np.array([0.0, 1.0])
+    _, f = o.flux(3, ds, q, q)
+    ex = euler_flux(q, ds)
+    assert np.isclose(f[1], ex[2]) and np.isclose(f[2], -ex[1])
+
+
+@pytest.mark.parametrize("iflux,bugcompat", [(1, 1), (2, 1), (3, 0)])
+def test_freestream_preservation(oracle_lib, small_grid, iflux, bugcompat):
+    o = oracle_lib.Oracle(small_grid.coord, small_grid.elem, small_grid.ptype, iflux=iflux,
+                          bugcompat=bugcompat)
+    o.residu()
+    res = o.d("res")
+    interior = small_grid.ptype == 0
+    scale = np.abs(o.d("ds")).max() * 1.0
+    assert np.abs(res[interior]).max() < 1e-12 * scale
+    assert np.abs(o.d("qx")).max() < 1e-12 and np.abs(o.d("qy")).max() < 1e-12
+
+
+def test_green_gauss_linear(oracle_lib, small_grid):
+    o = oracle_lib.Oracle(small_grid.coord, small_grid.elem, small_grid.ptype)
+    x, y = small_grid.coord[:, 0], small_grid.coord[:, 1]
+    g = np.array([[0.01, -0.02], [0.3, 0.1], [-0.2, 0.05], [0.04, 0.02]])
+    prim = o.d("prim")
+    prim[:] = np.array([1.0, 0.5, 0.1, 0.8])[None, :] + x[:, None] * g[:, 0] + y[:, None] * g[:, 1]
+    o.residu()
+    np.testing.assert_allclose(o.d("qx"), np.broadcast_to(g[:, 0], prim.shape), rtol=1e-9, atol=1e-11)
+    np.testing.assert_allclose(o.d("qy"), np.broadcast_to(g[:, 1], prim.shape), rtol=1e-9, atol=1e-11)
+
+
+def test_limiter(oracle_lib):
+    la = oracle_lib.limit_albada
+    assert la(1.0, -2.0) == 0.0 and la(-1.0, 2.0) == 0.0 and la(0.0, 5.0) == 0.0
+    assert np.isclose(la(1.0, 1.0), 1.0)
+    assert np.isclose(la(2.0, 3.0), la(3.0, 2.0))
+    assert 0 < la(1.0, 3.0) < 3.0
+
+
+def test_residual_history_falls(oracle_lib):
+    g = workload_grid("euler_160x48")
+    o = oracle_lib.Oracle(g.coord, g.elem, g.ptype, mach=0.8, aoa_deg=1.25, cfl=1.0)
+    st, h = o.iterate(150)
+    assert st == 0 and h["fres"][0] == 1.0
+    assert h["fres"][-1] < 0.05
+    assert 0.0 < h["cl"][-1] < 0.6
+
+
+def test_hllc_reference_form_blows_up(oracle_lib):
+    """With the reference HLLC (no rotation back) the 160x48 run stops on a
+    non-positive pressure in its first iteration; the corrected form runs."""
+    g = workload_grid("euler_160x48")
+    o = oracle_lib.Oracle(g.coord, g.elem, g.ptype, iflux=3, bugcompat=1)
+    st, h = o.iterate(5)
+    assert st == 3  # ORC_ERR_NONPOSITIVE
+    o2 = oracle_lib.Oracle(g.coord, g.elem, g.ptype, iflux=3, bugcompat=0)
+    st2, h2 = o2.iterate(5)
+    assert st2 == 0 and len(h2["fres"]) == 5
+
+
+def test_bugcompat_switches_change_results(oracle_lib, small_grid):
+    kw = dict(iflow=3, mach=0.7, aoa_deg=2.0, rey=6.5e6, cfl=0.5, nut_ratio=3.0)
+    a = oracle_lib.Oracle(small_grid.coord, small_grid.elem, small_grid.ptype, bugcompat=1, **kw)
+    b = oracle_lib.Oracle(small_grid.coord, small_grid.elem, small_grid.ptype, bugcompat=0, **kw)
+    assert not np.array_equal(a.d("wd"), b.d("wd"))
+    a.iterate(3)
+    b.iterate(3)
+    assert not np.array_equal(a.d("nut"), b.d("nut"))
