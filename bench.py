@@ -1,0 +1,443 @@
+"""Benchmark of the fvm2d hot path on GB300.
+
+Workload (the large Euler case): NACA 0012 O-grids of 1024 x 384 vertices
+(393,216 vertices, 784,384 triangles, 1,177,600 edges each), interior
+vertices jittered by +-10% of the local spacing from per-mesh seeds,
+M 0.8, AoA 1.25 deg, Roe flux with Green-Gauss MUSCL + van Albada limiter,
+3-stage RK, CFL 1.0, local time stepping, freestream start.  FP32 state,
+reconstruction, fluxes and RK stages; FP64 geometry, residual norm and
+forces.  ``--meshes`` (default 8) independent meshes share one device arena
+and every kernel launch (the batched path), so the working set (about
+1 GB) is far larger than the 129 MB L2: no L2 flush is needed between
+steps.
+
+A step is one full iteration of main.f:44-62 over every mesh of the batch:
+time step, three RK stages (gradients, fluxes, update), monitors.
+value = meshes x vertices x 3 stages x steps / device time of the steps.
+
+Also reported on the same line:
+  e2e           the same solve driven through the C ABI with host buffers:
+                state upload, iterations, RES.DAT rows and final state
+                download all inside the timed region;
+  roofline      the flux kernel (the dominant one): algorithmic bytes per
+                launch / its CUDA-event time, against the measured HBM peak;
+  cpu_baseline  the CPU oracle (the serial FP64 restatement of the
+                reference, single thread) on one mesh of the same workload;
+  vs_fp64_gpu   the plain FP64 single-mesh GPU path on the same workload;
+  fluxes        FP32 batched throughput with KFVS and HLLC.
+``--impl reference`` times the reference's CPU implementation (the oracle
+port; no Fortran compiler exists here) on all host cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = ("vertex-RK-stage updates/s and converged solves/s, p50/p99 latency, vs FP64 GPU")
+UNIT = "vertex-RK-stage updates/s"
+NI, NR = 1024, 384
+FLOW = dict(mach=0.8, aoa_deg=1.25, cfl=1.0, ilimit=1)
+FLUX_CODES = {"roe": 1, "kfvs": 2, "hllc": 3}
+
+
+def grid(seed: int, ni=NI, nr=NR):
+    from fvm2d_gb300.ogrid import naca_ogrid
+    return naca_ogrid(ni, nr, radius=20.0, first_spacing=5e-4, jitter=0.1, seed=seed)
+
+
+def sweep_fu_bytes(np_, ne, s=4, g=8, i=4):
+    """Algorithmic bytes of one flux+update pass over a mesh: reads edge
+    2i and ds 2g per edge; prim 4s, qx/qy 8s, coord 2g, prim_old 4s, dt s,
+    cvarea g per vertex; writes prim 4s per vertex."""
+    return ne * (2 * i + 2 * g) + np_ * (4 * s + 8 * s + 2 * g + 4 * s + s + g + 4 * s)
+
+
+def bytes_per_vertex_stage(np_, nt, ne, s=4, g=8):
+    """P(36s + 19g/3) + 12T + E(8 + 2g), per vertex-stage."""
+    return (np_ * (36 * s + 19 * g / 3) + 12 * nt + ne * (8 + 2 * g)) / np_
+
+
+class ClockSampler:
+    """nvidia-smi sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self._t.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for k, n in enumerate(names):
+                if "Active" in f[5 + k]:
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per flux-kernel launch per mesh from the committed ncu
+    summary (None if absent)."""
+    p = os.path.join(ROOT, "profiles", "flux_fp32_traffic.txt")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        for ln in f:
+            if ln.startswith("dram_bytes_per_launch_per_vertex:"):
+                return float(ln.split(":")[1])
+    return None
+
+
+def build_meshes(nmesh, rank):
+    import fvm2d_gb300 as F
+    from fvm2d_gb300.replicas import seed_for
+    out = []
+    for k in range(nmesh):
+        g = grid(seed_for(rank, k))
+        out.append(F.build_geometry(g.coord, g.elem, g.ptype))
+    return out
+
+
+def run_gpu(args):
+    import torch
+
+    import fvm2d_gb300 as F
+    from fvm2d_gb300 import replicas
+    from fvm2d_gb300.batch import Batch
+
+    replicas.init()
+    rank, local, size = replicas.world()
+    torch.cuda.set_device(local)
+    dev = torch.cuda.current_device()
+    meshes = build_meshes(args.meshes, rank)
+    P, T, E = meshes[0].np, meshes[0].nt, meshes[0].ne
+    V = sum(m.np for m in meshes)
+
+    def make_batch(flux, precision, ms):
+        b = Batch(precision, vertices=sum(m.np for m in ms), meshes=len(ms))
+        par = F.make_params(iflux=flux, precision=precision, bugcompat=0, **FLOW)
+        slots = [b.add(par, m) for m in ms]
+        return b, slots
+
+    # ---- value: FP32 batch, Roe ------------------------------------------
+    b, slots = make_batch(FLUX_CODES[args.flux], F.FP32, meshes)
+    ext = torch.cuda.ExternalStream(b.stream())
+    for s in slots:
+        b.start(s, args.warmup + args.steps + 2)
+    b.step(args.warmup)
+    b.sync()
+    b.timing(True)
+    b.step(1)           # instantiates the timed graph outside the timed region
+    b.sync()
+    b.timing(True)      # resets the per-kernel accumulators
+    n0 = b.launch_count()
+    replicas.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev) as clk:
+        e0.record(ext)
+        b.step(args.steps)
+        e1.record(ext)
+        b.sync()
+        torch.cuda.synchronize()
+    replicas.barrier()
+    launches = b.launch_count() - n0
+    ms_local = e0.elapsed_time(e1)
+    kt = b.timing_read()
+    b.timing(False)
+    ms = replicas.max_over_ranks(ms_local)
+    units = replicas.sum_over_ranks(V * 3 * args.steps)
+    value = units / (ms / 1e3)
+    polls = [b.poll(s) for s in slots]
+    ok = all(p["status"] == 0 for p in polls)
+
+    flux_ms, flux_n = kt["flux"]
+    flux_avg_s = flux_ms / 1e3 / max(flux_n, 1)
+    alg_flux = sum(sweep_fu_bytes(m.np, m.ne) for m in meshes)
+    achieved = alg_flux / flux_avg_s / 1e9
+    peak, peak_kind = measured_peaks()
+    tr = profile_traffic()
+    roofline = {"bound": "hbm", "kernel": "k_flux<float> (recon + Roe flux + gather + RK stage)",
+                "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} hbm_gbs",
+                "traffic": (round(tr * V, 0) if tr is not None else None),
+                "algorithmic_bytes_per_launch": alg_flux,
+                "avg_launch_ms": round(flux_avg_s * 1e3, 4),
+                "kernel_ms_share": {k: round(v[0] / max(sum(x[0] for x in kt.values()), 1e-9), 4)
+                                    for k, v in kt.items() if v[1]}}
+
+    # ---- e2e through the C ABI with host buffers -----------------------------
+    import numpy as np
+    init = []
+    for m in meshes:
+        par = F.make_params(precision=F.FP32, **FLOW)
+        prim = np.tile([par.r_inf, par.u_inf, par.v_inf, par.p_inf], (m.np, 1)).astype(np.float64)
+        init.append(prim)
+    finals = [np.zeros((m.np, 4)) for m in meshes]
+    b.sync()
+    replicas.barrier()
+    t0 = time.perf_counter()
+    for s, prim in zip(slots, init):
+        b.set_state(s, prim)
+        b.start(s, args.steps)
+    rows = 0
+    drained = [0] * len(slots)
+    done_steps = 0
+    depth = 512
+    while done_steps < args.steps:
+        k = min(depth, args.steps - done_steps)
+        b.step(k)
+        done_steps += k
+        for j, s in enumerate(slots):      # RES.DAT rows of this chunk
+            st = b.poll(s)
+            n = st["niter"] - drained[j]
+            if n > 0:
+                rows += len(b.history(s, drained[j], n)["fres"])
+                drained[j] = st["niter"]
+    for s, out in zip(slots, finals):
+        out[:] = b.get_state(s)["prim"]
+    b.sync()
+    e2e_s = replicas.max_over_ranks(time.perf_counter() - t0)
+    e2e_value = replicas.sum_over_ranks(V * 3 * args.steps) / e2e_s
+    h2d = V * 16 + len(slots) * 96 * 2
+    d2h = V * 16 * 3 + rows * 36 + len(slots) * 96 * 3
+    e2e = {"value": e2e_value, "unit": UNIT,
+           "h2d_bytes_per_step": round(h2d / args.steps, 1),
+           "d2h_bytes_per_step": round(d2h / args.steps, 1),
+           "what": "fvm_batch_set_state (host FP64 prim -> pinned -> device) + start + "
+                   "steps + RES.DAT rows + fvm_batch_get_state, wall clock"}
+    b.close()
+
+    extra = {}
+    if rank == 0 and not args.quick:
+        # FP64 plain single-mesh GPU path on the same workload
+        b64, s64 = make_batch(FLUX_CODES[args.flux], F.FP64, meshes[:1])
+        n64 = max(5, args.steps // 20)
+        b64.start(s64[0], n64 + 3)
+        b64.step(2)
+        b64.sync()
+        ext64 = torch.cuda.ExternalStream(b64.stream())
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(ext64)
+        b64.step(n64)
+        f1.record(ext64)
+        b64.sync()
+        v64 = P * 3 * n64 / (f0.elapsed_time(f1) / 1e3)
+        b64.close()
+        extra["vs_fp64_gpu"] = {"value": v64, "unit": UNIT,
+                                "ratio": value / v64 / size,
+                                "what": "FP64 single-mesh path (no FMA contraction), same mesh, "
+                                        f"{n64} iterations"}
+        fl = {}
+        for name in ("kfvs", "hllc"):
+            if name == args.flux:
+                continue
+            bf, sf = make_batch(FLUX_CODES[name], F.FP32, meshes)
+            for s in sf:
+                bf.start(s, args.steps + 10)
+            bf.step(3)
+            bf.sync()
+            extf = torch.cuda.ExternalStream(bf.stream())
+            g0 = torch.cuda.Event(enable_timing=True)
+            g1 = torch.cuda.Event(enable_timing=True)
+            nst = max(10, args.steps // 5)
+            g0.record(extf)
+            bf.step(nst)
+            g1.record(extf)
+            bf.sync()
+            fl[name] = V * 3 * nst / (g0.elapsed_time(g1) / 1e3)
+            bf.close()
+        extra["fluxes"] = fl
+        # CPU oracle, single thread, bounded sample on one mesh of the workload
+        extra["cpu_baseline"] = cpu_baseline(meshes, args)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": size,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32", "data": "synthetic",
+                "config": {"workload": f"naca0012 O-grid {NI}x{NR} jittered +-10%, Euler "
+                                       f"M0.8 AoA1.25, {args.flux} + limiter, RK3, CFL 1",
+                           "meshes_per_gpu": args.meshes, "vertices_per_mesh": P,
+                           "triangles_per_mesh": T, "edges_per_mesh": E,
+                           "arithmetic": "FP32 state/flux/RK; FP64 geometry, norms, forces",
+                           "l2": f"inputs larger than L2 (arena {V} vertices, "
+                                 f"~{bytes_per_vertex_stage(P, T, E) * V / 1e9:.2f} GB "
+                                 "touched per stage > 129 MB L2); no flush",
+                           "parallelism": f"replicas x{size} (no data-path collective)"},
+                "roofline": roofline, "e2e": e2e, "clocks": clk.summary(),
+                "gpu_launches": launches, "all_solves_ok": ok,
+                "bytes_per_vertex_stage": round(bytes_per_vertex_stage(P, T, E), 1)}
+        line.update(extra)
+        print(json.dumps(line), flush=True)
+    replicas.finish()
+
+
+def oracle_rate(nthreads, ni, nr, iters, seeds):
+    """Vertex-stages/s of the oracle, nthreads independent solves at once."""
+    from oracle import oracle
+    grids = [grid(s, ni, nr) for s in seeds[:nthreads]]
+    orcs = [oracle.Oracle(g.coord, g.elem, g.ptype, iflux=1, **FLOW) for g in grids]
+    for o in orcs:
+        o.iterate(1)
+    times = [0.0] * nthreads
+
+    def work(k):
+        t = time.perf_counter()
+        orcs[k].iterate(iters)
+        times[k] = time.perf_counter() - t
+    t0 = time.perf_counter()
+    th = [threading.Thread(target=work, args=(k,)) for k in range(nthreads)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    wall = time.perf_counter() - t0
+    return nthreads * grids[0].np * 3 * iters / wall, wall
+
+
+def cpu_baseline(meshes, args):
+    from oracle import oracle
+    oracle.build()
+    iters = 12
+    rate, wall = oracle_rate(1, NI, NR, iters, [2])
+    return {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{iters} iterations of one {NI}x{NR} mesh of the same workload, "
+                      f"serial FP64 oracle (gcc -O3 -ffp-contract=off), {wall:.1f} s"}
+
+
+def run_reference(args):
+    """The reference's CPU implementation of the path: the oracle port (the
+    Fortran reference cannot be compiled here), one independent solve per
+    host core."""
+    from fvm2d_gb300 import replicas
+    rank, local, size = replicas.world()
+    if size > 1:
+        replicas.init("gloo")
+        if rank != 0:
+            replicas.finish()
+            return
+    from oracle import oracle
+    oracle.build()
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    # each step: one iteration per core on a mesh sized so the run stays short
+    ni, nr = (256, 96) if args.steps + args.warmup > 40 else (512, 192)
+    seeds = list(range(2, 2 + cores))
+    from fvm2d_gb300.ogrid import naca_ogrid
+    grids = [naca_ogrid(ni, nr, radius=20.0, first_spacing=5e-4, jitter=0.1, seed=s)
+             for s in seeds]
+    orcs = [oracle.Oracle(g.coord, g.elem, g.ptype, iflux=FLUX_CODES[args.flux], bugcompat=0,
+                          **FLOW) for g in grids]
+
+    def run_steps(n):
+        def work(k):
+            orcs[k].iterate(n)
+        th = [threading.Thread(target=work, args=(k,)) for k in range(cores)]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+    run_steps(args.warmup)
+    t0 = time.perf_counter()
+    run_steps(args.steps)
+    wall = time.perf_counter() - t0
+    value = cores * grids[0].np * 3 * args.steps / wall
+    sample = (f"{cores} concurrent serial FP64 oracle solves (one per core), {ni}x{nr} jittered "
+              f"O-grid each, same flow and scheme, 1 iteration per step per core")
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": size, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": f"naca0012 O-grid jittered, Euler M0.8 AoA1.25, {args.flux} "
+                                   "+ limiter, RK3, CFL 1", "vertices_per_mesh": grids[0].np,
+                       "parallelism": f"{cores} host threads"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    replicas.finish()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--meshes", type=int, default=8)
+    ap.add_argument("--flux", choices=sorted(FLUX_CODES), default="roe")
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--quick", action="store_true", help="skip the side measurements")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        from fvm2d_gb300 import build
+        build.build()
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

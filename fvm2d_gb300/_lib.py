@@ -57,6 +57,16 @@ class FvmGeom(C.Structure):
                 ("cvarea", _pd), ("mcarea", _pd), ("drmin", _pd), ("wd", _pd)]
 
 
+class FvmBatchCaps(C.Structure):
+    _fields_ = [("vertices", C.c_int64), ("meshes", C.c_int32), ("viscous", C.c_int32),
+                ("blocks", C.c_int64), ("edge_entries", C.c_int64),
+                ("boundary_entries", C.c_int64), ("tri_entries", C.c_int64),
+                ("triangles", C.c_int64), ("edge_incidence", C.c_int64),
+                ("tri_incidence", C.c_int64), ("all_incidence", C.c_int64),
+                ("solid_edges", C.c_int64), ("max_slots", C.c_int32), ("max_tri", C.c_int32),
+                ("grid", C.c_int32), ("reserved", C.c_int32)]
+
+
 # every function the header declares, with its signature
 SIGNATURES = {
     "fvm_params_init": (C.c_int32, [C.POINTER(FvmParams), C.c_int32, C.c_double, C.c_double,
@@ -87,6 +97,25 @@ SIGNATURES = {
     "fvm_geom_build": (C.c_int32, [C.c_int32, C.c_int32, _pd, _pi, _pi, C.c_int32,
                                    C.POINTER(C.POINTER(FvmGeom))]),
     "fvm_geom_free": (C.c_int32, [C.POINTER(FvmGeom)]),
+    "fvm_batch_create": (C.c_int32, [C.c_int32, C.POINTER(FvmBatchCaps), C.POINTER(C.c_void_p)]),
+    "fvm_batch_destroy": (C.c_int32, [C.c_void_p]),
+    "fvm_batch_add": (C.c_int32, [C.c_void_p, C.POINTER(FvmParams), C.POINTER(FvmMesh), _pi]),
+    "fvm_batch_remove": (C.c_int32, [C.c_void_p, C.c_int32]),
+    "fvm_batch_set_state": (C.c_int32, [C.c_void_p, C.c_int32, _pd, _pd, _pd, _pd, C.c_int32]),
+    "fvm_batch_get_state": (C.c_int32, [C.c_void_p, C.c_int32, _pd, _pd, _pd, _pd, _pd, _pd]),
+    "fvm_batch_start": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.c_double]),
+    "fvm_batch_step": (C.c_int32, [C.c_void_p, C.c_int32]),
+    "fvm_batch_sync": (C.c_int32, [C.c_void_p]),
+    "fvm_batch_poll": (C.c_int32, [C.c_void_p, C.c_int32, _pi, _pi, _pd, _pd, _pd, _pi, _pi]),
+    "fvm_batch_history": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, _pd, _pi,
+                                      _pd, _pd, _pd]),
+    "fvm_batch_history_depth": (C.c_int32, []),
+    "fvm_batch_stream": (C.c_void_p, [C.c_void_p]),
+    "fvm_batch_timing": (C.c_int32, [C.c_void_p, C.c_int32]),
+    "fvm_batch_timing_read": (C.c_int32, [C.c_void_p, C.c_int32, C.c_char_p, _pd,
+                                          C.POINTER(C.c_int64), _pi]),
+    "fvm_batch_launch_count": (C.c_int64, [C.c_void_p]),
+    "fvm_layout_stats": (C.c_int32, [C.POINTER(FvmMesh), C.POINTER(C.c_int64)]),
 }
 
 _lib = None

@@ -1,0 +1,137 @@
+"""Python side of the batch C ABI: many meshes resident in one device arena,
+every kernel launched once per iteration for all of them (include/fvm_gpu.h,
+fvm_batch_*).  ``Batch.add`` admits a mesh, ``start`` arms a solve,
+``step`` enqueues iterations of every armed mesh, ``poll`` reports one."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+from ._lib import check, dptr, iptr
+from .solver import MeshArrays
+
+
+def layout_stats(mesh) -> dict:
+    """Block layout of a mesh after renumbering (host only)."""
+    m = mesh if isinstance(mesh, MeshArrays) else MeshArrays(mesh)
+    ms = m.struct()
+    out = (C.c_int64 * 6)()
+    check(L.lib().fvm_layout_stats(C.byref(ms), out), "fvm_layout_stats")
+    keys = ["blocks", "edge_entries", "tri_entries", "max_slots", "max_tri", "boundary_entries"]
+    return dict(zip(keys, [int(x) for x in out]))
+
+
+class Batch:
+    def __init__(self, precision: int, vertices: int, meshes: int, viscous: bool = False,
+                 **caps):
+        c = L.FvmBatchCaps()
+        c.vertices = int(vertices)
+        c.meshes = int(meshes)
+        c.viscous = 1 if viscous else 0
+        for k, v in caps.items():
+            setattr(c, k, int(v))
+        h = C.c_void_p()
+        check(L.lib().fvm_batch_create(precision, C.byref(c), C.byref(h)), "fvm_batch_create")
+        self.h = h
+        self.precision = precision
+        self._meshes = {}
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            L.lib().fvm_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add(self, params: L.FvmParams, mesh) -> int:
+        m = mesh if isinstance(mesh, MeshArrays) else MeshArrays(mesh)
+        ms = m.struct()
+        slot = C.c_int32(-1)
+        check(L.lib().fvm_batch_add(self.h, C.byref(params), C.byref(ms), C.byref(slot)),
+              "fvm_batch_add")
+        self._meshes[slot.value] = m
+        return slot.value
+
+    def try_add(self, params: L.FvmParams, mesh):
+        """add() that returns None when the arena has no room."""
+        try:
+            return self.add(params, mesh)
+        except L.FvmError as e:
+            if e.status == L.ERR_CAPACITY:
+                return None
+            raise
+
+    def remove(self, slot: int):
+        check(L.lib().fvm_batch_remove(self.h, slot), "fvm_batch_remove")
+        self._meshes.pop(slot, None)
+
+    def set_state(self, slot, prim, nut=None, mul=None, mu=None, iterlast=0):
+        prim = np.ascontiguousarray(prim, dtype=np.float64)
+        conv = [None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+                for a in (nut, mul, mu)]
+        check(L.lib().fvm_batch_set_state(self.h, slot, dptr(prim), *[dptr(a) for a in conv],
+                                          iterlast), "fvm_batch_set_state")
+
+    def get_state(self, slot) -> dict:
+        n = self._meshes[slot].np
+        out = {k: np.zeros((n, 4)) for k in ("prim", "qx", "qy")}
+        for k in ("nut", "mul", "mu"):
+            out[k] = np.zeros(n)
+        check(L.lib().fvm_batch_get_state(self.h, slot, dptr(out["prim"]), dptr(out["nut"]),
+                                          dptr(out["mul"]), dptr(out["mu"]), dptr(out["qx"]),
+                                          dptr(out["qy"])), "fvm_batch_get_state")
+        return out
+
+    def start(self, slot, nmax: int, minres: float = 0.0):
+        check(L.lib().fvm_batch_start(self.h, slot, nmax, minres), "fvm_batch_start")
+
+    def step(self, niter: int = 1):
+        check(L.lib().fvm_batch_step(self.h, niter), "fvm_batch_step")
+
+    def sync(self):
+        check(L.lib().fvm_batch_sync(self.h), "fvm_batch_sync")
+
+    def poll(self, slot) -> dict:
+        a, n, st, bad = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
+        f, cl, cd = C.c_double(), C.c_double(), C.c_double()
+        check(L.lib().fvm_batch_poll(self.h, slot, C.byref(a), C.byref(n), C.byref(f),
+                                     C.byref(cl), C.byref(cd), C.byref(st), C.byref(bad)),
+              "fvm_batch_poll")
+        return dict(active=a.value, niter=n.value, fres=f.value, cl=cl.value, cd=cd.value,
+                    status=st.value, bad_point=bad.value)
+
+    def history(self, slot, first: int, count: int) -> dict:
+        h = dict(fres=np.zeros(count), iresi=np.zeros(count, np.int32), fresi=np.zeros(count),
+                 cl=np.zeros(count), cd=np.zeros(count))
+        check(L.lib().fvm_batch_history(self.h, slot, first, count, dptr(h["fres"]),
+                                        iptr(h["iresi"]), dptr(h["fresi"]), dptr(h["cl"]),
+                                        dptr(h["cd"])), "fvm_batch_history")
+        return h
+
+    def stream(self) -> int:
+        return L.lib().fvm_batch_stream(self.h) or 0
+
+    def timing(self, on: bool):
+        check(L.lib().fvm_batch_timing(self.h, 1 if on else 0), "fvm_batch_timing")
+
+    def timing_read(self) -> dict:
+        names = C.create_string_buffer(32 * 8)
+        ms = (C.c_double * 8)()
+        cnt = (C.c_int64 * 8)()
+        n = C.c_int32()
+        check(L.lib().fvm_batch_timing_read(self.h, 8, names, ms, cnt, C.byref(n)),
+              "fvm_batch_timing_read")
+        out = {}
+        for k in range(n.value):
+            nm = names.raw[32 * k:32 * (k + 1)].split(b"\0")[0].decode()
+            out[nm] = (float(ms[k]), int(cnt[k]))
+        return out
+
+    def launch_count(self) -> int:
+        return int(L.lib().fvm_batch_launch_count(self.h))

@@ -38,7 +38,7 @@ UNITS = [
     ("fvm_kernels_fp64.cu", "nvcc", ["--fmad=false"]),
     ("fvm_kernels_fp32.cu", "nvcc", []),
     ("fvm_setup.cu", "nvcc", ["--fmad=false"]),
-    ("fvm_api.cpp", "cxx", []),
+    ("fvm_batch.cpp", "cxx", []),
     ("fvm_layout.cpp", "cxx", []),
     ("fvm_geometry.cpp", "cxx", []),
 ]

@@ -1,0 +1,1297 @@
+// fvm_batch.cpp -- host runtime of include/fvm_gpu.h.
+//
+// A Batch owns one device arena: every array of the hot path sized for a
+// capacity of vertices, block entries, incidence entries and mesh slots,
+// sub-allocated per mesh by first-fit range allocators.  Meshes are
+// admitted (fvm_batch_add) and retired (fvm_batch_remove) between steps;
+// the block work list lives in device memory, so the captured iteration
+// graph never changes.  The single-mesh fvm_gpu_* entry points are a batch
+// of one sized exactly for its mesh.
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <new>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/fvm_gpu.h"
+#include "fvm_internal.h"
+#include "fvm_launch.h"
+#include "fvm_layout.h"
+
+using namespace fvm;
+
+namespace {
+
+constexpr int kHistRows = 512;    // history ring per slot (RES.DAT rows)
+
+// first-fit allocator of index ranges [0, cap)
+class RangeAlloc {
+ public:
+  void init(int64_t cap) {
+    cap_ = cap;
+    free_.clear();
+    if (cap > 0) free_[0] = cap;
+  }
+  int64_t alloc(int64_t n) {   // -1 when no room; n == 0 gives 0
+    if (n <= 0) return 0;
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+      if (it->second >= n) {
+        const int64_t off = it->first, len = it->second;
+        free_.erase(it);
+        if (len > n) free_[off + n] = len - n;
+        return off;
+      }
+    }
+    return -1;
+  }
+  void release(int64_t off, int64_t n) {
+    if (n <= 0) return;
+    auto it = free_.emplace(off, n).first;
+    auto nx = std::next(it);
+    if (nx != free_.end() && it->first + it->second == nx->first) {
+      it->second += nx->second;
+      free_.erase(nx);
+    }
+    if (it != free_.begin()) {
+      auto pv = std::prev(it);
+      if (pv->first + pv->second == it->first) {
+        pv->second += it->second;
+        free_.erase(it);
+      }
+    }
+  }
+  int64_t cap() const { return cap_; }
+
+ private:
+  int64_t cap_ = 0;
+  std::map<int64_t, int64_t> free_;
+};
+
+enum Pool { P_V, P_BLK, P_BE, P_BB, P_BT, P_TRI, P_VE, P_VT, P_VA, P_SW, P_COUNT };
+
+struct Slot {
+  bool used = false;
+  fvm_params par{};
+  MeshLayout L;
+  int64_t off[P_COUNT] = {0};
+  int64_t len[P_COUNT] = {0};
+};
+
+const char *kKernelNames[] = {"visc", "grad", "flux", "sa", "monitor"};
+enum { K_VISC, K_GRAD, K_FLUX, K_SA, K_MON, K_COUNT };
+
+}  // namespace
+
+struct fvm_batch {
+  int prec = FVM_PREC_FP64;
+  size_t rsz = 8;
+  fvm_batch_caps caps{};
+  int64_t cap[P_COUNT] = {0};
+  RangeAlloc pool[P_COUNT];
+  std::vector<Slot> slots;
+  cudaStream_t stream = nullptr;
+  std::vector<void *> owned;
+  // device arrays
+  void *st[3] = {nullptr, nullptr, nullptr};
+  void *grad = nullptr, *resv = nullptr, *res = nullptr;
+  void *dt = nullptr, *mu = nullptr, *mul = nullptr, *nut[2] = {nullptr, nullptr};
+  double2 *coord = nullptr;
+  double *ais = nullptr, *cvarea = nullptr, *drmin = nullptr, *wd = nullptr;
+  int *orig = nullptr;
+  uint8_t *vflag = nullptr;
+  int2 *ve_rng = nullptr, *vt_rng = nullptr, *va_rng = nullptr;
+  uint16_t *ve_list = nullptr, *vt_list = nullptr;
+  int *va_list = nullptr;
+  BlockInfo *blocks = nullptr;
+  int2 *be_nodes = nullptr, *sw_nodes = nullptr;
+  double2 *be_ds = nullptr;
+  D4 *be_csl = nullptr;
+  int4 *bb_nodes = nullptr, *bt_nodes = nullptr;
+  double *elarea = nullptr;
+  MeshConst *mc = nullptr;
+  MeshCtl *ctl = nullptr;
+  BlockPartial *part = nullptr;
+  double *h_fres = nullptr, *h_fresi = nullptr, *h_cl = nullptr, *h_cd = nullptr;
+  int *h_iresi = nullptr;
+  int *work = nullptr, *nwork = nullptr;
+  LaunchCfg cfg{};
+  bool any_turbulent_ok = true;
+  cudaGraphExec_t graph = nullptr;
+  // timing
+  bool timing = false;
+  std::vector<cudaEvent_t> ev;    // pairs around each kernel of an iteration
+  std::vector<int> ev_kind;
+  double t_ms[K_COUNT] = {0};
+  int64_t t_launch[K_COUNT] = {0};
+  int64_t launches = 0;           // kernels launched since creation
+  int kernels_per_iter = 0;
+  unsigned char *pinned = nullptr;   // page-locked staging for state transfers
+  size_t pinned_size = 0;
+  std::string last_error;
+};
+
+namespace {
+
+template <typename T>
+cudaError_t dalloc(std::vector<void *> &owned, T **p, size_t n) {
+  *p = nullptr;
+  if (n == 0) n = 1;
+  void *q = nullptr;
+  cudaError_t e = cudaMalloc(&q, n * sizeof(T));
+  if (e != cudaSuccess) return e;
+  owned.push_back(q);
+  *p = static_cast<T *>(q);
+  return cudaSuccess;
+}
+
+int32_t cuda_status(fvm_batch *b, cudaError_t e) {
+  if (e == cudaSuccess) return FVM_OK;
+  if (b) b->last_error = cudaGetErrorString(e);
+  if (e == cudaErrorMemoryAllocation) return FVM_ERR_NOMEM;
+  return FVM_ERR_CUDA;
+}
+
+#define FVM_TRY(b, expr)                              \
+  do {                                                \
+    cudaError_t _e = (expr);                          \
+    if (_e != cudaSuccess) return cuda_status(b, _e); \
+  } while (0)
+
+template <typename R>
+ArenaPtrs<R> ptrs(const fvm_batch *b) {
+  ArenaPtrs<R> A;
+  std::memset(&A, 0, sizeof(A));
+  for (int i = 0; i < 3; i++) A.st[i] = static_cast<R4<R> *>(b->st[i]);
+  A.grad = static_cast<Grad<R> *>(b->grad);
+  A.resv = static_cast<R4<R> *>(b->resv);
+  A.res = static_cast<R4<R> *>(b->res);
+  A.dt = static_cast<R *>(b->dt);
+  A.mu = static_cast<R *>(b->mu);
+  A.mul = static_cast<R *>(b->mul);
+  A.nut[0] = static_cast<R *>(b->nut[0]);
+  A.nut[1] = static_cast<R *>(b->nut[1]);
+  A.coord = b->coord;
+  A.ais = b->ais;
+  A.cvarea = b->cvarea;
+  A.drmin = b->drmin;
+  A.wd = b->wd;
+  A.orig = b->orig;
+  A.vflag = b->vflag;
+  A.ve_rng = b->ve_rng;
+  A.ve_list = b->ve_list;
+  A.vt_rng = b->vt_rng;
+  A.vt_list = b->vt_list;
+  A.blocks = b->blocks;
+  A.be_nodes = b->be_nodes;
+  A.be_ds = b->be_ds;
+  A.be_csl = b->be_csl;
+  A.bb_nodes = b->bb_nodes;
+  A.bt_nodes = b->bt_nodes;
+  A.elarea = b->elarea;
+  A.sw_nodes = b->sw_nodes;
+  A.va_rng = b->va_rng;
+  A.va_list = b->va_list;
+  A.mc = b->mc;
+  A.ctl = b->ctl;
+  A.part = b->part;
+  A.h_fres = b->h_fres;
+  A.h_fresi = b->h_fresi;
+  A.h_cl = b->h_cl;
+  A.h_cd = b->h_cd;
+  A.h_iresi = b->h_iresi;
+  A.work = b->work;
+  A.nwork = b->nwork;
+  A.nslots = (int)b->slots.size();
+  return A;
+}
+
+MeshConst make_const(const fvm_params &p) {
+  MeshConst c;
+  std::memset(&c, 0, sizeof(c));
+  c.iflow = p.iflow;
+  c.iflux = p.iflux;
+  c.ilimit = p.ilimit;
+  c.vortex = p.vortex;
+  c.bugcompat = p.bugcompat;
+  c.precision = p.precision;
+  c.gamma = p.gamma;
+  c.gamma1 = p.gamma1;
+  c.gas_const = p.gas_const;
+  c.pi = p.pi;
+  c.prandtl = p.prandtl;
+  c.prandtl_turb = p.prandtl_turb;
+  c.albada11 = p.albada11;
+  c.albada12 = p.albada12;
+  c.albada21 = p.albada21;
+  c.albada22 = p.albada22;
+  c.epsilon = p.epsilon;
+  c.cb1 = p.cb1;
+  c.cb2 = p.cb2;
+  c.sigma_sa = p.sigma_sa;
+  c.kolm = p.kolm;
+  c.cw1 = p.cw1;
+  c.cw2 = p.cw2;
+  c.cw3 = p.cw3;
+  c.cv1 = p.cv1;
+  c.cv2 = p.cv2;
+  c.cv11 = p.cv11;
+  c.cw31 = p.cw31;
+  c.cw32 = p.cw32;
+  c.kolm2 = p.kolm2;
+  c.cb2sig1 = p.cb2sig1;
+  c.cb2sig2 = p.cb2sig2;
+  c.mach_inf = p.mach_inf;
+  c.aoa = p.aoa;
+  c.rey = p.rey;
+  c.cfl = p.cfl;
+  c.q_inf = p.q_inf;
+  c.r_inf = p.r_inf;
+  c.p_inf = p.p_inf;
+  c.t_inf = p.t_inf;
+  c.u_inf = p.u_inf;
+  c.v_inf = p.v_inf;
+  c.a_inf = p.a_inf;
+  c.sconst = p.sconst;
+  c.nut_inf = p.nut_inf;
+  c.xref = p.xref;
+  c.yref = p.yref;
+  for (int k = 0; k < 3; k++) {
+    c.airk[k] = p.airk[k];
+    c.birk[k] = p.birk[k];
+  }
+  c.sin_aoa = std::sin(p.aoa);
+  c.cos_aoa = std::cos(p.aoa);
+  return c;
+}
+
+// page-locked staging buffer of at least n bytes
+unsigned char *staging(fvm_batch *b, size_t n, cudaError_t &e) {
+  e = cudaSuccess;
+  if (b->pinned_size < n) {
+    if (b->pinned) cudaFreeHost(b->pinned);
+    b->pinned = nullptr;
+    b->pinned_size = 0;
+    void *p = nullptr;
+    e = cudaMallocHost(&p, n);
+    if (e != cudaSuccess) return nullptr;
+    b->pinned = static_cast<unsigned char *>(p);
+    b->pinned_size = n;
+  }
+  return b->pinned;
+}
+
+int32_t get_ctl(fvm_batch *b, int slot, MeshCtl &c) {
+  FVM_TRY(b, cudaMemcpyAsync(&c, b->ctl + slot, sizeof(MeshCtl), cudaMemcpyDeviceToHost, b->stream));
+  FVM_TRY(b, cudaStreamSynchronize(b->stream));
+  return FVM_OK;
+}
+
+int32_t put_ctl(fvm_batch *b, int slot, const MeshCtl &c) {
+  FVM_TRY(b, cudaMemcpyAsync(b->ctl + slot, &c, sizeof(MeshCtl), cudaMemcpyHostToDevice, b->stream));
+  FVM_TRY(b, cudaStreamSynchronize(b->stream));
+  return FVM_OK;
+}
+
+// host double [np][k] (driver order) -> device [np][k] of the slot
+int32_t put_vertex(fvm_batch *b, const Slot &s, void *dst_base, const double *src, int k,
+                   size_t stride) {
+  const int np = s.L.np;
+  cudaError_t e;
+  unsigned char *buf = staging(b, (size_t)np * stride, e);
+  FVM_TRY(b, e);
+  std::memset(buf, 0, (size_t)np * stride);
+  for (int v = 0; v < np; v++) {
+    const double *q = src + (size_t)s.L.perm[v] * k;
+    unsigned char *d = buf + (size_t)v * stride;
+    for (int c = 0; c < k; c++) {
+      if (b->rsz == 8) {
+        std::memcpy(d + 8 * c, &q[c], 8);
+      } else {
+        const float x = (float)q[c];
+        std::memcpy(d + 4 * c, &x, 4);
+      }
+    }
+  }
+  unsigned char *dst = static_cast<unsigned char *>(dst_base) + (size_t)s.off[P_V] * stride;
+  FVM_TRY(b, cudaMemcpyAsync(dst, buf, (size_t)np * stride, cudaMemcpyHostToDevice, b->stream));
+  FVM_TRY(b, cudaStreamSynchronize(b->stream));
+  return FVM_OK;
+}
+
+int32_t get_vertex(fvm_batch *b, const Slot &s, double *dst, const void *src_base, int k,
+                   size_t stride, int c0 = 0) {
+  const int np = s.L.np;
+  cudaError_t e;
+  unsigned char *buf = staging(b, (size_t)np * stride, e);
+  FVM_TRY(b, e);
+  const unsigned char *src = static_cast<const unsigned char *>(src_base) + (size_t)s.off[P_V] * stride;
+  FVM_TRY(b, cudaMemcpyAsync(buf, src, (size_t)np * stride, cudaMemcpyDeviceToHost, b->stream));
+  FVM_TRY(b, cudaStreamSynchronize(b->stream));
+  for (int v = 0; v < np; v++) {
+    double *d = dst + (size_t)s.L.perm[v] * k;
+    const unsigned char *q = buf + (size_t)v * stride;
+    for (int c = 0; c < k; c++) {
+      if (b->rsz == 8) {
+        std::memcpy(&d[c], q + 8 * (c0 + c), 8);
+      } else {
+        float x;
+        std::memcpy(&x, q + 4 * (c0 + c), 4);
+        d[c] = x;
+      }
+    }
+  }
+  return FVM_OK;
+}
+
+template <typename T>
+cudaError_t put_range(fvm_batch *b, T *base, int64_t off, const std::vector<T> &h) {
+  if (h.empty()) return cudaSuccess;
+  return cudaMemcpyAsync(base + off, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, b->stream);
+}
+
+int32_t update_work(fvm_batch *b) {
+  std::vector<int> work;
+  for (const Slot &s : b->slots)
+    if (s.used)
+      for (int k = 0; k < s.L.nblk; k++) work.push_back((int)(s.off[P_BLK] + k));
+  const int n = (int)work.size();
+  if (n) FVM_TRY(b, cudaMemcpyAsync(b->work, work.data(), n * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+  FVM_TRY(b, cudaMemcpyAsync(b->nwork, &n, sizeof(int), cudaMemcpyHostToDevice, b->stream));
+  FVM_TRY(b, cudaStreamSynchronize(b->stream));
+  return FVM_OK;
+}
+
+// kernels of one iteration, in order; optional timing events around each
+template <typename R>
+int32_t enqueue_iteration(fvm_batch *b, bool with_events) {
+  const ArenaPtrs<R> A = ptrs<R>(b);
+  const LaunchCfg &c = b->cfg;
+  const bool visc = b->caps.viscous != 0;
+  int k = 0;
+  auto mark = [&](int kind) -> cudaError_t {
+    if (!with_events) return cudaSuccess;
+    if ((size_t)(2 * k + 1) >= b->ev.size()) return cudaErrorInvalidValue;
+    b->ev_kind[k] = kind;
+    return cudaEventRecordWithFlags(b->ev[2 * k], b->stream, cudaEventRecordExternal);
+  };
+  auto done = [&]() -> cudaError_t {
+    if (!with_events) {
+      k++;
+      return cudaSuccess;
+    }
+    cudaError_t e = cudaEventRecordWithFlags(b->ev[2 * k + 1], b->stream, cudaEventRecordExternal);
+    k++;
+    return e;
+  };
+  for (int s = 1; s <= 3; s++) {
+    if (visc) {
+      FVM_TRY(b, mark(K_VISC));
+      FVM_TRY(b, launch_visc(A, c, s, s == 1, 0));
+      FVM_TRY(b, done());
+    }
+    FVM_TRY(b, mark(K_GRAD));
+    // inviscid meshes take their time step in the stage-1 gradient pass
+    FVM_TRY(b, launch_grad(A, c, s, s == 1 ? 1 : 0, 0));
+    FVM_TRY(b, done());
+    FVM_TRY(b, mark(K_FLUX));
+    FVM_TRY(b, launch_flux(A, c, s, 1 /*MODE_UPDATE*/, s, 0));
+    FVM_TRY(b, done());
+  }
+  if (visc) {
+    FVM_TRY(b, mark(K_SA));
+    FVM_TRY(b, launch_sa(A, c, 3, 0));
+    FVM_TRY(b, done());
+  }
+  FVM_TRY(b, mark(K_MON));
+  FVM_TRY(b, launch_monitor(A, c, b->prec == FVM_PREC_FP64 ? 1 : 0));
+  FVM_TRY(b, done());
+  b->kernels_per_iter = k;
+  return FVM_OK;
+}
+
+int32_t build_graph(fvm_batch *b) {
+  if (b->graph) return FVM_OK;
+  cudaGraph_t g = nullptr;
+  FVM_TRY(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  int32_t st = b->prec == FVM_PREC_FP64 ? enqueue_iteration<double>(b, b->timing)
+                                        : enqueue_iteration<float>(b, b->timing);
+  cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+  if (st != FVM_OK) {
+    if (g) cudaGraphDestroy(g);
+    return st;
+  }
+  FVM_TRY(b, e);
+  e = cudaGraphInstantiate(&b->graph, g, 0);
+  cudaGraphDestroy(g);
+  FVM_TRY(b, e);
+  return FVM_OK;
+}
+
+Slot *slot_of(fvm_batch *b, int32_t slot) {
+  if (!b || slot < 0 || slot >= (int32_t)b->slots.size() || !b->slots[slot].used) return nullptr;
+  return &b->slots[slot];
+}
+
+void default_caps(fvm_batch_caps &c) {
+  const int64_t V = std::max<int64_t>(c.vertices, 1024);
+  const int64_t M = std::max<int32_t>(c.meshes, 1);
+  if (!c.blocks) c.blocks = V / 128 + 4 * M + 16;
+  if (!c.edge_entries) c.edge_entries = 4 * V + 4096 * M;
+  if (!c.boundary_entries) c.boundary_entries = V / 8 + 256 * M;
+  if (!c.tri_entries) c.tri_entries = 3 * V + 4096 * M;
+  if (!c.triangles) c.triangles = 2 * V + 64 * M;
+  if (!c.edge_incidence) c.edge_incidence = 7 * V + 1024 * M;
+  if (!c.tri_incidence) c.tri_incidence = 7 * V + 1024 * M;
+  if (!c.all_incidence) c.all_incidence = 7 * V + 1024 * M;
+  if (!c.solid_edges) c.solid_edges = V / 8 + 256 * M;
+  if (!c.max_slots) c.max_slots = 1536;
+  if (!c.max_tri) c.max_tri = 1024;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// batch API
+// ---------------------------------------------------------------------------
+extern "C" int32_t fvm_batch_history_depth(void) { return kHistRows; }
+
+extern "C" int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *caps_in,
+                                    fvm_batch **out) {
+  if (!caps_in || !out) return FVM_ERR_ARG;
+  if (precision != FVM_PREC_FP64 && precision != FVM_PREC_FP32) return FVM_ERR_ARG;
+  if (caps_in->vertices <= 0 || caps_in->meshes <= 0 || caps_in->meshes > kMaxMeshes)
+    return FVM_ERR_ARG;
+  *out = nullptr;
+  fvm_batch *b = new (std::nothrow) fvm_batch();
+  if (!b) return FVM_ERR_NOMEM;
+  b->prec = precision;
+  b->rsz = precision == FVM_PREC_FP64 ? 8 : 4;
+  b->caps = *caps_in;
+  default_caps(b->caps);
+  const fvm_batch_caps &c = b->caps;
+  if (c.max_slots > (int)kSlotMask || c.max_tri > 0x3fff || c.vertices > INT_MAX / 8) {
+    delete b;
+    return FVM_ERR_ARG;
+  }
+  const int64_t caps[P_COUNT] = {c.vertices, c.blocks, c.edge_entries, c.boundary_entries,
+                                 c.tri_entries, c.triangles, c.edge_incidence,
+                                 c.tri_incidence, c.all_incidence, c.solid_edges};
+  for (int i = 0; i < P_COUNT; i++) {
+    if (caps[i] > INT_MAX) {
+      delete b;
+      return FVM_ERR_ARG;
+    }
+    b->cap[i] = caps[i];
+    b->pool[i].init(caps[i]);
+  }
+  b->slots.resize(c.meshes);
+  auto fail = [&](int32_t st) {
+    fvm_batch_destroy(b);
+    return st;
+  };
+#define TRYB(expr)                                           \
+  do {                                                       \
+    cudaError_t _e = (expr);                                 \
+    if (_e != cudaSuccess) return fail(cuda_status(b, _e));  \
+  } while (0)
+  TRYB(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+  auto &O = b->owned;
+  const size_t V = (size_t)c.vertices, r = b->rsz;
+  for (int i = 0; i < 3; i++) TRYB(dalloc(O, (unsigned char **)&b->st[i], 4 * r * V));
+  TRYB(dalloc(O, (unsigned char **)&b->grad, 8 * r * V));
+  TRYB(dalloc(O, (unsigned char **)&b->resv, 4 * r * V));
+  TRYB(dalloc(O, (unsigned char **)&b->res, 4 * r * V));
+  TRYB(dalloc(O, (unsigned char **)&b->dt, r * V));
+  TRYB(dalloc(O, (unsigned char **)&b->mu, r * V));
+  TRYB(dalloc(O, (unsigned char **)&b->mul, r * V));
+  TRYB(dalloc(O, (unsigned char **)&b->nut[0], r * V));
+  TRYB(dalloc(O, (unsigned char **)&b->nut[1], r * V));
+  TRYB(dalloc(O, &b->coord, V));
+  TRYB(dalloc(O, &b->ais, V));
+  TRYB(dalloc(O, &b->cvarea, V));
+  TRYB(dalloc(O, &b->drmin, V));
+  TRYB(dalloc(O, &b->wd, V));
+  TRYB(dalloc(O, &b->orig, V));
+  TRYB(dalloc(O, &b->vflag, V));
+  TRYB(dalloc(O, &b->ve_rng, V));
+  TRYB(dalloc(O, &b->vt_rng, V));
+  TRYB(dalloc(O, &b->va_rng, V));
+  TRYB(dalloc(O, &b->ve_list, (size_t)c.edge_incidence));
+  TRYB(dalloc(O, &b->vt_list, (size_t)c.tri_incidence));
+  TRYB(dalloc(O, &b->va_list, (size_t)c.all_incidence));
+  TRYB(dalloc(O, &b->blocks, (size_t)c.blocks));
+  TRYB(dalloc(O, &b->part, (size_t)c.blocks));
+  TRYB(dalloc(O, &b->work, (size_t)c.blocks));
+  TRYB(dalloc(O, &b->nwork, 1));
+  TRYB(dalloc(O, &b->be_nodes, (size_t)c.edge_entries));
+  TRYB(dalloc(O, &b->be_ds, (size_t)c.edge_entries));
+  if (precision == FVM_PREC_FP64) TRYB(dalloc(O, &b->be_csl, (size_t)c.edge_entries));
+  TRYB(dalloc(O, &b->bb_nodes, (size_t)c.boundary_entries));
+  TRYB(dalloc(O, &b->bt_nodes, (size_t)c.tri_entries));
+  TRYB(dalloc(O, &b->elarea, (size_t)c.triangles));
+  TRYB(dalloc(O, &b->sw_nodes, (size_t)c.solid_edges));
+  TRYB(dalloc(O, &b->mc, (size_t)c.meshes));
+  TRYB(dalloc(O, &b->ctl, (size_t)c.meshes));
+  const size_t H = (size_t)c.meshes * kHistRows;
+  TRYB(dalloc(O, &b->h_fres, H));
+  TRYB(dalloc(O, &b->h_fresi, H));
+  TRYB(dalloc(O, &b->h_cl, H));
+  TRYB(dalloc(O, &b->h_cd, H));
+  TRYB(dalloc(O, &b->h_iresi, H));
+  TRYB(cudaMemsetAsync(b->ctl, 0, sizeof(MeshCtl) * c.meshes, b->stream));
+  TRYB(cudaMemsetAsync(b->nwork, 0, sizeof(int), b->stream));
+  TRYB(cudaMemsetAsync(b->grad, 0, 8 * r * V, b->stream));
+  TRYB(cudaMemsetAsync(b->resv, 0, 4 * r * V, b->stream));
+  TRYB(cudaStreamSynchronize(b->stream));
+#undef TRYB
+  b->cfg.max_slots = c.max_slots;
+  b->cfg.max_tri = c.max_tri;
+  b->cfg.viscous = c.viscous != 0;
+  b->cfg.stream = b->stream;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (sms <= 0) sms = 152;
+  b->cfg.grid = c.grid > 0 ? c.grid : std::max<int>(1, std::min<int64_t>(c.blocks, 8LL * sms));
+  cudaError_t e = precision == FVM_PREC_FP64 ? prepare_attributes(b->cfg, (double *)nullptr)
+                                             : prepare_attributes(b->cfg, (float *)nullptr);
+  if (e != cudaSuccess) return fail(cuda_status(b, e));
+  *out = b;
+  return FVM_OK;
+}
+
+extern "C" int32_t fvm_batch_destroy(fvm_batch *b) {
+  if (!b) return FVM_OK;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  for (cudaEvent_t e : b->ev) cudaEventDestroy(e);
+  for (void *p : b->owned) cudaFree(p);
+  if (b->pinned) cudaFreeHost(b->pinned);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return FVM_OK;
+}
+
+extern "C" int32_t fvm_batch_add(fvm_batch *b, const fvm_params *par, const fvm_mesh *m,
+                                 int32_t *slot_out) {
+  if (!b || !par || !m || !slot_out) return FVM_ERR_ARG;
+  *slot_out = -1;
+  if (m->np < 3 || m->nt < 1 || m->netot < 1 || m->ne < 1 || !m->coord || !m->elem ||
+      !m->ptype || !m->edge || !m->iedge || !m->ds || !m->elarea || !m->cvarea ||
+      !m->mcarea || !m->drmin)
+    return FVM_ERR_ARG;
+  if (par->iflow == FVM_TURBULENT && !m->wd) return FVM_ERR_ARG;
+  if (m->nbe > 0 && !m->beindx) return FVM_ERR_ARG;
+  if (par->precision != b->prec) return FVM_ERR_ARG;
+  if (par->iflow != FVM_INVISCID && !b->caps.viscous) return FVM_ERR_ARG;
+  int sid = -1;
+  for (size_t i = 0; i < b->slots.size(); i++)
+    if (!b->slots[i].used) {
+      sid = (int)i;
+      break;
+    }
+  if (sid < 0) return FVM_ERR_CAPACITY;
+  Slot &S = b->slots[sid];
+  S = Slot();
+  S.par = *par;
+  int32_t st = build_layout(*m, kBlockVerts, S.L);
+  if (st != FVM_OK) return st;
+  const MeshLayout &L = S.L;
+  if (L.max_slots > b->cfg.max_slots || L.max_tri > b->cfg.max_tri) return FVM_ERR_CAPACITY;
+  const int64_t need[P_COUNT] = {L.np, L.nblk, (int64_t)L.be_nodes.size(), (int64_t)L.bb_nodes.size(),
+                                 (int64_t)L.bt_nodes.size(), L.nt, (int64_t)L.ve_list.size(),
+                                 (int64_t)L.vt_list.size(), (int64_t)L.va_list.size(),
+                                 (int64_t)L.sw_nodes.size()};
+  for (int i = 0; i < P_COUNT; i++) {
+    const int64_t off = b->pool[i].alloc(need[i]);
+    if (off < 0) {
+      for (int j = 0; j < i; j++) b->pool[j].release(S.off[j], S.len[j]);
+      S = Slot();
+      return FVM_ERR_CAPACITY;
+    }
+    S.off[i] = off;
+    S.len[i] = need[i];
+  }
+  const int np = L.np;
+  const int v0 = (int)S.off[P_V];
+  // vertex arrays
+  std::vector<double2> coord(np);
+  std::vector<double> ais(np), cvarea(np), drmin(np), wd(np, 1.0);
+  std::vector<int> orig(np);
+  std::vector<int2> ve(np), vt(np), va(np);
+  const double n1b6 = 1.0 / 6.0;
+  for (int v = 0; v < np; v++) {
+    const int o = L.perm[v];
+    coord[v] = make_double2(m->coord[2 * o], m->coord[2 * o + 1]);
+    ais[v] = n1b6 / m->mcarea[o];   // green_gauss.f:34
+    cvarea[v] = m->cvarea[o];
+    drmin[v] = m->drmin[o];
+    if (m->wd) wd[v] = m->wd[o];
+    orig[v] = o + 1;
+    ve[v] = make_int2((int)(S.off[P_VE] + L.ve_ptr[v]), (int)(S.off[P_VE] + L.ve_ptr[v + 1]));
+    vt[v] = make_int2((int)(S.off[P_VT] + L.vt_ptr[v]), (int)(S.off[P_VT] + L.vt_ptr[v + 1]));
+    va[v] = make_int2((int)(S.off[P_VA] + L.va_ptr[v]), (int)(S.off[P_VA] + L.va_ptr[v + 1]));
+  }
+  std::vector<BlockInfo> blocks = L.blocks;
+  for (int k = 0; k < L.nblk; k++) {
+    BlockInfo &bi = blocks[k];
+    bi.mesh = sid;
+    bi.v0 += v0;
+    bi.e0 += (int)S.off[P_BE];
+    bi.b0 += (int)S.off[P_BB];
+    bi.t0 += (int)S.off[P_BT];
+    bi.part = (int)S.off[P_BLK] + k;
+  }
+  std::vector<int2> be(L.be_nodes);
+  std::vector<double2> be_ds(be.size());
+  for (size_t k = 0; k < be.size(); k++) {
+    be[k].x += v0;
+    be[k].y += v0;
+    const int e = L.be_edge[k];
+    be_ds[k] = make_double2(m->ds[2 * e], m->ds[2 * e + 1]);
+  }
+  std::vector<int4> bb(L.bb_nodes);
+  for (int4 &q : bb) {
+    q.x += v0;
+    q.y += v0;
+  }
+  std::vector<int4> bt(L.bt_nodes);
+  for (int4 &q : bt) {
+    q.x += v0;
+    q.y += v0;
+    q.z += v0;
+    q.w += (int)S.off[P_TRI];
+  }
+  std::vector<int> valist(L.va_list);
+  for (int &x : valist) {
+    const unsigned u = (unsigned)x;
+    x = (int)((u & 0x80000000u) | ((u & 0x7fffffffu) + (unsigned)v0));
+  }
+  std::vector<int2> sw(L.sw_nodes);
+  for (int2 &q : sw) {
+    q.x += v0;
+    q.y += v0;
+  }
+  std::vector<double> elarea(m->elarea, m->elarea + L.nt);
+  MeshConst mc = make_const(*par);
+  mc.v0 = v0;
+  mc.nv = np;
+  mc.blk0 = (int)S.off[P_BLK];
+  mc.nblk = L.nblk;
+  mc.sw0 = (int)S.off[P_SW];
+  mc.nsw = (int)L.sw_nodes.size();
+  for (int k = 0; k < 3; k++) mc.orig123[k] = v0 + L.iperm[k];
+  MeshCtl ctl;
+  std::memset(&ctl, 0, sizeof(ctl));
+  ctl.err_point = INT_MAX;
+  ctl.hist_off = sid * kHistRows;
+  ctl.hist_cap = kHistRows;
+  auto err = [&](cudaError_t e) -> int32_t {
+    fvm_batch_remove(b, sid);
+    return cuda_status(b, e);
+  };
+  S.used = true;
+  cudaError_t e = cudaSuccess;
+#define PUT(expr)                  \
+  if ((e = (expr)) != cudaSuccess) \
+    return err(e);
+  PUT(put_range(b, b->coord, v0, coord));
+  PUT(put_range(b, b->ais, v0, ais));
+  PUT(put_range(b, b->cvarea, v0, cvarea));
+  PUT(put_range(b, b->drmin, v0, drmin));
+  PUT(put_range(b, b->wd, v0, wd));
+  PUT(put_range(b, b->orig, v0, orig));
+  PUT(put_range(b, b->vflag, v0, L.vflag));
+  PUT(put_range(b, b->ve_rng, v0, ve));
+  PUT(put_range(b, b->vt_rng, v0, vt));
+  PUT(put_range(b, b->va_rng, v0, va));
+  PUT(put_range(b, b->ve_list, S.off[P_VE], L.ve_list));
+  PUT(put_range(b, b->vt_list, S.off[P_VT], L.vt_list));
+  PUT(put_range(b, b->va_list, S.off[P_VA], valist));
+  PUT(put_range(b, b->blocks, S.off[P_BLK], blocks));
+  PUT(put_range(b, b->be_nodes, S.off[P_BE], be));
+  PUT(put_range(b, b->be_ds, S.off[P_BE], be_ds));
+  if (b->be_csl)
+    PUT(launch_edge_csl(b->be_ds + S.off[P_BE], b->be_csl + S.off[P_BE], (int)be.size(), b->stream));
+  PUT(put_range(b, b->bb_nodes, S.off[P_BB], bb));
+  PUT(put_range(b, b->bt_nodes, S.off[P_BT], bt));
+  PUT(put_range(b, b->elarea, S.off[P_TRI], elarea));
+  PUT(put_range(b, b->sw_nodes, S.off[P_SW], sw));
+  PUT(cudaMemcpyAsync(b->mc + sid, &mc, sizeof(mc), cudaMemcpyHostToDevice, b->stream));
+  PUT(cudaMemcpyAsync(b->ctl + sid, &ctl, sizeof(ctl), cudaMemcpyHostToDevice, b->stream));
+  const size_t r = b->rsz;
+  PUT(cudaMemsetAsync(static_cast<unsigned char *>(b->grad) + (size_t)v0 * 8 * r, 0, 8 * r * np, b->stream));
+  PUT(cudaMemsetAsync(static_cast<unsigned char *>(b->resv) + (size_t)v0 * 4 * r, 0, 4 * r * np, b->stream));
+  PUT(cudaStreamSynchronize(b->stream));
+#undef PUT
+  // freestream state (initialize.f:60-89)
+  {
+    std::vector<double> prim(4 * (size_t)np), nut(np, 0.0), mul(np, 0.0), mu(np, 0.0);
+    for (int v = 0; v < np; v++) {
+      prim[4 * v] = par->r_inf;
+      prim[4 * v + 1] = par->u_inf;
+      prim[4 * v + 2] = par->v_inf;
+      prim[4 * v + 3] = par->p_inf;
+    }
+    if (par->iflow != FVM_INVISCID) {
+      const double temp = par->p_inf / par->r_inf / par->gas_const;
+      const double mul0 = std::pow(temp / par->t_inf, 1.5) *
+                          ((par->t_inf + par->sconst) / (temp + par->sconst)) / par->rey;
+      for (int v = 0; v < np; v++) {
+        mul[v] = mul0;
+        if (par->iflow == FVM_TURBULENT) {
+          nut[v] = par->nut_inf;
+          const double chi = nut[v] * par->r_inf / mul0;
+          const double chi3 = (chi * chi) * chi;
+          mu[v] = mul0 + par->r_inf * nut[v] * (chi3 / (chi3 + par->cv11));
+        } else {
+          mu[v] = mul0;
+        }
+      }
+    }
+    st = fvm_batch_set_state(b, sid, prim.data(), nut.data(), mul.data(), mu.data(), 0);
+    if (st) {
+      fvm_batch_remove(b, sid);
+      return st;
+    }
+  }
+  if ((st = update_work(b))) {
+    fvm_batch_remove(b, sid);
+    return st;
+  }
+  *slot_out = sid;
+  return FVM_OK;
+}
+
+extern "C" int32_t fvm_batch_remove(fvm_batch *b, int32_t slot) {
+  Slot *S = slot_of(b, slot);
+  if (!S) return FVM_ERR_ARG;
+  MeshCtl z;
+  std::memset(&z, 0, sizeof(z));
+  int32_t st = put_ctl(b, slot, z);
+  for (int i = 0; i < P_COUNT; i++) b->pool[i].release(S->off[i], S->len[i]);
+  *S = Slot();
+  int32_t st2 = update_work(b);
+  return st ? st : st2;
+}
+
+extern "C" int32_t fvm_batch_set_state(fvm_batch *b, int32_t slot, const double *prim,
+                                       const double *nut, const double *mul, const double *mu,
+                                       int32_t iterlast) {
+  Slot *S = slot_of(b, slot);
+  if (!S || !prim) return FVM_ERR_ARG;
+  MeshCtl c;
+  int32_t st = get_ctl(b, slot, c);
+  if (st) return st;
+  const size_t r = b->rsz;
+  if ((st = put_vertex(b, *S, b->st[c.phase], prim, 4, 4 * r))) return st;
+  if (nut && (st = put_vertex(b, *S, b->nut[c.nphase], nut, 1, r))) return st;
+  if (mul && (st = put_vertex(b, *S, b->mul, mul, 1, r))) return st;
+  if (mu && (st = put_vertex(b, *S, b->mu, mu, 1, r))) return st;
+  c.iter = iterlast;
+  c.iterlast = iterlast;
+  c.fres1 = 0.0;
+  c.err = 0;
+  c.err_point = INT_MAX;
+  c.active = 0;
+  return put_ctl(b, slot, c);
+}
+
+extern "C" int32_t fvm_batch_get_state(fvm_batch *b, int32_t slot, double *prim, double *nut,
+                                       double *mul, double *mu, double *qx, double *qy) {
+  Slot *S = slot_of(b, slot);
+  if (!S) return FVM_ERR_ARG;
+  MeshCtl c;
+  int32_t st = get_ctl(b, slot, c);
+  if (st) return st;
+  const size_t r = b->rsz;
+  if (prim && (st = get_vertex(b, *S, prim, b->st[c.phase], 4, 4 * r))) return st;
+  if (nut && (st = get_vertex(b, *S, nut, b->nut[c.nphase], 1, r))) return st;
+  if (mul && (st = get_vertex(b, *S, mul, b->mul, 1, r))) return st;
+  if (mu && (st = get_vertex(b, *S, mu, b->mu, 1, r))) return st;
+  if (qx && (st = get_vertex(b, *S, qx, b->grad, 4, 8 * r, 0))) return st;
+  if (qy && (st = get_vertex(b, *S, qy, b->grad, 4, 8 * r, 4))) return st;
+  return FVM_OK;
+}
+
+extern "C" int32_t fvm_batch_start(fvm_batch *b, int32_t slot, int32_t nmax, double minres) {
+  Slot *S = slot_of(b, slot);
+  if (!S || nmax < 0) return FVM_ERR_ARG;
+  MeshCtl c;
+  int32_t st = get_ctl(b, slot, c);
+  if (st) return st;
+  c.active = nmax > 0 ? 1 : 0;
+  c.n_done = 0;
+  c.n_max = nmax;
+  c.minres = minres;
+  c.err = 0;
+  c.err_point = INT_MAX;
+  return put_ctl(b, slot, c);
+}
+
+extern "C" int32_t fvm_batch_step(fvm_batch *b, int32_t niter) {
+  if (!b || niter < 0) return FVM_ERR_ARG;
+  int32_t st = build_graph(b);
+  if (st) return st;
+  for (int i = 0; i < niter; i++) {
+    FVM_TRY(b, cudaGraphLaunch(b->graph, b->stream));
+    b->launches += b->kernels_per_iter;
+    if (b->timing) {
+      FVM_TRY(b, cudaStreamSynchronize(b->stream));
+      for (int k = 0; k < b->kernels_per_iter; k++) {
+        float ms = 0.f;
+        FVM_TRY(b, cudaEventElapsedTime(&ms, b->ev[2 * k], b->ev[2 * k + 1]));
+        b->t_ms[b->ev_kind[k]] += ms;
+        b->t_launch[b->ev_kind[k]] += 1;
+      }
+    }
+  }
+  return FVM_OK;
+}
+
+extern "C" int32_t fvm_batch_sync(fvm_batch *b) {
+  if (!b) return FVM_ERR_ARG;
+  FVM_TRY(b, cudaStreamSynchronize(b->stream));
+  return FVM_OK;
+}
+
+extern "C" int32_t fvm_batch_poll(fvm_batch *b, int32_t slot, int32_t *active, int32_t *niter,
+                                  double *fres, double *cl, double *cd, int32_t *status,
+                                  int32_t *bad_point) {
+  if (!slot_of(b, slot)) return FVM_ERR_ARG;
+  MeshCtl c;
+  int32_t st = get_ctl(b, slot, c);
+  if (st) return st;
+  if (active) *active = c.active;
+  if (niter) *niter = c.n_done;
+  if (fres) *fres = c.fres;
+  if (cl) *cl = c.cl;
+  if (cd) *cd = c.cd;
+  if (status) *status = c.err;
+  if (bad_point) *bad_point = (c.err == FVM_ERR_NONPOSITIVE) ? c.err_point : 0;
+  return FVM_OK;
+}
+
+extern "C" int32_t fvm_batch_history(fvm_batch *b, int32_t slot, int32_t first, int32_t count,
+                                     double *fres, int32_t *iresi, double *fresi, double *cl,
+                                     double *cd) {
+  if (!slot_of(b, slot) || first < 0 || count < 0) return FVM_ERR_ARG;
+  MeshCtl c;
+  int32_t st = get_ctl(b, slot, c);
+  if (st) return st;
+  if (first + count > c.n_done || c.n_done - first > kHistRows) return FVM_ERR_ARG;
+  std::vector<double> f(count), fi(count), l(count), d(count);
+  std::vector<int> ir(count);
+  // the rows form at most two contiguous runs of the slot's ring
+  int done = 0;
+  while (done < count) {
+    const int r0 = (first + done) % kHistRows;
+    const int run = std::min(count - done, kHistRows - r0);
+    const size_t row = (size_t)c.hist_off + r0;
+    FVM_TRY(b, cudaMemcpyAsync(&f[done], b->h_fres + row, 8 * run, cudaMemcpyDeviceToHost, b->stream));
+    FVM_TRY(b, cudaMemcpyAsync(&fi[done], b->h_fresi + row, 8 * run, cudaMemcpyDeviceToHost, b->stream));
+    FVM_TRY(b, cudaMemcpyAsync(&l[done], b->h_cl + row, 8 * run, cudaMemcpyDeviceToHost, b->stream));
+    FVM_TRY(b, cudaMemcpyAsync(&d[done], b->h_cd + row, 8 * run, cudaMemcpyDeviceToHost, b->stream));
+    FVM_TRY(b, cudaMemcpyAsync(&ir[done], b->h_iresi + row, 4 * run, cudaMemcpyDeviceToHost, b->stream));
+    done += run;
+  }
+  FVM_TRY(b, cudaStreamSynchronize(b->stream));
+  for (int i = 0; i < count; i++) {
+    if (fres) fres[i] = f[i];
+    if (fresi) fresi[i] = fi[i];
+    if (cl) cl[i] = l[i];
+    if (cd) cd[i] = d[i];
+    if (iresi) iresi[i] = ir[i];
+  }
+  return FVM_OK;
+}
+
+extern "C" void *fvm_batch_stream(fvm_batch *b) { return b ? (void *)b->stream : nullptr; }
+
+extern "C" int32_t fvm_batch_timing(fvm_batch *b, int32_t on) {
+  if (!b) return FVM_ERR_ARG;
+  const bool want = on != 0;
+  for (int k = 0; k < K_COUNT; k++) {
+    b->t_ms[k] = 0.0;
+    b->t_launch[k] = 0;
+  }
+  if (want == b->timing) return FVM_OK;
+  FVM_TRY(b, cudaStreamSynchronize(b->stream));
+  if (want && b->ev.empty()) {
+    const int pairs = 16;
+    b->ev.resize(2 * pairs);
+    b->ev_kind.assign(pairs, 0);
+    for (auto &e : b->ev) FVM_TRY(b, cudaEventCreate(&e));
+  }
+  b->timing = want;
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  return FVM_OK;
+}
+
+extern "C" int32_t fvm_batch_timing_read(fvm_batch *b, int32_t max, char *names, double *ms,
+                                         int64_t *launches, int32_t *n) {
+  if (!b || max < 0) return FVM_ERR_ARG;
+  const int cnt = std::min<int>(max, K_COUNT);
+  for (int k = 0; k < cnt; k++) {
+    if (names) std::snprintf(names + 32 * k, 32, "%s", kKernelNames[k]);
+    if (ms) ms[k] = b->t_ms[k];
+    if (launches) launches[k] = b->t_launch[k];
+  }
+  if (n) *n = cnt;
+  return FVM_OK;
+}
+
+extern "C" int64_t fvm_batch_launch_count(fvm_batch *b) { return b ? b->launches : -1; }
+
+extern "C" int32_t fvm_layout_stats(const fvm_mesh *m, int64_t *out) {
+  if (!m || !out) return FVM_ERR_ARG;
+  MeshLayout L;
+  int32_t st = build_layout(*m, kBlockVerts, L);
+  if (st) return st;
+  out[0] = L.nblk;
+  out[1] = (int64_t)L.be_nodes.size();
+  out[2] = (int64_t)L.bt_nodes.size();
+  out[3] = L.max_slots;
+  out[4] = L.max_tri;
+  out[5] = (int64_t)L.bb_nodes.size();
+  return FVM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// single-mesh API: a batch of one
+// ---------------------------------------------------------------------------
+struct fvm_handle {
+  fvm_batch *b = nullptr;
+  int slot = 0;
+  int np = 0;
+  int iflow = 1;
+};
+
+namespace {
+
+Slot &hslot(fvm_handle *h) { return h->b->slots[h->slot]; }
+
+template <typename R>
+int32_t residu_impl(fvm_handle *h) {
+  fvm_batch *b = h->b;
+  const ArenaPtrs<R> A = ptrs<R>(b);
+  if (h->iflow != FVM_INVISCID) FVM_TRY(b, launch_visc(A, b->cfg, 0, 0, 1));
+  FVM_TRY(b, launch_grad(A, b->cfg, 0, 0, 1));
+  FVM_TRY(b, launch_flux(A, b->cfg, 0, 0 /*MODE_RESIDUAL*/, 0, 1));
+  b->launches += (h->iflow != FVM_INVISCID) ? 3 : 2;
+  FVM_TRY(b, cudaStreamSynchronize(b->stream));
+  return FVM_OK;
+}
+
+}  // namespace
+
+extern "C" const char *fvm_gpu_strerror(int32_t s) {
+  switch (s) {
+    case FVM_OK: return "ok";
+    case FVM_ERR_ARG: return "invalid argument";
+    case FVM_ERR_CUDA: return "CUDA runtime error";
+    case FVM_ERR_NONPOSITIVE: return "Density/pressure is negative at point";
+    case FVM_ERR_ROE_SONIC: return "Sonic speed is negative";
+    case FVM_ERR_ZERO_FIRST_RES: return "Residue in first iteration is zero";
+    case FVM_ERR_TIMEOUT: return "device wait timed out";
+    case FVM_ERR_NOMEM: return "device memory allocation failed";
+    case FVM_ERR_STATE: return "call out of order";
+    case FVM_ERR_GEOMETRY: return "degenerate or inconsistent geometry";
+    case FVM_ERR_CAPACITY: return "capacity exceeded";
+    default: return "unknown status";
+  }
+}
+
+extern "C" int32_t fvm_gpu_create(const fvm_params *par, const fvm_mesh *m, fvm_handle **out) {
+  if (!par || !m || !out) return FVM_ERR_ARG;
+  *out = nullptr;
+  if (m->np < 3 || m->nt < 1) return FVM_ERR_ARG;
+  // size the arena exactly for this mesh
+  MeshLayout L;
+  if (!m->edge || !m->iedge || !m->elem || !m->ptype || (m->nbe > 0 && !m->beindx))
+    return FVM_ERR_ARG;
+  int32_t st = build_layout(*m, kBlockVerts, L);
+  if (st) return st;
+  fvm_batch_caps c;
+  std::memset(&c, 0, sizeof(c));
+  c.vertices = L.np;
+  c.meshes = 1;
+  c.viscous = par->iflow != FVM_INVISCID;
+  c.blocks = L.nblk;
+  c.edge_entries = std::max<int64_t>(1, L.be_nodes.size());
+  c.boundary_entries = std::max<int64_t>(1, L.bb_nodes.size());
+  c.tri_entries = std::max<int64_t>(1, L.bt_nodes.size());
+  c.triangles = L.nt;
+  c.edge_incidence = std::max<int64_t>(1, L.ve_list.size());
+  c.tri_incidence = std::max<int64_t>(1, L.vt_list.size());
+  c.all_incidence = std::max<int64_t>(1, L.va_list.size());
+  c.solid_edges = std::max<int64_t>(1, L.sw_nodes.size());
+  c.max_slots = std::max(1, L.max_slots);
+  c.max_tri = std::max(1, L.max_tri);
+  c.grid = L.nblk;
+  fvm_handle *h = new (std::nothrow) fvm_handle();
+  if (!h) return FVM_ERR_NOMEM;
+  if ((st = fvm_batch_create(par->precision, &c, &h->b))) {
+    delete h;
+    return st;
+  }
+  if ((st = fvm_batch_add(h->b, par, m, &h->slot))) {
+    fvm_batch_destroy(h->b);
+    delete h;
+    return st;
+  }
+  h->np = m->np;
+  h->iflow = par->iflow;
+  *out = h;
+  return FVM_OK;
+}
+
+extern "C" int32_t fvm_gpu_destroy(fvm_handle *h) {
+  if (!h) return FVM_OK;
+  fvm_batch_destroy(h->b);
+  delete h;
+  return FVM_OK;
+}
+
+extern "C" int32_t fvm_gpu_set_state(fvm_handle *h, const double *prim, const double *nut,
+                                     const double *mul, const double *mu, int32_t iterlast) {
+  if (!h) return FVM_ERR_ARG;
+  return fvm_batch_set_state(h->b, h->slot, prim, nut, mul, mu, iterlast);
+}
+
+extern "C" int32_t fvm_gpu_get_state(fvm_handle *h, double *prim, double *nut, double *mul,
+                                     double *mu, double *qx, double *qy) {
+  if (!h) return FVM_ERR_ARG;
+  return fvm_batch_get_state(h->b, h->slot, prim, nut, mul, mu, qx, qy);
+}
+
+extern "C" int32_t fvm_gpu_get_residual(fvm_handle *h, double *res) {
+  if (!h || !res) return FVM_ERR_ARG;
+  return get_vertex(h->b, hslot(h), res, h->b->res, 4, 4 * h->b->rsz);
+}
+
+extern "C" int32_t fvm_gpu_get_dt(fvm_handle *h, double *dt) {
+  if (!h || !dt) return FVM_ERR_ARG;
+  return get_vertex(h->b, hslot(h), dt, h->b->dt, 1, h->b->rsz);
+}
+
+extern "C" int32_t fvm_gpu_get_prim_old(fvm_handle *h, double *prim_old) {
+  if (!h || !prim_old) return FVM_ERR_ARG;
+  MeshCtl c;
+  int32_t st = get_ctl(h->b, h->slot, c);
+  if (st) return st;
+  return get_vertex(h->b, hslot(h), prim_old, h->b->st[(c.phase + 2) % 3], 4, 4 * h->b->rsz);
+}
+
+extern "C" int32_t fvm_gpu_save_old(fvm_handle *h) {
+  if (!h) return FVM_ERR_ARG;
+  fvm_batch *b = h->b;
+  MeshCtl c;
+  int32_t st = get_ctl(b, h->slot, c);
+  if (st) return st;
+  const size_t rec = 4 * b->rsz, off = (size_t)hslot(h).off[P_V] * rec;
+  FVM_TRY(b, cudaMemcpyAsync(static_cast<unsigned char *>(b->st[(c.phase + 2) % 3]) + off,
+                             static_cast<unsigned char *>(b->st[c.phase]) + off, rec * h->np,
+                             cudaMemcpyDeviceToDevice, b->stream));
+  FVM_TRY(b, cudaStreamSynchronize(b->stream));
+  return FVM_OK;
+}
+
+extern "C" int32_t fvm_gpu_time_step(fvm_handle *h) {
+  if (!h) return FVM_ERR_ARG;
+  fvm_batch *b = h->b;
+  if (b->prec == FVM_PREC_FP64) FVM_TRY(b, launch_time_step(ptrs<double>(b), b->cfg));
+  else FVM_TRY(b, launch_time_step(ptrs<float>(b), b->cfg));
+  b->launches++;
+  FVM_TRY(b, cudaStreamSynchronize(b->stream));
+  return FVM_OK;
+}
+
+extern "C" int32_t fvm_gpu_residu(fvm_handle *h) {
+  if (!h) return FVM_ERR_ARG;
+  MeshCtl c;
+  int32_t st = get_ctl(h->b, h->slot, c);
+  if (st) return st;
+  c.err = 0;
+  if ((st = put_ctl(h->b, h->slot, c))) return st;
+  st = h->b->prec == FVM_PREC_FP64 ? residu_impl<double>(h) : residu_impl<float>(h);
+  if (st) return st;
+  if ((st = get_ctl(h->b, h->slot, c))) return st;
+  return c.err ? c.err : FVM_OK;
+}
+
+extern "C" int32_t fvm_gpu_update(fvm_handle *h, int32_t irk) {
+  if (!h || irk < 1 || irk > 3) return FVM_ERR_ARG;
+  fvm_batch *b = h->b;
+  if (b->prec == FVM_PREC_FP64) FVM_TRY(b, launch_update(ptrs<double>(b), b->cfg, irk));
+  else FVM_TRY(b, launch_update(ptrs<float>(b), b->cfg, irk));
+  b->launches++;
+  FVM_TRY(b, cudaStreamSynchronize(b->stream));
+  return FVM_OK;
+}
+
+extern "C" int32_t fvm_gpu_sa_model(fvm_handle *h) {
+  if (!h) return FVM_ERR_ARG;
+  if (h->iflow != FVM_TURBULENT) return FVM_OK;
+  fvm_batch *b = h->b;
+  if (b->prec == FVM_PREC_FP64) FVM_TRY(b, launch_sa(ptrs<double>(b), b->cfg, 0, 1));
+  else FVM_TRY(b, launch_sa(ptrs<float>(b), b->cfg, 0, 1));
+  b->launches++;
+  MeshCtl c;
+  int32_t st = get_ctl(b, h->slot, c);
+  if (st) return st;
+  c.nphase = 1 - c.nphase;
+  return put_ctl(b, h->slot, c);
+}
+
+extern "C" int32_t fvm_gpu_limitgrad(fvm_handle *h) {
+  if (!h) return FVM_ERR_ARG;
+  fvm_batch *b = h->b;
+  if (b->prec == FVM_PREC_FP64) FVM_TRY(b, launch_limitgrad(ptrs<double>(b), b->cfg));
+  else FVM_TRY(b, launch_limitgrad(ptrs<float>(b), b->cfg));
+  b->launches++;
+  FVM_TRY(b, cudaStreamSynchronize(b->stream));
+  return FVM_OK;
+}
+
+extern "C" int32_t fvm_gpu_check_positivity(fvm_handle *h, int32_t *bad_point) {
+  if (!h) return FVM_ERR_ARG;
+  fvm_batch *b = h->b;
+  MeshCtl c;
+  int32_t st = get_ctl(b, h->slot, c);
+  if (st) return st;
+  c.err_point = INT_MAX;
+  if ((st = put_ctl(b, h->slot, c))) return st;
+  if (b->prec == FVM_PREC_FP64) FVM_TRY(b, launch_positivity(ptrs<double>(b), b->cfg));
+  else FVM_TRY(b, launch_positivity(ptrs<float>(b), b->cfg));
+  b->launches++;
+  if ((st = get_ctl(b, h->slot, c))) return st;
+  const int bad = c.err_point == INT_MAX ? 0 : c.err_point;
+  if (bad_point) *bad_point = bad;
+  return bad ? FVM_ERR_NONPOSITIVE : FVM_OK;
+}
+
+extern "C" int32_t fvm_gpu_clcd(fvm_handle *h, double *cl, double *cd) {
+  if (!h) return FVM_ERR_ARG;
+  fvm_batch *b = h->b;
+  const int serial = b->prec == FVM_PREC_FP64;
+  if (b->prec == FVM_PREC_FP64) FVM_TRY(b, launch_clcd(ptrs<double>(b), b->cfg, h->slot, serial));
+  else FVM_TRY(b, launch_clcd(ptrs<float>(b), b->cfg, h->slot, serial));
+  b->launches++;
+  MeshCtl c;
+  int32_t st = get_ctl(b, h->slot, c);
+  if (st) return st;
+  if (cl) *cl = c.cl;
+  if (cd) *cd = c.cd;
+  return FVM_OK;
+}
+
+extern "C" int32_t fvm_gpu_conres(fvm_handle *h, int32_t first, double *fres, double *fresi,
+                                  int32_t *iresi) {
+  if (!h) return FVM_ERR_ARG;
+  fvm_batch *b = h->b;
+  MeshCtl c;
+  int32_t st = get_ctl(b, h->slot, c);
+  if (st) return st;
+  c.err = 0;
+  if ((st = put_ctl(b, h->slot, c))) return st;
+  if (b->prec == FVM_PREC_FP64) FVM_TRY(b, launch_conres(ptrs<double>(b), b->cfg, h->slot, first));
+  else FVM_TRY(b, launch_conres(ptrs<float>(b), b->cfg, h->slot, first));
+  b->launches += 2;
+  if ((st = get_ctl(b, h->slot, c))) return st;
+  if (fres) *fres = c.fres;
+  if (fresi) *fresi = c.fresi;
+  if (iresi) *iresi = c.iresi;
+  return c.err ? c.err : FVM_OK;
+}
+
+extern "C" int32_t fvm_gpu_iterate(fvm_handle *h, int32_t nmax, double minres, int32_t *niter,
+                                   double *hist_fres, int32_t *hist_iresi, double *hist_fresi,
+                                   double *hist_cl, double *hist_cd, int32_t *bad_point) {
+  if (!h || nmax < 0) return FVM_ERR_ARG;
+  if (niter) *niter = 0;
+  if (bad_point) *bad_point = 0;
+  if (nmax == 0) return FVM_OK;
+  fvm_batch *b = h->b;
+  int32_t st = fvm_batch_start(b, h->slot, nmax, minres);
+  if (st) return st;
+  int consumed = 0, active = 1, done = 0, status = 0, bad = 0;
+  while (true) {
+    const int k = std::min(kHistRows, nmax - consumed);
+    if ((st = fvm_batch_step(b, k))) return st;
+    if ((st = fvm_batch_poll(b, h->slot, &active, &done, nullptr, nullptr, nullptr, &status, &bad)))
+      return st;
+    const int rows = done - consumed;
+    if (rows > 0) {
+      auto off_d = [&](double *p) { return p ? p + consumed : nullptr; };
+      if ((st = fvm_batch_history(b, h->slot, consumed, rows, off_d(hist_fres),
+                                  hist_iresi ? hist_iresi + consumed : nullptr, off_d(hist_fresi),
+                                  off_d(hist_cl), off_d(hist_cd))))
+        return st;
+    }
+    consumed = done;
+    if (!active || consumed >= nmax) break;
+  }
+  if (niter) *niter = consumed;
+  if (bad_point) *bad_point = bad;
+  return status ? status : FVM_OK;
+}
+
+// ---- stand-alone set-up kernels -----------------------------------------
+extern "C" int32_t fvm_gpu_dtlength(int32_t np, int32_t nt, const double *coord,
+                                    const int32_t *elem, const double *elarea, double *drmin) {
+  if (np < 1 || nt < 1 || !coord || !elem || !elarea || !drmin) return FVM_ERR_ARG;
+  for (int64_t k = 0; k < 3 * (int64_t)nt; k++)
+    if (elem[k] < 1 || elem[k] > np) return FVM_ERR_ARG;
+  std::vector<void *> O;
+  double2 *dc = nullptr;
+  int *de = nullptr;
+  double *da = nullptr, *dr = nullptr;
+  cudaError_t e = cudaSuccess;
+  if ((e = dalloc(O, &dc, np)) == cudaSuccess && (e = dalloc(O, &de, 3 * (size_t)nt)) == cudaSuccess &&
+      (e = dalloc(O, &da, nt)) == cudaSuccess && (e = dalloc(O, &dr, np)) == cudaSuccess &&
+      (e = cudaMemcpy(dc, coord, 16 * (size_t)np, cudaMemcpyHostToDevice)) == cudaSuccess &&
+      (e = cudaMemcpy(de, elem, 12 * (size_t)nt, cudaMemcpyHostToDevice)) == cudaSuccess &&
+      (e = cudaMemcpy(da, elarea, 8 * (size_t)nt, cudaMemcpyHostToDevice)) == cudaSuccess &&
+      (e = launch_dtlength(np, nt, dc, de, da, dr, 0)) == cudaSuccess)
+    e = cudaMemcpy(drmin, dr, 8 * (size_t)np, cudaMemcpyDeviceToHost);
+  for (void *p : O) cudaFree(p);
+  return cuda_status(nullptr, e);
+}
+
+extern "C" int32_t fvm_gpu_wall_dist(int32_t np, int32_t ne, const double *coord,
+                                     const int32_t *edge, const int32_t *ptype, int32_t bugcompat,
+                                     double *wd) {
+  if (np < 1 || ne < 0 || !coord || !edge || !ptype || !wd) return FVM_ERR_ARG;
+  std::vector<int2> sedge;   // wall_dist.f:17-25
+  for (int i = 0; i < ne; i++) {
+    const int a = edge[2 * i] - 1, c = edge[2 * i + 1] - 1;
+    if (a < 0 || a >= np || c < 0 || c >= np) return FVM_ERR_ARG;
+    if (ptype[a] == FVM_PT_SOLID && ptype[c] == FVM_PT_SOLID) sedge.push_back(make_int2(a, c));
+  }
+  std::vector<void *> O;
+  double2 *dc = nullptr;
+  int2 *ds = nullptr;
+  int *dp = nullptr;
+  double *dw = nullptr;
+  cudaError_t e = cudaSuccess;
+  if ((e = dalloc(O, &dc, np)) == cudaSuccess && (e = dalloc(O, &ds, sedge.size())) == cudaSuccess &&
+      (e = dalloc(O, &dp, np)) == cudaSuccess && (e = dalloc(O, &dw, np)) == cudaSuccess &&
+      (e = cudaMemcpy(dc, coord, 16 * (size_t)np, cudaMemcpyHostToDevice)) == cudaSuccess &&
+      (sedge.empty() ||
+       (e = cudaMemcpy(ds, sedge.data(), 8 * sedge.size(), cudaMemcpyHostToDevice)) == cudaSuccess) &&
+      (e = cudaMemcpy(dp, ptype, 4 * (size_t)np, cudaMemcpyHostToDevice)) == cudaSuccess &&
+      (e = launch_wall_dist(np, (int)sedge.size(), dc, ds, dp, bugcompat, dw, 0)) == cudaSuccess)
+    e = cudaMemcpy(wd, dw, 8 * (size_t)np, cudaMemcpyDeviceToHost);
+  for (void *p : O) cudaFree(p);
+  return cuda_status(nullptr, e);
+}

@@ -82,8 +82,8 @@ struct MeshCtl {
   int n_max;         // iterations allowed in this iterate call
   int err;           // FVM_ERR_* (0 = none)
   int err_point;     // min driver index (1-based) of a non-positive point
-  int hist_off;      // offset of this mesh's history rows
-  int hist_cap;      // rows available
+  int hist_off;      // first history row of this slot
+  int hist_cap;      // rows of the slot's history ring
   int pad;
   double minres, fres1, fres, fresi, cl, cd;
   int iresi, pad2;
@@ -124,10 +124,10 @@ struct ArenaPtrs {
   const double *cvarea, *drmin, *wd;
   const int *orig;       // driver index (1-based) of each vertex
   const uint8_t *vflag;
-  // incidence
-  const int *ve_ptr;      // [V+1] absolute offsets into ve_list
+  // incidence: per vertex {begin, end} into the list arrays
+  const int2 *ve_rng;
   const uint16_t *ve_list;
-  const int *vt_ptr;
+  const int2 *vt_rng;
   const uint16_t *vt_list;
   // block entries
   const BlockInfo *blocks;
@@ -140,7 +140,7 @@ struct ArenaPtrs {
   // solid edges per mesh for clcd (n1, n2) in beindx order
   const int2 *sw_nodes;
   // all-edge incidence (limitgrad.f loops over netot edges)
-  const int *va_ptr;
+  const int2 *va_rng;
   const int *va_list;     // other vertex | (is n2) << 31
   // per mesh
   const MeshConst *mc;
@@ -152,6 +152,7 @@ struct ArenaPtrs {
   // block work list (indices into blocks[]) and its length
   const int *work;
   const int *nwork;
+  int nslots;             // mesh slots (monitor grid)
 };
 
 }  // namespace fvm

@@ -44,7 +44,7 @@ __global__ void __launch_bounds__(kBlockVerts) k_visc(ArenaPtrs<R> A, int stage,
     const MeshCtl &ctl = A.ctl[bi.mesh];
     if (!routine && !ctl.active) continue;
     const MeshConst &mc = A.mc[bi.mesh];
-    if (threadIdx.x >= bi.nv) continue;
+    if (mc.iflow == 1 || threadIdx.x >= bi.nv) continue;   // inviscid: mu stays 0
     const int v = bi.v0 + threadIdx.x;
     const R4<R> P = A.st[cur_buf(ctl.phase, stage)][v];
     if (do_dt) A.dt[v] = time_step<R>(mc, P, A.mu[v], A.drmin[v]);
@@ -138,8 +138,8 @@ __global__ void __launch_bounds__(kBlockVerts) k_grad(ArenaPtrs<R> A, int stage,
       const int v = bi.v0 + threadIdx.x;
       R qx[4] = {R(0), R(0), R(0), R(0)}, qy[4] = {R(0), R(0), R(0), R(0)};
       R rv[3] = {R(0), R(0), R(0)};
-      const int j0 = A.vt_ptr[v], j1 = A.vt_ptr[v + 1];
-      for (int j = j0; j < j1; j++) {
+      const int2 jr = A.vt_rng[v];
+      for (int j = jr.x; j < jr.y; j++) {
         const uint16_t e = A.vt_list[j];
         const int slot = e & 0x3fff;
         const TriSmem<R> ts = s_tri[slot];
@@ -302,8 +302,8 @@ __global__ void __launch_bounds__(kBlockVerts) k_flux(ArenaPtrs<R> A, int stage,
       } else {
         acc[0] = acc[1] = acc[2] = acc[3] = R(0);
       }
-      const int j0 = A.ve_ptr[v], j1 = A.ve_ptr[v + 1];
-      for (int j = j0; j < j1; j++) {
+      const int2 jr = A.ve_rng[v];
+      for (int j = jr.x; j < jr.y; j++) {
         const uint16_t e = A.ve_list[j];
         const R4<R> f = s_flux[e & kSlotMask];
         if (e & kSolidBit) {
@@ -475,11 +475,13 @@ __global__ void __launch_bounds__(kBlockVerts) k_sa(ArenaPtrs<R> A, int stage, i
     if (threadIdx.x < bi.nv) {
       const int v = bi.v0 + threadIdx.x;
       R divf = R(0);
-      for (int j = A.vt_ptr[v]; j < A.vt_ptr[v + 1]; j++) {
+      const int2 tr = A.vt_rng[v];
+      for (int j = tr.x; j < tr.y; j++) {
         const uint16_t e = A.vt_list[j];
         divf = divf + s_t[3 * (e & 0x3fff) + (e >> kTriPosShift)];
       }
-      for (int j = A.ve_ptr[v]; j < A.ve_ptr[v + 1]; j++) {
+      const int2 er = A.ve_rng[v];
+      for (int j = er.x; j < er.y; j++) {
         const uint16_t e = A.ve_list[j];
         if (e & kSolidBit) continue;
         const R f = s_e[e & kSlotMask];
@@ -611,9 +613,8 @@ __device__ void conres_block(const ArenaPtrs<R> &A, const MeshConst &mc, double 
 
 // One CTA (256 threads) per mesh slot listed in mesh_list.
 template <typename R>
-__global__ void __launch_bounds__(256) k_monitor(ArenaPtrs<R> A, const int *mesh_list,
-                                                 int serial_clcd) {
-  const int m = mesh_list[blockIdx.x];
+__global__ void __launch_bounds__(256) k_monitor(ArenaPtrs<R> A, int serial_clcd) {
+  const int m = blockIdx.x;
   MeshCtl &ctl = A.ctl[m];
   if (!ctl.active) return;
   const MeshConst &mc = A.mc[m];
@@ -652,8 +653,8 @@ __global__ void __launch_bounds__(256) k_monitor(ArenaPtrs<R> A, const int *mesh
   }
   fres = fres / ctl.fres1;
   ctl.fres = fres;
-  if (ctl.n_done < ctl.hist_cap) {
-    const int row = ctl.hist_off + ctl.n_done;
+  {
+    const int row = ctl.hist_off + ctl.n_done % ctl.hist_cap;
     A.h_fres[row] = fres;
     A.h_iresi[row] = ctl.iresi;
     A.h_fresi[row] = ctl.fresi;
@@ -823,7 +824,8 @@ __global__ void __launch_bounds__(kBlockVerts) k_limitgrad(ArenaPtrs<R> A) {
       qmax[q] = R(-1.0e10);
       phi[q] = R(1);
     }
-    const int j0 = A.va_ptr[v], j1 = A.va_ptr[v + 1];
+    const int2 ar = A.va_rng[v];
+    const int j0 = ar.x, j1 = ar.y;
     for (int j = j0; j < j1; j++) {
       const int o = A.va_list[j] & 0x7fffffff;
       const R4<R> po = P[o];

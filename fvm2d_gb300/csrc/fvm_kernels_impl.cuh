@@ -40,10 +40,9 @@ namespace fvm {
     k_sa<R><<<c.grid, kBlockVerts, sm, c.stream>>>(A, stage, routine, c.max_tri);           \
     return cudaGetLastError();                                                             \
   }                                                                                        \
-  cudaError_t launch_monitor(const ArenaPtrs<R> &A, const LaunchCfg &c,                     \
-                             const int *mesh_list, int nmesh, int serial_clcd) {           \
-    if (nmesh <= 0) return cudaSuccess;                                                    \
-    k_monitor<R><<<nmesh, 256, 0, c.stream>>>(A, mesh_list, serial_clcd);                   \
+  cudaError_t launch_monitor(const ArenaPtrs<R> &A, const LaunchCfg &c, int serial_clcd) {  \
+    if (A.nslots <= 0) return cudaSuccess;                                                 \
+    k_monitor<R><<<A.nslots, 256, 0, c.stream>>>(A, serial_clcd);                          \
     return cudaGetLastError();                                                             \
   }                                                                                        \
   cudaError_t launch_update(const ArenaPtrs<R> &A, const LaunchCfg &c, int irk) {           \

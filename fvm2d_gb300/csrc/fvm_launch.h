@@ -26,8 +26,7 @@ struct LaunchCfg {
   cudaError_t launch_flux(const ArenaPtrs<R> &A, const LaunchCfg &c, int stage, int mode,  \
                           int irk, int routine);                                          \
   cudaError_t launch_sa(const ArenaPtrs<R> &A, const LaunchCfg &c, int stage, int routine);\
-  cudaError_t launch_monitor(const ArenaPtrs<R> &A, const LaunchCfg &c,                    \
-                             const int *mesh_list, int nmesh, int serial_clcd);            \
+  cudaError_t launch_monitor(const ArenaPtrs<R> &A, const LaunchCfg &c, int serial_clcd); \
   cudaError_t launch_update(const ArenaPtrs<R> &A, const LaunchCfg &c, int irk);           \
   cudaError_t launch_time_step(const ArenaPtrs<R> &A, const LaunchCfg &c);                 \
   cudaError_t launch_positivity(const ArenaPtrs<R> &A, const LaunchCfg &c);                \

@@ -176,7 +176,8 @@ def write_amdba(path: str, grid: Grid) -> None:
     with open(path, "w") as f:
         f.write(f"{grid.np} {grid.nt}\n")
         for i in range(grid.np):
-            f.write(f"{i + 1} {grid.coord[i, 0]!r} {grid.coord[i, 1]!r} {int(grid.ptype[i])}\n")
+            f.write(f"{i + 1} {float(grid.coord[i, 0])!r} {float(grid.coord[i, 1])!r} "
+                    f"{int(grid.ptype[i])}\n")
         for i in range(grid.nt):
             n1, n2, n3 = (int(v) for v in grid.elem[i])
             f.write(f"{i + 1} {n1} {n2} {n3} 0\n")

@@ -227,6 +227,80 @@ int32_t fvm_geom_build(int32_t np, int32_t nt, const double *coord,
                        int32_t cell_type, fvm_geom **out);
 int32_t fvm_geom_free(fvm_geom *g);
 
+/* ---- batches: many meshes of uneven size in one launch per kernel ------- */
+/*
+ * No counterpart in the reference (which solves one grid per process).  A
+ * batch is a device arena holding many meshes at once; every kernel of an
+ * iteration runs once for all of them (a persistent grid-stride loop over
+ * the blocks of every armed mesh), and one CUDA graph holds the whole
+ * iteration.  Meshes are admitted and retired between steps without
+ * re-capturing the graph: the kernels read the work list from device
+ * memory.  The single-mesh fvm_gpu_* calls above are a batch of one.
+ */
+typedef struct fvm_batch fvm_batch;
+
+typedef struct fvm_batch_caps {
+  int64_t vertices;          /* total vertices of all resident meshes         */
+  int32_t meshes;            /* resident meshes at a time                     */
+  int32_t viscous;           /* 1 if laminar/turbulent meshes may be admitted */
+  /* optional overrides; 0 = derived from vertices and meshes */
+  int64_t blocks, edge_entries, boundary_entries, tri_entries, triangles;
+  int64_t edge_incidence, tri_incidence, all_incidence, solid_edges;
+  int32_t max_slots, max_tri;   /* per-block shared-memory sizing           */
+  int32_t grid;                 /* CTAs of the block kernels (0 = occupancy) */
+  int32_t reserved;
+} fvm_batch_caps;
+
+int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *caps,
+                         fvm_batch **out);
+int32_t fvm_batch_destroy(fvm_batch *b);
+/* Admits a mesh (geometry upload, block tables, freestream state) and
+ * returns its slot; FVM_ERR_CAPACITY when the arena has no room. */
+int32_t fvm_batch_add(fvm_batch *b, const fvm_params *p, const fvm_mesh *m,
+                      int32_t *slot);
+int32_t fvm_batch_remove(fvm_batch *b, int32_t slot);
+int32_t fvm_batch_set_state(fvm_batch *b, int32_t slot, const double *prim,
+                            const double *nut, const double *mul,
+                            const double *mu, int32_t iterlast);
+int32_t fvm_batch_get_state(fvm_batch *b, int32_t slot, double *prim,
+                            double *nut, double *mul, double *mu, double *qx,
+                            double *qy);
+/* Arms a solve of up to nmax iterations that stops after the first
+ * iteration with fres <= minres (main.f:42). */
+int32_t fvm_batch_start(fvm_batch *b, int32_t slot, int32_t nmax,
+                        double minres);
+/* Enqueues niter iterations of every armed mesh; asynchronous. */
+int32_t fvm_batch_step(fvm_batch *b, int32_t niter);
+int32_t fvm_batch_sync(fvm_batch *b);
+/* Waits for the stream and reports one slot: *active (still iterating),
+ * *niter (iterations since start), the last fres, cl, cd, and the status
+ * (FVM_OK or the stop that ended it, with *bad_point for positivity). */
+int32_t fvm_batch_poll(fvm_batch *b, int32_t slot, int32_t *active,
+                       int32_t *niter, double *fres, double *cl, double *cd,
+                       int32_t *status, int32_t *bad_point);
+/* Copies RES.DAT rows [first, first+count) of the current solve (the
+ * device keeps the last fvm_batch_history_depth() rows). */
+int32_t fvm_batch_history(fvm_batch *b, int32_t slot, int32_t first,
+                          int32_t count, double *fres, int32_t *iresi,
+                          double *fresi, double *cl, double *cd);
+int32_t fvm_batch_history_depth(void);
+/* The batch's CUDA stream (cudaStream_t), for callers that order their own
+ * work or events after the batch's. */
+void *fvm_batch_stream(fvm_batch *b);
+/* Per-kernel device time: when on, CUDA events are recorded around every
+ * kernel of each iteration and accumulated by kernel name. */
+int32_t fvm_batch_timing(fvm_batch *b, int32_t on);
+int32_t fvm_batch_timing_read(fvm_batch *b, int32_t max, char *names,
+                              double *ms, int64_t *launches, int32_t *n);
+/* Launches of this library's kernels since the batch was created. */
+int64_t fvm_batch_launch_count(fvm_batch *b);
+
+/* Layout statistics of a mesh after renumbering (no GPU needed):
+ * out[0] blocks, [1] interior edge entries (cut edges counted in both
+ * blocks), [2] triangle entries, [3] max slots of a block, [4] max
+ * triangles of a block, [5] boundary edge entries. */
+int32_t fvm_layout_stats(const fvm_mesh *m, int64_t *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,124 @@
+"""Batched path: many meshes of uneven size in one arena and one launch per
+kernel.  Each solve must give the same result alone and in any mix (the
+per-vertex arithmetic never depends on other meshes, so "the same" is
+bit for bit), meshes must be admissible and removable between steps, and
+a full arena must refuse a mesh with a status, not fail."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+from fvm2d_gb300 import _lib as L  # noqa: E402
+from fvm2d_gb300.ogrid import naca_ogrid  # noqa: E402
+
+
+def mesh(fvm_lib, ni, nr, seed=0, **kw):
+    g = naca_ogrid(ni, nr, jitter=0.1 if seed else 0.0, seed=seed, **kw)
+    return fvm_lib.build_geometry(g.coord, g.elem, g.ptype)
+
+
+CASES = [dict(ni=64, nr=24, seed=0), dict(ni=96, nr=40, seed=3), dict(ni=48, nr=20, seed=5,
+                                                                       thickness=0.15)]
+FLOWS = [dict(mach=0.8, aoa_deg=1.25), dict(mach=0.5, aoa_deg=3.0, iflux=L.KFVS),
+         dict(mach=0.7, aoa_deg=-1.0, iflux=L.HLLC, bugcompat=0)]
+
+
+def alone(fvm_lib, prec, m, flow, n):
+    from fvm2d_gb300.batch import Batch
+    b = Batch(prec, vertices=m.np, meshes=1)
+    s = b.add(fvm_lib.make_params(precision=prec, **flow), m)
+    b.start(s, n)
+    b.step(n)
+    p = b.poll(s)
+    h = b.history(s, 0, p["niter"])
+    st = b.get_state(s)
+    b.close()
+    return h, st
+
+
+@pytest.mark.parametrize("prec", [L.FP64, L.FP32])
+def test_alone_equals_mix(fvm_lib, prec):
+    from fvm2d_gb300.batch import Batch
+    ms = [mesh(fvm_lib, **c) for c in CASES]
+    n = 40
+    ref = [alone(fvm_lib, prec, m, f, n) for m, f in zip(ms, FLOWS)]
+    b = Batch(prec, vertices=sum(m.np for m in ms) + 5000, meshes=5)
+    slots = [b.add(fvm_lib.make_params(precision=prec, **f), m) for m, f in zip(ms, FLOWS)]
+    for s in slots:
+        b.start(s, n)
+    b.step(n + 5)      # extra steps: finished meshes must stay untouched
+    for s, (h0, st0) in zip(slots, ref):
+        p = b.poll(s)
+        assert p["status"] == 0 and p["niter"] == n and not p["active"]
+        h = b.history(s, 0, n)
+        for k in ("fres", "cl", "cd", "iresi"):
+            np.testing.assert_array_equal(h[k], h0[k])
+        np.testing.assert_array_equal(b.get_state(s)["prim"], st0["prim"])
+
+
+def test_fp64_batch_matches_handle(fvm_lib):
+    """The batch path and the single-mesh C ABI run the same kernels."""
+    from fvm2d_gb300.batch import Batch
+    m = mesh(fvm_lib, 64, 24)
+    s1 = fvm_lib.Solver(fvm_lib.make_params(), m)
+    st, h1 = s1.iterate(30)
+    b = Batch(L.FP64, vertices=m.np, meshes=1)
+    s = b.add(fvm_lib.make_params(), m)
+    b.start(s, 30)
+    b.step(30)
+    h = b.history(s, 0, 30)
+    np.testing.assert_array_equal(h["fres"], h1["fres"])
+
+
+def test_admit_and_retire_between_steps(fvm_lib):
+    from fvm2d_gb300.batch import Batch
+    prec = L.FP32
+    a, c = mesh(fvm_lib, 64, 24), mesh(fvm_lib, 96, 40, seed=3)
+    ref_a, _ = alone(fvm_lib, prec, a, FLOWS[0], 60)
+    b = Batch(prec, vertices=a.np + c.np + 100, meshes=2)
+    sa = b.add(fvm_lib.make_params(precision=prec, **FLOWS[0]), a)
+    b.start(sa, 60)
+    b.step(20)
+    sc = b.add(fvm_lib.make_params(precision=prec, **FLOWS[1]), c)   # admitted mid-solve
+    b.start(sc, 100)
+    b.step(20)
+    b.remove(sc)                                                      # retired mid-solve
+    b.step(25)
+    p = b.poll(sa)
+    assert p["niter"] == 60 and p["status"] == 0
+    h = b.history(sa, 0, 60)
+    np.testing.assert_array_equal(h["fres"], ref_a["fres"])
+    # the freed range is reusable
+    sd = b.add(fvm_lib.make_params(precision=prec, **FLOWS[2]), c)
+    assert sd >= 0
+
+
+def test_capacity_is_a_status(fvm_lib):
+    from fvm2d_gb300.batch import Batch
+    m = mesh(fvm_lib, 64, 24)
+    b = Batch(L.FP32, vertices=m.np + 10, meshes=3)
+    assert b.try_add(fvm_lib.make_params(precision=L.FP32), m) is not None
+    assert b.try_add(fvm_lib.make_params(precision=L.FP32), m) is None
+    b2 = Batch(L.FP32, vertices=10 * m.np, meshes=1)
+    assert b2.try_add(fvm_lib.make_params(precision=L.FP32), m) is not None
+    assert b2.try_add(fvm_lib.make_params(precision=L.FP32), m) is None
+
+
+def test_mixed_euler_laminar(fvm_lib, oracle_lib):
+    """A viscous-capable arena runs Euler and laminar meshes together; each
+    matches its oracle run."""
+    from fvm2d_gb300.batch import Batch
+    g1 = naca_ogrid(64, 24)
+    g2 = naca_ogrid(48, 20, thickness=0.1)
+    flows = [dict(mach=0.8, aoa_deg=1.25), dict(iflow=L.LAMINAR, mach=0.5, aoa_deg=0.0,
+                                                 rey=5000.0, cfl=0.8)]
+    ors = [oracle_lib.Oracle(g.coord, g.elem, g.ptype, **f) for g, f in zip((g1, g2), flows)]
+    b = Batch(L.FP64, vertices=g1.np + g2.np, meshes=2, viscous=True)
+    slots = [b.add(fvm_lib.make_params(**f), o.mesh_arrays()) for f, o in zip(flows, ors)]
+    for s in slots:
+        b.start(s, 25)
+    b.step(25)
+    for s, o in zip(slots, ors):
+        st, oh = o.iterate(25)
+        h = b.history(s, 0, 25)
+        assert np.max(np.abs(h["fres"] - oh["fres"]) / oh["fres"]) <= 1e-10
