@@ -116,7 +116,7 @@ class ClockSampler:
             except ValueError:
                 continue
             for k, n in enumerate(names):
-                if "Active" in f[5 + k]:
+                if f[5 + k].strip() == "Active":
                     reasons.add(n)
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
@@ -359,7 +359,7 @@ def oracle_rate(nthreads, ni, nr, iters, seeds):
 def cpu_baseline(meshes, args):
     from oracle import oracle
     oracle.build()
-    iters = 12
+    iters = 40
     rate, wall = oracle_rate(1, NI, NR, iters, [2])
     return {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
             "sample": f"{iters} iterations of one {NI}x{NR} mesh of the same workload, "

@@ -3,8 +3,9 @@
 Every translation unit is compiled in parallel:
   * CUDA kernels for sm_103a only (``-gencode arch=compute_103a,code=sm_103a``);
     the FP64 kernels and the set-up kernels with ``--fmad=false`` so their
-    arithmetic is rounded exactly as written, the FP32 kernels with
-    contraction allowed;
+    arithmetic is rounded exactly as written; the FP32 kernels with
+    contraction allowed and approximate division and square root (a few
+    ulp; the FP32 path is judged against the FP64 oracle by tolerance);
   * host C++ with ``-ffp-contract=off`` (the driver-side geometry must equal
     the serial FP64 arithmetic on x86 and on Arm alike).
 No CPU fallback is built: without this library the package refuses to run.
@@ -22,7 +23,9 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 INC = os.path.join(os.path.dirname(HERE), "include")
-OUT = os.path.join(HERE, "_build", platform.machine())
+# FVM_BUILD_TAG / FVM_FP32_FLAGS select an alternative build (own directory)
+TAG = os.environ.get("FVM_BUILD_TAG", "")
+OUT = os.path.join(HERE, "_build", platform.machine() + (("-" + TAG) if TAG else ""))
 LIB = os.path.join(OUT, "libfvm2d_gb300.so")
 
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
@@ -36,7 +39,8 @@ CXX_COMMON = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wext
 
 UNITS = [
     ("fvm_kernels_fp64.cu", "nvcc", ["--fmad=false"]),
-    ("fvm_kernels_fp32.cu", "nvcc", []),
+    ("fvm_kernels_fp32.cu", "nvcc", os.environ.get(
+        "FVM_FP32_FLAGS", "-prec-div=false -prec-sqrt=false").split()),
     ("fvm_setup.cu", "nvcc", ["--fmad=false"]),
     ("fvm_batch.cpp", "cxx", []),
     ("fvm_layout.cpp", "cxx", []),

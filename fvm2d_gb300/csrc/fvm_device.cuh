@@ -54,6 +54,15 @@ __device__ __forceinline__ R limit_albada(R ul, R ur, R eps) {
   R bot = sq(ul) + sq(ur) + R(2) * eps;
   return top / bot;
 }
+// FP32: the same value without a branch (bot >= 2 eps > 0), so the warp
+// does not diverge on the sign test
+template <>
+__device__ __forceinline__ float limit_albada<float>(float ul, float ur, float eps) {
+  const float top = (sq(ul) + eps) * ur + (sq(ur) + eps) * ul;
+  const float bot = sq(ul) + sq(ur) + 2.0f * eps;
+  const float r = top / bot;
+  return (ul * ur <= 0.0f) ? 0.0f : r;
+}
 
 // recon.f:4-50 for one variable
 template <typename R>

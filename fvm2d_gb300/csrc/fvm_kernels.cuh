@@ -14,6 +14,10 @@
 
 #include "fvm_device.cuh"
 
+#ifndef FVM_FLUX_MINB32
+#define FVM_FLUX_MINB32 3   // resident CTAs per SM asked of the FP32 flux kernel
+#endif
+
 namespace fvm {
 
 enum { MODE_RESIDUAL = 0, MODE_UPDATE = 1 };
@@ -223,7 +227,7 @@ __device__ __forceinline__ void edge_flux(const ArenaPtrs<R> &A, const MeshConst
 }
 
 template <typename R>
-__global__ void __launch_bounds__(kBlockVerts) k_flux(ArenaPtrs<R> A, int stage, int mode,
+__global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_FLUX_MINB32 : 2) k_flux(ArenaPtrs<R> A, int stage, int mode,
                                                       int irk, int routine) {
   extern __shared__ __align__(32) unsigned char smem_raw[];
   R4<R> *s_flux = reinterpret_cast<R4<R> *>(smem_raw);
