@@ -42,6 +42,7 @@ UNITS = [
     ("fvm_kernels_fp32.cu", "nvcc", os.environ.get(
         "FVM_FP32_FLAGS", "-prec-div=false -prec-sqrt=false").split()),
     ("fvm_setup.cu", "nvcc", ["--fmad=false"]),
+    ("fvm_noalloc.cu", "nvcc", ["--fmad=false"]),
     ("fvm_batch.cpp", "cxx", []),
     ("fvm_layout.cpp", "cxx", []),
     ("fvm_geometry.cpp", "cxx", []),

@@ -227,6 +227,28 @@ int32_t fvm_geom_build(int32_t np, int32_t nt, const double *coord,
                        int32_t cell_type, fvm_geom **out);
 int32_t fvm_geom_free(fvm_geom *g);
 
+/* ---- allocation-free entry point ----------------------------------------- */
+/* No counterpart in the reference.  conres.f:11-31 (RMS and first argmax of
+ * the density change, normalised by the first iteration's value) for
+ * callers that cannot allocate device memory: drivers whose device memory
+ * is owned by an OpenACC / CUDA Fortran data region or by another
+ * framework's pool, where a library cudaMalloc (which also synchronises the
+ * device and may fail mid-run) is not allowed.  prim and prim_old are the
+ * caller's DEVICE arrays prim(4,np) in driver order; the results go to host
+ * memory.  first != 0 sets *fres1 from this call (and returns
+ * FVM_ERR_ZERO_FIRST_RES when it is zero); otherwise *fres1 is the
+ * normaliser.  Scratch is a fixed static device array sized for
+ * FVM_NOALLOC_MAX_POINTS points, held by every GPU that loads the library
+ * until exit; larger np is refused with FVM_ERR_ARG.  Nothing is allocated.
+ * The first call on a device looks up the scratch address on that device,
+ * so make it before any stream capture.  All calls share the scratch and
+ * run on the default stream, synchronously: calls that overlap on the GPU
+ * (from several host threads) race. */
+#define FVM_NOALLOC_MAX_POINTS (1 << 20)
+int32_t fvm_gpu_conres_noalloc(const double *prim, const double *prim_old,
+                               int32_t np, int32_t first, double *fres1,
+                               double *fres, double *fresi, int32_t *iresi);
+
 /* ---- batches: many meshes of uneven size in one launch per kernel ------- */
 /*
  * No counterpart in the reference (which solves one grid per process).  A
