@@ -35,6 +35,31 @@ __device__ __forceinline__ int old_buf(int p, int stage) {
 template <typename R>
 __device__ __forceinline__ R4<R> ld4(const R4<R> *p) { return *p; }
 
+// Bulk prefetch of [p, p + bytes) into L2 (cp.async.bulk.prefetch, no
+// completion to wait for).  The range is shrunk to 16-byte boundaries
+// inside the given one, so nothing outside it is touched.
+__device__ __forceinline__ void prefetch_l2(const void *p, size_t bytes) {
+  const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+  const uintptr_t b = (a + 15) & ~uintptr_t(15);
+  const uintptr_t e = (a + bytes) & ~uintptr_t(15);
+  if (e <= b) return;
+  uintptr_t n = e - b;
+  // the size operand is 32-bit; split very long ranges
+  while (n > 0) {
+    const uint32_t chunk = n > (1u << 20) ? (1u << 20) : (uint32_t)n;
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(b + (e - b - n)), "r"(chunk)
+                 : "memory");
+    n -= chunk;
+  }
+}
+
+// The next block this CTA will process (persistent loop), for prefetching.
+__device__ __forceinline__ const BlockInfo *next_block(const BlockInfo *blocks, const int *work,
+                                                       int w, int nwork) {
+  const int nw = w + gridDim.x;
+  return nw < nwork ? blocks + work[nw] : nullptr;
+}
+
 // ---------------------------------------------------------------------------
 // Viscosity (viscosity.f:2-55) and, at stage 1, the viscous time step
 // (time_step.f:13-20) from the previous mu.  One thread per vertex.
@@ -88,6 +113,17 @@ __global__ void __launch_bounds__(kBlockVerts) k_grad(ArenaPtrs<R> A, int stage,
     const MeshConst &mc = A.mc[bi.mesh];
     const bool visc = mc.iflow != 1;
     const R4<R> *P = A.st[cur_buf(ctl.phase, stage)];
+    if (threadIdx.x == 0) {
+      const BlockInfo *nb = next_block(A.blocks, A.work, w, nwork);
+      if (nb) {
+        const BlockInfo n = *nb;
+        prefetch_l2(A.bt_nodes + n.t0, sizeof(int4) * n.nt);
+        prefetch_l2(P + n.v0, sizeof(R4<R>) * n.nv);
+        prefetch_l2(A.coord + n.v0, sizeof(double2) * n.nv);
+        prefetch_l2(A.vt_rng + n.v0, sizeof(int2) * n.nv);
+        prefetch_l2(A.ais + n.v0, sizeof(double) * n.nv);
+      }
+    }
     // phase 1: one thread per triangle touching the block
     for (int k = threadIdx.x; k < bi.nt; k += blockDim.x) {
       const int4 t = A.bt_nodes[bi.t0 + k];
@@ -242,6 +278,24 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_FLUX_MINB32 
     const MeshConst &mc = A.mc[bi.mesh];
     const int p = ctl.phase;
     const R4<R> *P = A.st[cur_buf(p, stage)];
+    if (threadIdx.x == 0) {
+      const BlockInfo *nb = next_block(A.blocks, A.work, w, nwork);
+      if (nb) {
+        const BlockInfo n = *nb;
+        prefetch_l2(A.be_nodes + n.e0, sizeof(int2) * n.ne);
+        if (sizeof(R) == 8) prefetch_l2(A.be_csl + n.e0, sizeof(D4) * n.ne);
+        else prefetch_l2(A.be_ds + n.e0, sizeof(double2) * n.ne);
+        prefetch_l2(P + n.v0, sizeof(R4<R>) * n.nv);
+        prefetch_l2(A.grad + n.v0, sizeof(Grad<R>) * n.nv);
+        prefetch_l2(A.coord + n.v0, sizeof(double2) * n.nv);
+        prefetch_l2(A.ve_rng + n.v0, sizeof(int2) * n.nv);
+        if (mode == MODE_UPDATE) {
+          prefetch_l2(A.st[old_buf(p, stage)] + n.v0, sizeof(R4<R>) * n.nv);
+          prefetch_l2(A.dt + n.v0, sizeof(R) * n.nv);
+          prefetch_l2(A.cvarea + n.v0, sizeof(double) * n.nv);
+        }
+      }
+    }
     int err = 0;
     // phase 1a: interior edges
     for (int k = threadIdx.x; k < bi.ne; k += blockDim.x) {
