@@ -114,6 +114,8 @@ struct fvm_batch {
   D4 *be_csl = nullptr;
   int4 *bb_nodes = nullptr, *bt_nodes = nullptr;
   double *elarea = nullptr;
+  float2 *be_dxy = nullptr;
+  TriGeo32 *tri_g32 = nullptr;
   MeshConst *mc = nullptr;
   MeshCtl *ctl = nullptr;
   BlockPartial *part = nullptr;
@@ -194,6 +196,8 @@ ArenaPtrs<R> ptrs(const fvm_batch *b) {
   A.bb_nodes = b->bb_nodes;
   A.bt_nodes = b->bt_nodes;
   A.elarea = b->elarea;
+  A.be_dxy = b->be_dxy;
+  A.tri_g32 = b->tri_g32;
   A.sw_nodes = b->sw_nodes;
   A.va_rng = b->va_rng;
   A.va_list = b->va_list;
@@ -357,9 +361,20 @@ cudaError_t put_range(fvm_batch *b, T *base, int64_t off, const std::vector<T> &
 
 int32_t update_work(fvm_batch *b) {
   std::vector<int> work;
+  int flux = -1;
   for (const Slot &s : b->slots)
-    if (s.used)
+    if (s.used) {
       for (int k = 0; k < s.L.nblk; k++) work.push_back((int)(s.off[P_BLK] + k));
+      flux = (flux == -1 || flux == s.par.iflux) ? s.par.iflux : 0;
+    }
+  if (flux < 0) flux = b->cfg.flux;   // empty batch: keep the current kernels
+  if (flux != b->cfg.flux) {
+    b->cfg.flux = flux;                // a different flux kernel: re-capture
+    if (b->graph) {
+      cudaGraphExecDestroy(b->graph);
+      b->graph = nullptr;
+    }
+  }
   const int n = (int)work.size();
   if (n) FVM_TRY(b, cudaMemcpyAsync(b->work, work.data(), n * sizeof(int), cudaMemcpyHostToDevice, b->stream));
   FVM_TRY(b, cudaMemcpyAsync(b->nwork, &n, sizeof(int), cudaMemcpyHostToDevice, b->stream));
@@ -535,6 +550,10 @@ extern "C" int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *cap
   TRYB(dalloc(O, &b->bb_nodes, (size_t)c.boundary_entries));
   TRYB(dalloc(O, &b->bt_nodes, (size_t)c.tri_entries));
   TRYB(dalloc(O, &b->elarea, (size_t)c.triangles));
+  if (precision == FVM_PREC_FP32) {
+    TRYB(dalloc(O, &b->be_dxy, (size_t)c.edge_entries));
+    TRYB(dalloc(O, &b->tri_g32, (size_t)c.triangles));
+  }
   TRYB(dalloc(O, &b->sw_nodes, (size_t)c.solid_edges));
   TRYB(dalloc(O, &b->mc, (size_t)c.meshes));
   TRYB(dalloc(O, &b->ctl, (size_t)c.meshes));
@@ -679,6 +698,35 @@ extern "C" int32_t fvm_batch_add(fvm_batch *b, const fvm_params *par, const fvm_
     q.y += v0;
   }
   std::vector<double> elarea(m->elarea, m->elarea + L.nt);
+  // FP32 copies of FP64 differences (rounded once) for the FP32 kernels
+  std::vector<float2> be_dxy;
+  std::vector<TriGeo32> tri_g32;
+  if (b->prec == FVM_PREC_FP32) {
+    be_dxy.resize(L.be_edge.size());
+    for (size_t k = 0; k < L.be_edge.size(); k++) {
+      const int e = L.be_edge[k];
+      const int n1 = m->edge[2 * e] - 1, n2 = m->edge[2 * e + 1] - 1;
+      be_dxy[k] = make_float2((float)(m->coord[2 * n2] - m->coord[2 * n1]),
+                              (float)(m->coord[2 * n2 + 1] - m->coord[2 * n1 + 1]));
+    }
+    tri_g32.resize(L.nt);
+    for (int t = 0; t < L.nt; t++) {
+      const int a = m->elem[3 * t] - 1, c2 = m->elem[3 * t + 1] - 1, c3 = m->elem[3 * t + 2] - 1;
+      const double x1 = m->coord[2 * a], y1 = m->coord[2 * a + 1];
+      const double x2 = m->coord[2 * c2], y2 = m->coord[2 * c2 + 1];
+      const double x3 = m->coord[2 * c3], y3 = m->coord[2 * c3 + 1];
+      TriGeo32 g;
+      g.dbxx[0] = (float)(y2 - y3);
+      g.dbxx[1] = (float)(y3 - y1);
+      g.dbxx[2] = (float)(y1 - y2);
+      g.dbyy[0] = (float)(x3 - x2);
+      g.dbyy[1] = (float)(x1 - x3);
+      g.dbyy[2] = (float)(x2 - x1);
+      g.areat = (float)(0.25 / m->elarea[t]);
+      g.pad = 0.f;
+      tri_g32[t] = g;
+    }
+  }
   MeshConst mc = make_const(*par);
   mc.v0 = v0;
   mc.nv = np;
@@ -722,6 +770,8 @@ extern "C" int32_t fvm_batch_add(fvm_batch *b, const fvm_params *par, const fvm_
   PUT(put_range(b, b->bb_nodes, S.off[P_BB], bb));
   PUT(put_range(b, b->bt_nodes, S.off[P_BT], bt));
   PUT(put_range(b, b->elarea, S.off[P_TRI], elarea));
+  if (b->be_dxy) PUT(put_range(b, b->be_dxy, S.off[P_BE], be_dxy));
+  if (b->tri_g32) PUT(put_range(b, b->tri_g32, S.off[P_TRI], tri_g32));
   PUT(put_range(b, b->sw_nodes, S.off[P_SW], sw));
   PUT(cudaMemcpyAsync(b->mc + sid, &mc, sizeof(mc), cudaMemcpyHostToDevice, b->stream));
   PUT(cudaMemcpyAsync(b->ctl + sid, &ctl, sizeof(ctl), cudaMemcpyHostToDevice, b->stream));

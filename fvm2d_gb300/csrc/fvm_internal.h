@@ -108,6 +108,13 @@ struct alignas(8 * sizeof(R) > 32 ? 32 : 8 * sizeof(R)) Grad {
 struct alignas(32) D4 {
   double x, y, z, w;
 };
+// FP32 copies of FP64 geometric differences, rounded once (used by the FP32
+// kernels so their hot loops execute no FP64 instruction)
+struct alignas(16) TriGeo32 {
+  float dbxx[3], dbyy[3];   // green_gauss.f:108-113: y2-y3, y3-y1, y1-y2 / x3-x2, x1-x3, x2-x1
+  float areat;              // 0.25/elarea (green_gauss.f:180)
+  float pad;
+};
 
 // Device pointers of an arena (all arena-global indices).
 template <typename R>
@@ -137,6 +144,8 @@ struct ArenaPtrs {
   const int4 *bb_nodes;   // boundary entries (n1, n2, type, -)
   const int4 *bt_nodes;   // triangle entries (n1, n2, n3, arena triangle)
   const double *elarea;   // per arena triangle
+  const float2 *be_dxy;   // FP32 path: x(n2)-x(n1), y(n2)-y(n1) of each edge entry
+  const TriGeo32 *tri_g32; // FP32 path: per arena triangle
   // solid edges per mesh for clcd (n1, n2) in beindx order
   const int2 *sw_nodes;
   // all-edge incidence (limitgrad.f loops over netot edges)

@@ -15,7 +15,7 @@
 #include "fvm_device.cuh"
 
 #ifndef FVM_FLUX_MINB32
-#define FVM_FLUX_MINB32 3   // resident CTAs per SM asked of the FP32 flux kernel
+#define FVM_FLUX_MINB32 4   // resident CTAs per SM asked of the FP32 flux kernel
 #endif
 
 namespace fvm {
@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(kBlockVerts) k_grad(ArenaPtrs<R> A, int stage,
         const BlockInfo n = *nb;
         prefetch_l2(A.bt_nodes + n.t0, sizeof(int4) * n.nt);
         prefetch_l2(P + n.v0, sizeof(R4<R>) * n.nv);
-        prefetch_l2(A.coord + n.v0, sizeof(double2) * n.nv);
+        if (sizeof(R) == 8) prefetch_l2(A.coord + n.v0, sizeof(double2) * n.nv);
         prefetch_l2(A.vt_rng + n.v0, sizeof(int2) * n.nv);
         prefetch_l2(A.ais + n.v0, sizeof(double) * n.nv);
       }
@@ -127,10 +127,23 @@ __global__ void __launch_bounds__(kBlockVerts) k_grad(ArenaPtrs<R> A, int stage,
     // phase 1: one thread per triangle touching the block
     for (int k = threadIdx.x; k < bi.nt; k += blockDim.x) {
       const int4 t = A.bt_nodes[bi.t0 + k];
-      const double2 c1 = A.coord[t.x], c2 = A.coord[t.y], c3 = A.coord[t.z];
       const R4<R> p1 = P[t.x], p2 = P[t.y], p3 = P[t.z];
-      const R dbxx[3] = {R(c2.y - c3.y), R(c3.y - c1.y), R(c1.y - c2.y)};
-      const R dbyy[3] = {R(c3.x - c2.x), R(c1.x - c3.x), R(c2.x - c1.x)};
+      R dbxx[3], dbyy[3];
+      if constexpr (sizeof(R) == 4) {
+        const TriGeo32 tg = A.tri_g32[t.w];
+        for (int j = 0; j < 3; j++) {
+          dbxx[j] = tg.dbxx[j];
+          dbyy[j] = tg.dbyy[j];
+        }
+      } else {
+        const double2 c1 = A.coord[t.x], c2 = A.coord[t.y], c3 = A.coord[t.z];
+        dbxx[0] = c2.y - c3.y;
+        dbxx[1] = c3.y - c1.y;
+        dbxx[2] = c1.y - c2.y;
+        dbyy[0] = c3.x - c2.x;
+        dbyy[1] = c1.x - c3.x;
+        dbyy[2] = c2.x - c1.x;
+      }
       TriSmem<R> ts;
 #pragma unroll
       for (int q = 0; q < 4; q++) {
@@ -162,7 +175,9 @@ __global__ void __launch_bounds__(kBlockVerts) k_grad(ArenaPtrs<R> A, int stage,
                       R(mc.gamma1);
         const R efx = txx * um + txy * vm + gpr * ext;
         const R efy = txy * um + tyy * vm + gpr * eyt;
-        const R areat = R(0.25 / A.elarea[t.w]);
+        R areat;
+        if constexpr (sizeof(R) == 4) areat = A.tri_g32[t.w].areat;
+        else areat = 0.25 / A.elarea[t.w];
         R *sv = s_vis + 9 * k;
 #pragma unroll
         for (int j = 0; j < 3; j++) {
@@ -225,23 +240,56 @@ __global__ void __launch_bounds__(kBlockVerts) k_grad(ArenaPtrs<R> A, int stage,
 // applied (MODE_UPDATE).  At stage 3 of an iteration it also produces the
 // conres.f partials and the density/pressure positivity check.
 // ---------------------------------------------------------------------------
+// Mesh constants of the flux pass in the state precision, loaded once per
+// block (keeps conversions out of the edge loop).
 template <typename R>
-__device__ __forceinline__ void edge_flux(const ArenaPtrs<R> &A, const MeshConst &mc,
+struct FluxConst {
+  R a11, a12, a21, a22, eps, gamma, gamma1, pi;
+  int ilimit, iflux, rotate_back;
+};
+
+template <typename R>
+__device__ __forceinline__ FluxConst<R> flux_const(const MeshConst &mc) {
+  FluxConst<R> c;
+  c.a11 = R(mc.albada11);
+  c.a12 = R(mc.albada12);
+  c.a21 = R(mc.albada21);
+  c.a22 = R(mc.albada22);
+  c.eps = R(mc.epsilon);
+  c.gamma = R(mc.gamma);
+  c.gamma1 = R(mc.gamma1);
+  c.pi = R(mc.pi);
+  c.ilimit = mc.ilimit;
+  c.iflux = mc.iflux;
+  c.rotate_back = mc.bugcompat ? 0 : 1;
+  return c;
+}
+
+// FLUX = 1/2/3 compiles one Riemann solver only (every resident mesh uses
+// it); FLUX = 0 dispatches on the mesh's iflux.
+template <typename R, int FLUX>
+__device__ __forceinline__ void edge_flux(const ArenaPtrs<R> &A, const FluxConst<R> &fc,
                                           const R4<R> *P, int e, R f[4], int &err) {
   const int2 nn = A.be_nodes[e];
   const R4<R> p1 = P[nn.x], p2 = P[nn.y];
   const Grad<R> g1 = A.grad[nn.x], g2 = A.grad[nn.y];
-  const double2 c1 = A.coord[nn.x], c2 = A.coord[nn.y];
-  const R dx = R(c2.x - c1.x), dy = R(c2.y - c1.y);
+  R dx, dy;
+  if constexpr (sizeof(R) == 4) {
+    const float2 d = A.be_dxy[e];
+    dx = d.x;
+    dy = d.y;
+  } else {
+    const double2 c1 = A.coord[nn.x], c2 = A.coord[nn.y];
+    dx = c2.x - c1.x;
+    dy = c2.y - c1.y;
+  }
   R pl[4], pr[4];
-  const R a11 = R(mc.albada11), a12 = R(mc.albada12), a21 = R(mc.albada21), a22 = R(mc.albada22);
-  const R eps = R(mc.epsilon);
 #pragma unroll
   for (int q = 0; q < 4; q++)
     recon1<R>(comp(p1, q), comp(p2, q), g1.qx[q], g1.qy[q], g2.qx[q], g2.qy[q], dx, dy,
-              mc.ilimit, a11, a12, a21, a22, eps, pl[q], pr[q]);
+              fc.ilimit, fc.a11, fc.a12, fc.a21, fc.a22, fc.eps, pl[q], pr[q]);
   R ct, st, len;
-  if (sizeof(R) == 8) {
+  if constexpr (sizeof(R) == 8) {
     const D4 csl = A.be_csl[e];
     ct = R(csl.x);
     st = R(csl.y);
@@ -253,16 +301,17 @@ __device__ __forceinline__ void edge_flux(const ArenaPtrs<R> &A, const MeshConst
     ct = d1 / len;
     st = d2 / len;
   }
-  if (mc.iflux == 1) {
-    if (!roe_flux<R>(ct, st, len, pl, pr, R(mc.gamma), R(mc.gamma1), f)) err = 1;
-  } else if (mc.iflux == 2) {
-    kfvs_flux<R>(ct, st, len, pl, pr, R(mc.gamma1), R(mc.pi), f);
+  const int which = FLUX ? FLUX : fc.iflux;
+  if (which == 1) {
+    if (!roe_flux<R>(ct, st, len, pl, pr, fc.gamma, fc.gamma1, f)) err = 1;
+  } else if (which == 2) {
+    kfvs_flux<R>(ct, st, len, pl, pr, fc.gamma1, fc.pi, f);
   } else {
-    hllc_flux<R>(ct, st, len, pl, pr, R(mc.gamma), R(mc.gamma1), mc.bugcompat ? 0 : 1, f);
+    hllc_flux<R>(ct, st, len, pl, pr, fc.gamma, fc.gamma1, fc.rotate_back, f);
   }
 }
 
-template <typename R>
+template <typename R, int FLUX>
 __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_FLUX_MINB32 : 2) k_flux(ArenaPtrs<R> A, int stage, int mode,
                                                       int irk, int routine) {
   extern __shared__ __align__(32) unsigned char smem_raw[];
@@ -284,10 +333,13 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_FLUX_MINB32 
         const BlockInfo n = *nb;
         prefetch_l2(A.be_nodes + n.e0, sizeof(int2) * n.ne);
         if (sizeof(R) == 8) prefetch_l2(A.be_csl + n.e0, sizeof(D4) * n.ne);
-        else prefetch_l2(A.be_ds + n.e0, sizeof(double2) * n.ne);
+        else {
+          prefetch_l2(A.be_ds + n.e0, sizeof(double2) * n.ne);
+          prefetch_l2(A.be_dxy + n.e0, sizeof(float2) * n.ne);
+        }
         prefetch_l2(P + n.v0, sizeof(R4<R>) * n.nv);
         prefetch_l2(A.grad + n.v0, sizeof(Grad<R>) * n.nv);
-        prefetch_l2(A.coord + n.v0, sizeof(double2) * n.nv);
+        if (sizeof(R) == 8) prefetch_l2(A.coord + n.v0, sizeof(double2) * n.nv);
         prefetch_l2(A.ve_rng + n.v0, sizeof(int2) * n.nv);
         if (mode == MODE_UPDATE) {
           prefetch_l2(A.st[old_buf(p, stage)] + n.v0, sizeof(R4<R>) * n.nv);
@@ -297,10 +349,11 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_FLUX_MINB32 
       }
     }
     int err = 0;
+    const FluxConst<R> fc = flux_const<R>(mc);
     // phase 1a: interior edges
     for (int k = threadIdx.x; k < bi.ne; k += blockDim.x) {
       R f[4];
-      edge_flux<R>(A, mc, P, bi.e0 + k, f, err);
+      edge_flux<R, FLUX>(A, fc, P, bi.e0 + k, f, err);
       R4<R> o;
       o.x = f[0];
       o.y = f[1];

@@ -31,7 +31,12 @@ namespace fvm {
                           int irk, int routine) {                                          \
     size_t sm = smem_flux(c, (R *)nullptr);                                                \
     if (sm > kMaxSmem) return cudaErrorInvalidConfiguration;                              \
-    k_flux<R><<<c.grid, kBlockVerts, sm, c.stream>>>(A, stage, mode, irk, routine);         \
+    switch (c.flux) {                                                                      \
+      case 1: k_flux<R, 1><<<c.grid, kBlockVerts, sm, c.stream>>>(A, stage, mode, irk, routine); break; \
+      case 2: k_flux<R, 2><<<c.grid, kBlockVerts, sm, c.stream>>>(A, stage, mode, irk, routine); break; \
+      case 3: k_flux<R, 3><<<c.grid, kBlockVerts, sm, c.stream>>>(A, stage, mode, irk, routine); break; \
+      default: k_flux<R, 0><<<c.grid, kBlockVerts, sm, c.stream>>>(A, stage, mode, irk, routine); \
+    }                                                                                      \
     return cudaGetLastError();                                                             \
   }                                                                                        \
   cudaError_t launch_sa(const ArenaPtrs<R> &A, const LaunchCfg &c, int stage, int routine) {\
@@ -77,7 +82,13 @@ namespace fvm {
     cudaError_t e = cudaFuncSetAttribute(k_grad<R>,                                        \
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g); \
     if (e == cudaSuccess)                                                                  \
-      e = cudaFuncSetAttribute(k_flux<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f); \
+      e = cudaFuncSetAttribute(k_flux<R, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f); \
+    if (e == cudaSuccess)                                                                  \
+      e = cudaFuncSetAttribute(k_flux<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f); \
+    if (e == cudaSuccess)                                                                  \
+      e = cudaFuncSetAttribute(k_flux<R, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f); \
+    if (e == cudaSuccess)                                                                  \
+      e = cudaFuncSetAttribute(k_flux<R, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f); \
     if (e == cudaSuccess)                                                                  \
       e = cudaFuncSetAttribute(k_sa<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s); \
     return e;                                                                              \

@@ -15,6 +15,7 @@ struct LaunchCfg {
   int max_tri;       // max triangle entries of any block
   int max_slots;     // max edge slots (interior + 2 x boundary) of any block
   bool viscous;      // any mesh viscous (gradient-pass shared memory)
+  int flux;          // 1/2/3: every mesh uses that Riemann solver; 0: mixed
   cudaStream_t stream;
 };
 
