@@ -552,7 +552,7 @@ extern "C" int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *cap
   TRYB(dalloc(O, &b->elarea, (size_t)c.triangles));
   if (precision == FVM_PREC_FP32) {
     TRYB(dalloc(O, &b->be_dxy, (size_t)c.edge_entries));
-    TRYB(dalloc(O, &b->tri_g32, (size_t)c.triangles));
+    TRYB(dalloc(O, &b->tri_g32, (size_t)c.tri_entries));
   }
   TRYB(dalloc(O, &b->sw_nodes, (size_t)c.solid_edges));
   TRYB(dalloc(O, &b->mc, (size_t)c.meshes));
@@ -709,8 +709,9 @@ extern "C" int32_t fvm_batch_add(fvm_batch *b, const fvm_params *par, const fvm_
       be_dxy[k] = make_float2((float)(m->coord[2 * n2] - m->coord[2 * n1]),
                               (float)(m->coord[2 * n2 + 1] - m->coord[2 * n1 + 1]));
     }
-    tri_g32.resize(L.nt);
-    for (int t = 0; t < L.nt; t++) {
+    tri_g32.resize(L.bt_nodes.size());
+    for (size_t k = 0; k < L.bt_nodes.size(); k++) {
+      const int t = L.bt_nodes[k].w;   // driver triangle of this block entry
       const int a = m->elem[3 * t] - 1, c2 = m->elem[3 * t + 1] - 1, c3 = m->elem[3 * t + 2] - 1;
       const double x1 = m->coord[2 * a], y1 = m->coord[2 * a + 1];
       const double x2 = m->coord[2 * c2], y2 = m->coord[2 * c2 + 1];
@@ -724,7 +725,7 @@ extern "C" int32_t fvm_batch_add(fvm_batch *b, const fvm_params *par, const fvm_
       g.dbyy[2] = (float)(x2 - x1);
       g.areat = (float)(0.25 / m->elarea[t]);
       g.pad = 0.f;
-      tri_g32[t] = g;
+      tri_g32[k] = g;
     }
   }
   MeshConst mc = make_const(*par);
@@ -771,7 +772,7 @@ extern "C" int32_t fvm_batch_add(fvm_batch *b, const fvm_params *par, const fvm_
   PUT(put_range(b, b->bt_nodes, S.off[P_BT], bt));
   PUT(put_range(b, b->elarea, S.off[P_TRI], elarea));
   if (b->be_dxy) PUT(put_range(b, b->be_dxy, S.off[P_BE], be_dxy));
-  if (b->tri_g32) PUT(put_range(b, b->tri_g32, S.off[P_TRI], tri_g32));
+  if (b->tri_g32) PUT(put_range(b, b->tri_g32, S.off[P_BT], tri_g32));
   PUT(put_range(b, b->sw_nodes, S.off[P_SW], sw));
   PUT(cudaMemcpyAsync(b->mc + sid, &mc, sizeof(mc), cudaMemcpyHostToDevice, b->stream));
   PUT(cudaMemcpyAsync(b->ctl + sid, &ctl, sizeof(ctl), cudaMemcpyHostToDevice, b->stream));

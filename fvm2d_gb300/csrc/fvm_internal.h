@@ -145,7 +145,7 @@ struct ArenaPtrs {
   const int4 *bt_nodes;   // triangle entries (n1, n2, n3, arena triangle)
   const double *elarea;   // per arena triangle
   const float2 *be_dxy;   // FP32 path: x(n2)-x(n1), y(n2)-y(n1) of each edge entry
-  const TriGeo32 *tri_g32; // FP32 path: per arena triangle
+  const TriGeo32 *tri_g32; // FP32 path: per triangle entry of the blocks (bt_* order)
   // solid edges per mesh for clcd (n1, n2) in beindx order
   const int2 *sw_nodes;
   // all-edge incidence (limitgrad.f loops over netot edges)

@@ -118,6 +118,7 @@ __global__ void __launch_bounds__(kBlockVerts) k_grad(ArenaPtrs<R> A, int stage,
       if (nb) {
         const BlockInfo n = *nb;
         prefetch_l2(A.bt_nodes + n.t0, sizeof(int4) * n.nt);
+        if (sizeof(R) == 4) prefetch_l2(A.tri_g32 + n.t0, sizeof(TriGeo32) * n.nt);
         prefetch_l2(P + n.v0, sizeof(R4<R>) * n.nv);
         if (sizeof(R) == 8) prefetch_l2(A.coord + n.v0, sizeof(double2) * n.nv);
         prefetch_l2(A.vt_rng + n.v0, sizeof(int2) * n.nv);
@@ -130,7 +131,7 @@ __global__ void __launch_bounds__(kBlockVerts) k_grad(ArenaPtrs<R> A, int stage,
       const R4<R> p1 = P[t.x], p2 = P[t.y], p3 = P[t.z];
       R dbxx[3], dbyy[3];
       if constexpr (sizeof(R) == 4) {
-        const TriGeo32 tg = A.tri_g32[t.w];
+        const TriGeo32 tg = A.tri_g32[bi.t0 + k];
         for (int j = 0; j < 3; j++) {
           dbxx[j] = tg.dbxx[j];
           dbyy[j] = tg.dbyy[j];
@@ -176,7 +177,7 @@ __global__ void __launch_bounds__(kBlockVerts) k_grad(ArenaPtrs<R> A, int stage,
         const R efx = txx * um + txy * vm + gpr * ext;
         const R efy = txy * um + tyy * vm + gpr * eyt;
         R areat;
-        if constexpr (sizeof(R) == 4) areat = A.tri_g32[t.w].areat;
+        if constexpr (sizeof(R) == 4) areat = A.tri_g32[bi.t0 + k].areat;
         else areat = 0.25 / A.elarea[t.w];
         R *sv = s_vis + 9 * k;
 #pragma unroll
