@@ -419,6 +419,90 @@ def run_reference(args):
     replicas.finish()
 
 
+def fp64_iteration_ladder(sizes=(5000, 20000, 80000, 200000, 400000)):
+    """Per-iteration time of the plain FP64 single-mesh GPU path (one mesh per
+    batch, CUDA-event timed) on a ladder of grid sizes, Euler and laminar."""
+    import torch
+
+    import fvm2d_gb300 as F
+    from fvm2d_gb300 import serve
+    from fvm2d_gb300.batch import Batch
+    out = {}
+    for lam in (False, True):
+        pts = []
+        for n in sizes:
+            req = serve.Request(rid=0, arrival=0.0, thickness=0.12, camber=0.02, camber_pos=0.4,
+                                npts=n, laminar=lam, mach=0.6, aoa_deg=2.0,
+                                rey=5000.0 if lam else 0.0, seed=0)
+            prep = serve.prepare(req, F.FP64)
+            P = prep.np
+            b = Batch(F.FP64, vertices=P, meshes=1, viscous=True)
+            s = b.add_prepared(prep)
+            b.start(s, 40)
+            b.step(3)
+            b.sync()
+            ext = torch.cuda.ExternalStream(b.stream())
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            k = 10 if P < 100000 else 5
+            e0.record(ext)
+            b.step(k)
+            e1.record(ext)
+            b.sync()
+            pts.append((P, e0.elapsed_time(e1) / 1e3 / k))
+            b.close()
+        out["laminar" if lam else "euler"] = pts
+    return out
+
+
+def interp_time(ladder, P):
+    """Per-iteration time at P vertices: log-log interpolation on the
+    ladder, proportional to P beyond its ends."""
+    import numpy as np
+    ps = np.array([p for p, _ in ladder], dtype=float)
+    ts = np.array([t for _, t in ladder], dtype=float)
+    if P <= ps[0]:
+        return float(ts[0] * P / ps[0])
+    if P >= ps[-1]:
+        return float(ts[-1] * P / ps[-1])
+    return float(np.exp(np.interp(np.log(P), np.log(ps), np.log(ts))))
+
+
+def run_serve(args):
+    """Batched FP32 serving of the request workload; converged solves/s and
+    latency percentiles, with the FP64 single-mesh path's solves/s."""
+    import torch
+
+    import fvm2d_gb300 as F
+    from fvm2d_gb300 import serve
+    torch.cuda.init()
+    reqs = serve.generate_requests(n=args.requests, rate=args.rate, seed=args.seed)
+    srv = serve.Server(vertices=args.arena_vertices, meshes=512, chunk=args.chunk,
+                       workers=args.workers, max_iter=args.max_iter, minres=args.minres)
+    res, stats = srv.run(reqs)
+    srv.close()
+    ladder = fp64_iteration_ladder()
+    t64 = sum(interp_time(ladder["laminar" if r.laminar else "euler"], r.npts) * r.niter
+              for r in res if r.status == 0)
+    solves64 = stats["completed_ok"] / t64
+    line = {"metric": METRIC, "mode": "serve", "value": stats["solves_per_s"],
+            "unit": "converged solves/s", "higher_is_better": True, "n_gpus": 1,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"{args.requests} NACA 4-digit requests, Poisson {args.rate}/s, "
+                                   "5k-400k vertices log-uniform, 70% Euler / 30% laminar, "
+                                   f"stop at drop {args.minres} or {args.max_iter} iterations",
+                       "arena_vertices": args.arena_vertices, "chunk": args.chunk},
+            "latency_s": {"p50": stats["p50_latency_s"], "p99": stats["p99_latency_s"]},
+            "stats": stats,
+            "vs_fp64_gpu": {"solves_per_s": solves64, "ratio": stats["solves_per_s"] / solves64,
+                            "what": "FP64 single-mesh path, one solve at a time: per-iteration "
+                                    "time measured on a ladder of grid sizes (CUDA events), "
+                                    "interpolated per request, times the iterations the request "
+                                    "took", "ladder_s_per_iteration": ladder},
+            "vs_baseline": None}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -428,11 +512,24 @@ def main():
     ap.add_argument("--flux", choices=sorted(FLUX_CODES), default="roe")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--quick", action="store_true", help="skip the side measurements")
+    ap.add_argument("--mode", choices=["throughput", "serve"], default="throughput")
+    ap.add_argument("--requests", type=int, default=512)
+    ap.add_argument("--rate", type=float, default=20.0)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--arena-vertices", type=int, default=6_000_000)
+    ap.add_argument("--chunk", type=int, default=50)
+    ap.add_argument("--workers", type=int, default=8)
+    ap.add_argument("--max-iter", type=int, default=5000)
+    ap.add_argument("--minres", type=float, default=1e-6)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     if args.impl == "reference":
         run_reference(args)
+    elif args.mode == "serve":
+        from fvm2d_gb300 import build
+        build.build()
+        run_serve(args)
     else:
         from fvm2d_gb300 import build
         build.build()

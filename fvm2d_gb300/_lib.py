@@ -118,6 +118,11 @@ SIGNATURES = {
     "fvm_layout_stats": (C.c_int32, [C.POINTER(FvmMesh), C.POINTER(C.c_int64)]),
     "fvm_gpu_conres_noalloc": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, _pd,
                                            _pd, _pd, _pi]),
+    "fvm_batch_prepare": (C.c_int32, [C.POINTER(FvmParams), C.POINTER(FvmMesh),
+                                      C.POINTER(C.c_void_p)]),
+    "fvm_batch_add_prepared": (C.c_int32, [C.c_void_p, C.c_void_p, _pi]),
+    "fvm_prepared_free": (C.c_int32, [C.c_void_p]),
+    "fvm_prepared_bytes": (C.c_int64, [C.c_void_p, C.c_int32]),
 }
 
 _lib = None

@@ -23,6 +23,35 @@ def layout_stats(mesh) -> dict:
     return dict(zip(keys, [int(x) for x in out]))
 
 
+class Prepared:
+    """A mesh whose block layout has been built on the host (thread safe,
+    no device work); admit it with Batch.add_prepared."""
+
+    def __init__(self, params: L.FvmParams, mesh):
+        m = mesh if isinstance(mesh, MeshArrays) else MeshArrays(mesh)
+        ms = m.struct()
+        h = C.c_void_p()
+        check(L.lib().fvm_batch_prepare(C.byref(params), C.byref(ms), C.byref(h)),
+              "fvm_batch_prepare")
+        self.h = h
+        self.mesh = m
+        self.np = m.np
+
+    def nbytes(self, precision: int) -> int:
+        return int(L.lib().fvm_prepared_bytes(self.h, precision))
+
+    def release(self):
+        if self.h is not None and self.h.value:
+            L.lib().fvm_prepared_free(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
 class Batch:
     def __init__(self, precision: int, vertices: int, meshes: int, viscous: bool = False,
                  **caps):
@@ -66,6 +95,18 @@ class Batch:
             if e.status == L.ERR_CAPACITY:
                 return None
             raise
+
+    def add_prepared(self, prep: Prepared):
+        """Upload a prepared mesh; returns its slot or None when the arena has
+        no room (the prepared mesh is kept for a later try)."""
+        slot = C.c_int32(-1)
+        st = L.lib().fvm_batch_add_prepared(self.h, prep.h, C.byref(slot))
+        if st == L.ERR_CAPACITY:
+            return None
+        check(st, "fvm_batch_add_prepared")
+        prep.h = None          # taken by the batch
+        self._meshes[slot.value] = prep.mesh
+        return slot.value
 
     def remove(self, slot: int):
         check(L.lib().fvm_batch_remove(self.h, slot), "fvm_batch_remove")

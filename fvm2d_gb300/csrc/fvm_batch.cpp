@@ -597,16 +597,110 @@ extern "C" int32_t fvm_batch_destroy(fvm_batch *b) {
   return FVM_OK;
 }
 
-extern "C" int32_t fvm_batch_add(fvm_batch *b, const fvm_params *par, const fvm_mesh *m,
-                                 int32_t *slot_out) {
-  if (!b || !par || !m || !slot_out) return FVM_ERR_ARG;
-  *slot_out = -1;
+// A mesh ready to upload: block layout plus every host array the device
+// needs, in renumbered order with mesh-relative indices.
+struct fvm_prepared {
+  fvm_params par{};
+  MeshLayout L;
+  std::vector<double2> coord;
+  std::vector<double> ais, cvarea, drmin, wd, elarea;
+  std::vector<int> orig;
+  std::vector<double2> be_ds;
+  std::vector<float2> be_dxy;      // FP32 batches
+  std::vector<TriGeo32> tri_g32;   // FP32 batches
+};
+
+extern "C" int32_t fvm_batch_prepare(const fvm_params *par, const fvm_mesh *m, fvm_prepared **out) {
+  if (!par || !m || !out) return FVM_ERR_ARG;
+  *out = nullptr;
   if (m->np < 3 || m->nt < 1 || m->netot < 1 || m->ne < 1 || !m->coord || !m->elem ||
       !m->ptype || !m->edge || !m->iedge || !m->ds || !m->elarea || !m->cvarea ||
       !m->mcarea || !m->drmin)
     return FVM_ERR_ARG;
   if (par->iflow == FVM_TURBULENT && !m->wd) return FVM_ERR_ARG;
   if (m->nbe > 0 && !m->beindx) return FVM_ERR_ARG;
+  fvm_prepared *P = new (std::nothrow) fvm_prepared();
+  if (!P) return FVM_ERR_NOMEM;
+  P->par = *par;
+  int32_t st = build_layout(*m, kBlockVerts, P->L);
+  if (st != FVM_OK) {
+    delete P;
+    return st;
+  }
+  const MeshLayout &L = P->L;
+  const int np = L.np;
+  P->coord.resize(np);
+  P->ais.resize(np);
+  P->cvarea.resize(np);
+  P->drmin.resize(np);
+  P->wd.assign(np, 1.0);
+  P->orig.resize(np);
+  const double n1b6 = 1.0 / 6.0;
+  for (int v = 0; v < np; v++) {
+    const int o = L.perm[v];
+    P->coord[v] = make_double2(m->coord[2 * o], m->coord[2 * o + 1]);
+    P->ais[v] = n1b6 / m->mcarea[o];   // green_gauss.f:34
+    P->cvarea[v] = m->cvarea[o];
+    P->drmin[v] = m->drmin[o];
+    if (m->wd) P->wd[v] = m->wd[o];
+    P->orig[v] = o + 1;
+  }
+  P->elarea.assign(m->elarea, m->elarea + L.nt);
+  P->be_ds.resize(L.be_edge.size());
+  P->be_dxy.resize(L.be_edge.size());
+  for (size_t k = 0; k < L.be_edge.size(); k++) {
+    const int e = L.be_edge[k];
+    P->be_ds[k] = make_double2(m->ds[2 * e], m->ds[2 * e + 1]);
+    // FP32 copies of FP64 differences, rounded once
+    const int n1 = m->edge[2 * e] - 1, n2 = m->edge[2 * e + 1] - 1;
+    P->be_dxy[k] = make_float2((float)(m->coord[2 * n2] - m->coord[2 * n1]),
+                               (float)(m->coord[2 * n2 + 1] - m->coord[2 * n1 + 1]));
+  }
+  P->tri_g32.resize(L.bt_nodes.size());
+  for (size_t k = 0; k < L.bt_nodes.size(); k++) {
+    const int t = L.bt_nodes[k].w;   // driver triangle of this block entry
+    const int a = m->elem[3 * t] - 1, c2 = m->elem[3 * t + 1] - 1, c3 = m->elem[3 * t + 2] - 1;
+    const double x1 = m->coord[2 * a], y1 = m->coord[2 * a + 1];
+    const double x2 = m->coord[2 * c2], y2 = m->coord[2 * c2 + 1];
+    const double x3 = m->coord[2 * c3], y3 = m->coord[2 * c3 + 1];
+    TriGeo32 g;
+    g.dbxx[0] = (float)(y2 - y3);
+    g.dbxx[1] = (float)(y3 - y1);
+    g.dbxx[2] = (float)(y1 - y2);
+    g.dbyy[0] = (float)(x3 - x2);
+    g.dbyy[1] = (float)(x1 - x3);
+    g.dbyy[2] = (float)(x2 - x1);
+    g.areat = (float)(0.25 / m->elarea[t]);
+    g.pad = 0.f;
+    P->tri_g32[k] = g;
+  }
+  *out = P;
+  return FVM_OK;
+}
+
+extern "C" int32_t fvm_prepared_free(fvm_prepared *prep) {
+  delete prep;
+  return FVM_OK;
+}
+
+extern "C" int64_t fvm_prepared_bytes(const fvm_prepared *prep, int32_t precision) {
+  if (!prep) return -1;
+  const MeshLayout &L = prep->L;
+  const int64_t r = precision == FVM_PREC_FP64 ? 8 : 4;
+  const int64_t V = L.np;
+  int64_t bytes = V * (3 * 4 * r + 8 * r + 4 * r + 4 * r + 5 * r + 16 + 4 * 8 + 4 + 1 + 3 * 8);
+  bytes += (int64_t)L.be_nodes.size() * (8 + 16 + (precision == FVM_PREC_FP64 ? 32 : 8));
+  bytes += (int64_t)L.bb_nodes.size() * 16 + (int64_t)L.bt_nodes.size() * (16 + (r == 4 ? 32 : 0));
+  bytes += (int64_t)L.nt * 8 + (int64_t)L.ve_list.size() * 2 + (int64_t)L.vt_list.size() * 2;
+  bytes += (int64_t)L.va_list.size() * 4 + (int64_t)L.sw_nodes.size() * 8;
+  bytes += (int64_t)L.nblk * (sizeof(BlockInfo) + sizeof(BlockPartial) + 4);
+  return bytes;
+}
+
+extern "C" int32_t fvm_batch_add_prepared(fvm_batch *b, fvm_prepared *prep, int32_t *slot_out) {
+  if (!b || !prep || !slot_out) return FVM_ERR_ARG;
+  *slot_out = -1;
+  const fvm_params *par = &prep->par;
   if (par->precision != b->prec) return FVM_ERR_ARG;
   if (par->iflow != FVM_INVISCID && !b->caps.viscous) return FVM_ERR_ARG;
   int sid = -1;
@@ -616,43 +710,33 @@ extern "C" int32_t fvm_batch_add(fvm_batch *b, const fvm_params *par, const fvm_
       break;
     }
   if (sid < 0) return FVM_ERR_CAPACITY;
+  const MeshLayout &Lp = prep->L;
+  if (Lp.max_slots > b->cfg.max_slots || Lp.max_tri > b->cfg.max_tri) return FVM_ERR_CAPACITY;
+  const int64_t need[P_COUNT] = {Lp.np, Lp.nblk, (int64_t)Lp.be_nodes.size(), (int64_t)Lp.bb_nodes.size(),
+                                 (int64_t)Lp.bt_nodes.size(), Lp.nt, (int64_t)Lp.ve_list.size(),
+                                 (int64_t)Lp.vt_list.size(), (int64_t)Lp.va_list.size(),
+                                 (int64_t)Lp.sw_nodes.size()};
+  int64_t off[P_COUNT];
+  for (int i = 0; i < P_COUNT; i++) {
+    off[i] = b->pool[i].alloc(need[i]);
+    if (off[i] < 0) {
+      for (int j = 0; j < i; j++) b->pool[j].release(off[j], need[j]);
+      return FVM_ERR_CAPACITY;
+    }
+  }
   Slot &S = b->slots[sid];
   S = Slot();
   S.par = *par;
-  int32_t st = build_layout(*m, kBlockVerts, S.L);
-  if (st != FVM_OK) return st;
-  const MeshLayout &L = S.L;
-  if (L.max_slots > b->cfg.max_slots || L.max_tri > b->cfg.max_tri) return FVM_ERR_CAPACITY;
-  const int64_t need[P_COUNT] = {L.np, L.nblk, (int64_t)L.be_nodes.size(), (int64_t)L.bb_nodes.size(),
-                                 (int64_t)L.bt_nodes.size(), L.nt, (int64_t)L.ve_list.size(),
-                                 (int64_t)L.vt_list.size(), (int64_t)L.va_list.size(),
-                                 (int64_t)L.sw_nodes.size()};
+  S.L = prep->L;
   for (int i = 0; i < P_COUNT; i++) {
-    const int64_t off = b->pool[i].alloc(need[i]);
-    if (off < 0) {
-      for (int j = 0; j < i; j++) b->pool[j].release(S.off[j], S.len[j]);
-      S = Slot();
-      return FVM_ERR_CAPACITY;
-    }
-    S.off[i] = off;
+    S.off[i] = off[i];
     S.len[i] = need[i];
   }
+  const MeshLayout &L = S.L;
   const int np = L.np;
   const int v0 = (int)S.off[P_V];
-  // vertex arrays
-  std::vector<double2> coord(np);
-  std::vector<double> ais(np), cvarea(np), drmin(np), wd(np, 1.0);
-  std::vector<int> orig(np);
   std::vector<int2> ve(np), vt(np), va(np);
-  const double n1b6 = 1.0 / 6.0;
   for (int v = 0; v < np; v++) {
-    const int o = L.perm[v];
-    coord[v] = make_double2(m->coord[2 * o], m->coord[2 * o + 1]);
-    ais[v] = n1b6 / m->mcarea[o];   // green_gauss.f:34
-    cvarea[v] = m->cvarea[o];
-    drmin[v] = m->drmin[o];
-    if (m->wd) wd[v] = m->wd[o];
-    orig[v] = o + 1;
     ve[v] = make_int2((int)(S.off[P_VE] + L.ve_ptr[v]), (int)(S.off[P_VE] + L.ve_ptr[v + 1]));
     vt[v] = make_int2((int)(S.off[P_VT] + L.vt_ptr[v]), (int)(S.off[P_VT] + L.vt_ptr[v + 1]));
     va[v] = make_int2((int)(S.off[P_VA] + L.va_ptr[v]), (int)(S.off[P_VA] + L.va_ptr[v + 1]));
@@ -668,12 +752,9 @@ extern "C" int32_t fvm_batch_add(fvm_batch *b, const fvm_params *par, const fvm_
     bi.part = (int)S.off[P_BLK] + k;
   }
   std::vector<int2> be(L.be_nodes);
-  std::vector<double2> be_ds(be.size());
-  for (size_t k = 0; k < be.size(); k++) {
-    be[k].x += v0;
-    be[k].y += v0;
-    const int e = L.be_edge[k];
-    be_ds[k] = make_double2(m->ds[2 * e], m->ds[2 * e + 1]);
+  for (int2 &q : be) {
+    q.x += v0;
+    q.y += v0;
   }
   std::vector<int4> bb(L.bb_nodes);
   for (int4 &q : bb) {
@@ -697,37 +778,6 @@ extern "C" int32_t fvm_batch_add(fvm_batch *b, const fvm_params *par, const fvm_
     q.x += v0;
     q.y += v0;
   }
-  std::vector<double> elarea(m->elarea, m->elarea + L.nt);
-  // FP32 copies of FP64 differences (rounded once) for the FP32 kernels
-  std::vector<float2> be_dxy;
-  std::vector<TriGeo32> tri_g32;
-  if (b->prec == FVM_PREC_FP32) {
-    be_dxy.resize(L.be_edge.size());
-    for (size_t k = 0; k < L.be_edge.size(); k++) {
-      const int e = L.be_edge[k];
-      const int n1 = m->edge[2 * e] - 1, n2 = m->edge[2 * e + 1] - 1;
-      be_dxy[k] = make_float2((float)(m->coord[2 * n2] - m->coord[2 * n1]),
-                              (float)(m->coord[2 * n2 + 1] - m->coord[2 * n1 + 1]));
-    }
-    tri_g32.resize(L.bt_nodes.size());
-    for (size_t k = 0; k < L.bt_nodes.size(); k++) {
-      const int t = L.bt_nodes[k].w;   // driver triangle of this block entry
-      const int a = m->elem[3 * t] - 1, c2 = m->elem[3 * t + 1] - 1, c3 = m->elem[3 * t + 2] - 1;
-      const double x1 = m->coord[2 * a], y1 = m->coord[2 * a + 1];
-      const double x2 = m->coord[2 * c2], y2 = m->coord[2 * c2 + 1];
-      const double x3 = m->coord[2 * c3], y3 = m->coord[2 * c3 + 1];
-      TriGeo32 g;
-      g.dbxx[0] = (float)(y2 - y3);
-      g.dbxx[1] = (float)(y3 - y1);
-      g.dbxx[2] = (float)(y1 - y2);
-      g.dbyy[0] = (float)(x3 - x2);
-      g.dbyy[1] = (float)(x1 - x3);
-      g.dbyy[2] = (float)(x2 - x1);
-      g.areat = (float)(0.25 / m->elarea[t]);
-      g.pad = 0.f;
-      tri_g32[k] = g;
-    }
-  }
   MeshConst mc = make_const(*par);
   mc.v0 = v0;
   mc.nv = np;
@@ -750,12 +800,12 @@ extern "C" int32_t fvm_batch_add(fvm_batch *b, const fvm_params *par, const fvm_
 #define PUT(expr)                  \
   if ((e = (expr)) != cudaSuccess) \
     return err(e);
-  PUT(put_range(b, b->coord, v0, coord));
-  PUT(put_range(b, b->ais, v0, ais));
-  PUT(put_range(b, b->cvarea, v0, cvarea));
-  PUT(put_range(b, b->drmin, v0, drmin));
-  PUT(put_range(b, b->wd, v0, wd));
-  PUT(put_range(b, b->orig, v0, orig));
+  PUT(put_range(b, b->coord, v0, prep->coord));
+  PUT(put_range(b, b->ais, v0, prep->ais));
+  PUT(put_range(b, b->cvarea, v0, prep->cvarea));
+  PUT(put_range(b, b->drmin, v0, prep->drmin));
+  PUT(put_range(b, b->wd, v0, prep->wd));
+  PUT(put_range(b, b->orig, v0, prep->orig));
   PUT(put_range(b, b->vflag, v0, L.vflag));
   PUT(put_range(b, b->ve_rng, v0, ve));
   PUT(put_range(b, b->vt_rng, v0, vt));
@@ -765,14 +815,14 @@ extern "C" int32_t fvm_batch_add(fvm_batch *b, const fvm_params *par, const fvm_
   PUT(put_range(b, b->va_list, S.off[P_VA], valist));
   PUT(put_range(b, b->blocks, S.off[P_BLK], blocks));
   PUT(put_range(b, b->be_nodes, S.off[P_BE], be));
-  PUT(put_range(b, b->be_ds, S.off[P_BE], be_ds));
+  PUT(put_range(b, b->be_ds, S.off[P_BE], prep->be_ds));
   if (b->be_csl)
     PUT(launch_edge_csl(b->be_ds + S.off[P_BE], b->be_csl + S.off[P_BE], (int)be.size(), b->stream));
   PUT(put_range(b, b->bb_nodes, S.off[P_BB], bb));
   PUT(put_range(b, b->bt_nodes, S.off[P_BT], bt));
-  PUT(put_range(b, b->elarea, S.off[P_TRI], elarea));
-  if (b->be_dxy) PUT(put_range(b, b->be_dxy, S.off[P_BE], be_dxy));
-  if (b->tri_g32) PUT(put_range(b, b->tri_g32, S.off[P_BT], tri_g32));
+  PUT(put_range(b, b->elarea, S.off[P_TRI], prep->elarea));
+  if (b->be_dxy) PUT(put_range(b, b->be_dxy, S.off[P_BE], prep->be_dxy));
+  if (b->tri_g32) PUT(put_range(b, b->tri_g32, S.off[P_BT], prep->tri_g32));
   PUT(put_range(b, b->sw_nodes, S.off[P_SW], sw));
   PUT(cudaMemcpyAsync(b->mc + sid, &mc, sizeof(mc), cudaMemcpyHostToDevice, b->stream));
   PUT(cudaMemcpyAsync(b->ctl + sid, &ctl, sizeof(ctl), cudaMemcpyHostToDevice, b->stream));
@@ -782,6 +832,7 @@ extern "C" int32_t fvm_batch_add(fvm_batch *b, const fvm_params *par, const fvm_
   PUT(cudaStreamSynchronize(b->stream));
 #undef PUT
   // freestream state (initialize.f:60-89)
+  int32_t st;
   {
     std::vector<double> prim(4 * (size_t)np), nut(np, 0.0), mul(np, 0.0), mu(np, 0.0);
     for (int v = 0; v < np; v++) {
@@ -816,8 +867,23 @@ extern "C" int32_t fvm_batch_add(fvm_batch *b, const fvm_params *par, const fvm_
     fvm_batch_remove(b, sid);
     return st;
   }
+  delete prep;   // consumed on success only
   *slot_out = sid;
   return FVM_OK;
+}
+
+extern "C" int32_t fvm_batch_add(fvm_batch *b, const fvm_params *par, const fvm_mesh *m,
+                                 int32_t *slot_out) {
+  if (!b || !par || !m || !slot_out) return FVM_ERR_ARG;
+  *slot_out = -1;
+  if (par->precision != b->prec) return FVM_ERR_ARG;
+  if (par->iflow != FVM_INVISCID && !b->caps.viscous) return FVM_ERR_ARG;
+  fvm_prepared *prep = nullptr;
+  int32_t st = fvm_batch_prepare(par, m, &prep);
+  if (st) return st;
+  st = fvm_batch_add_prepared(b, prep, slot_out);
+  if (st) delete prep;
+  return st;
 }
 
 extern "C" int32_t fvm_batch_remove(fvm_batch *b, int32_t slot) {

@@ -1,0 +1,209 @@
+"""Continuous-batching service of steady airfoil solves on one GPU.
+
+Requests arrive over time (seeded Poisson process).  Each names an airfoil
+(NACA 4-digit thickness, camber and its position), a grid size, a flow
+(Euler or laminar Navier-Stokes, Mach, angle of attack, Reynolds number).
+The service:
+
+* prepares each arrived request on host worker threads: O-grid, driver
+  geometry (geometric.f chain), GPU dtlength, block layout (fvm_batch_prepare);
+* admits prepared meshes into one device arena while it has room (the
+  admission test is the arena's capacity in vertices, block entries and
+  incidence entries, i.e. the HBM footprint; a refused mesh waits);
+* advances every resident solve together, ``chunk`` iterations per step,
+  all meshes in one launch per kernel (one CUDA graph per iteration);
+* retires a solve when it reaches its residual drop or iteration cap
+  (main.f:42), frees its arena ranges and admits the next.
+
+So requests that arrive while others run join them on the device; no solve
+waits for a batch boundary.  Latency is finish time minus arrival time.
+"""
+from __future__ import annotations
+
+import collections
+import concurrent.futures as cf
+import dataclasses
+import math
+import time
+
+import numpy as np
+
+from . import _lib as L
+from .batch import Batch, Prepared
+from .ogrid import naca_ogrid
+from .solver import build_geometry, make_params
+
+
+@dataclasses.dataclass
+class Request:
+    rid: int
+    arrival: float          # seconds after the start of the run
+    thickness: float
+    camber: float
+    camber_pos: float
+    npts: int               # requested vertex count
+    laminar: bool
+    mach: float
+    aoa_deg: float
+    rey: float
+    seed: int
+
+
+@dataclasses.dataclass
+class Result:
+    rid: int
+    npts: int
+    laminar: bool
+    arrival: float
+    admitted: float = math.nan
+    finished: float = math.nan
+    niter: int = 0
+    fres: float = math.nan
+    cl: float = math.nan
+    cd: float = math.nan
+    status: int = 0
+    converged: bool = False
+
+    @property
+    def latency(self) -> float:
+        return self.finished - self.arrival
+
+
+def generate_requests(n: int = 512, rate: float = 20.0, seed: int = 0, pmin: int = 5000,
+                      pmax: int = 400000, laminar_frac: float = 0.3) -> list[Request]:
+    """The serving workload: Poisson arrivals at ``rate`` per second; NACA
+    4-digit thickness U[9,15]%, max camber U[0,4]% at U[30,50]% chord;
+    vertex counts log-uniform in [pmin, pmax]; 70% Euler / 30% laminar with
+    Re U[1e3,1e4]; Mach U[0.3,0.85]; angle of attack U[-3,5] degrees."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, size=n))
+    t -= t[0]
+    out = []
+    for i in range(n):
+        lam = rng.uniform() < laminar_frac
+        out.append(Request(
+            rid=i, arrival=float(t[i]), thickness=float(rng.uniform(0.09, 0.15)),
+            camber=float(rng.uniform(0.0, 0.04)), camber_pos=float(rng.uniform(0.3, 0.5)),
+            npts=int(round(math.exp(rng.uniform(math.log(pmin), math.log(pmax))))),
+            laminar=bool(lam), mach=float(rng.uniform(0.3, 0.85)),
+            aoa_deg=float(rng.uniform(-3.0, 5.0)),
+            rey=float(rng.uniform(1e3, 1e4)) if lam else 0.0, seed=1000 + i))
+    return out
+
+
+def grid_for(req: Request):
+    """O-grid with about ``npts`` vertices and ni:nr near 10:3."""
+    ni = max(16, int(round(math.sqrt(req.npts * 10.0 / 3.0) / 2.0)) * 2)
+    nr = max(8, int(round(req.npts / ni)))
+    first = 2e-4 if req.laminar else 1e-3
+    radius = 30.0 if req.laminar else 20.0
+    first = min(first, 0.5 * radius / nr)
+    return naca_ogrid(ni, nr, thickness=req.thickness, camber=req.camber,
+                      camber_pos=req.camber_pos, radius=radius, first_spacing=first)
+
+
+def params_for(req: Request, precision: int) -> L.FvmParams:
+    if req.laminar:
+        return make_params(iflow=L.LAMINAR, mach=req.mach, aoa_deg=req.aoa_deg, rey=req.rey,
+                           cfl=0.8, precision=precision, bugcompat=0)
+    return make_params(mach=req.mach, aoa_deg=req.aoa_deg, cfl=1.0, precision=precision,
+                       bugcompat=0)
+
+
+def prepare(req: Request, precision: int) -> Prepared:
+    g = grid_for(req)
+    m = build_geometry(g.coord, g.elem, g.ptype)
+    return Prepared(params_for(req, precision), m)
+
+
+class Server:
+    def __init__(self, vertices: int = 6_000_000, meshes: int = 256, precision: int = L.FP32,
+                 chunk: int = 50, workers: int = 8, max_iter: int = 5000, minres: float = 1e-6):
+        self.batch = Batch(precision, vertices=vertices, meshes=meshes, viscous=True)
+        self.precision = precision
+        self.chunk = chunk
+        self.workers = workers
+        self.max_iter = max_iter
+        self.minres = minres
+
+    def close(self):
+        self.batch.close()
+
+    def run(self, requests: list[Request], log=None) -> tuple[list[Result], dict]:
+        b = self.batch
+        results = {r.rid: Result(rid=r.rid, npts=r.npts, laminar=r.laminar, arrival=r.arrival)
+                   for r in requests}
+        order = sorted(requests, key=lambda r: r.arrival)
+        pool = cf.ThreadPoolExecutor(max_workers=self.workers)
+        preparing = collections.deque()      # (req, future), arrival order
+        ready = collections.deque()          # (req, Prepared)
+        resident = {}                        # slot -> req
+        nxt = 0
+        done = 0
+        steps = 0
+        resident_vertices = []
+        t0 = time.perf_counter()
+        while done < len(order):
+            now = time.perf_counter() - t0
+            while nxt < len(order) and order[nxt].arrival <= now:
+                preparing.append((order[nxt], pool.submit(prepare, order[nxt], self.precision)))
+                nxt += 1
+            while preparing and preparing[0][1].done():
+                req, fut = preparing.popleft()
+                ready.append((req, fut.result()))
+            while ready:                                   # admission by footprint
+                req, prep = ready[0]
+                slot = b.add_prepared(prep)
+                if slot is None:
+                    if not resident:
+                        raise RuntimeError(f"request {req.rid} ({req.npts} vertices) "
+                                           "does not fit an empty arena")
+                    break
+                ready.popleft()
+                b.start(slot, self.max_iter, self.minres)
+                resident[slot] = req
+                results[req.rid].admitted = time.perf_counter() - t0
+                results[req.rid].npts = b._meshes[slot].np     # the grid's actual size
+            if not resident:
+                if nxt < len(order) and not preparing and not ready:
+                    time.sleep(max(0.0, min(0.01, order[nxt].arrival - now)))
+                else:
+                    time.sleep(0.001)
+                continue
+            b.step(self.chunk)                             # all resident solves at once
+            steps += 1
+            resident_vertices.append(sum(b._meshes[s].np for s in resident))
+            for slot in list(resident):
+                p = b.poll(slot)
+                if p["active"]:
+                    continue
+                req = resident.pop(slot)
+                r = results[req.rid]
+                r.finished = time.perf_counter() - t0
+                r.niter, r.fres, r.cl, r.cd, r.status = (p["niter"], p["fres"], p["cl"],
+                                                         p["cd"], p["status"])
+                r.converged = p["status"] == 0 and p["fres"] <= self.minres
+                b.remove(slot)
+                done += 1
+                if log:
+                    log(r)
+        pool.shutdown()
+        makespan = time.perf_counter() - t0
+        res = [results[r.rid] for r in requests]
+        lat = np.array([r.latency for r in res])
+        ok = [r for r in res if r.status == 0]
+        by_rid = {r.rid: r for r in requests}
+        failures = [dict(rid=r.rid, status=r.status, niter=r.niter, npts=r.npts,
+                         laminar=r.laminar, mach=by_rid[r.rid].mach,
+                         aoa_deg=by_rid[r.rid].aoa_deg) for r in res if r.status != 0]
+        stats = dict(requests=len(res), completed_ok=len(ok), failures=failures,
+                     reached_minres=sum(r.converged for r in res),
+                     iteration_cap=sum(r.status == 0 and not r.converged for r in res),
+                     makespan_s=makespan, solves_per_s=len(ok) / makespan,
+                     p50_latency_s=float(np.percentile(lat, 50)),
+                     p99_latency_s=float(np.percentile(lat, 99)),
+                     vertex_stage_updates=float(sum(r.npts * 3 * r.niter for r in res)),
+                     mean_resident_vertices=float(np.mean(resident_vertices)) if resident_vertices else 0.0,
+                     steps=steps, chunk=self.chunk)
+        stats["vertex_stage_updates_per_s"] = stats["vertex_stage_updates"] / makespan
+        return res, stats

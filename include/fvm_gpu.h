@@ -281,6 +281,20 @@ int32_t fvm_batch_destroy(fvm_batch *b);
 int32_t fvm_batch_add(fvm_batch *b, const fvm_params *p, const fvm_mesh *m,
                       int32_t *slot);
 int32_t fvm_batch_remove(fvm_batch *b, int32_t slot);
+/* fvm_batch_add in two halves, so the host work can overlap the GPU:
+ * fvm_batch_prepare builds the block layout on the host (thread safe, no
+ * device work; the mesh arrays are copied), fvm_batch_add_prepared uploads
+ * it.  On success the batch takes the prepared object; on any error
+ * (FVM_ERR_CAPACITY included) it stays with the caller, who may retry it
+ * later or release it with fvm_prepared_free. */
+typedef struct fvm_prepared fvm_prepared;
+int32_t fvm_batch_prepare(const fvm_params *p, const fvm_mesh *m,
+                          fvm_prepared **out);
+int32_t fvm_batch_add_prepared(fvm_batch *b, fvm_prepared *prep,
+                               int32_t *slot);
+int32_t fvm_prepared_free(fvm_prepared *prep);
+/* Device bytes a prepared mesh occupies in a batch of this precision. */
+int64_t fvm_prepared_bytes(const fvm_prepared *prep, int32_t precision);
 int32_t fvm_batch_set_state(fvm_batch *b, int32_t slot, const double *prim,
                             const double *nut, const double *mul,
                             const double *mu, int32_t iterlast);
