@@ -64,7 +64,9 @@ class FvmBatchCaps(C.Structure):
                 ("triangles", C.c_int64), ("edge_incidence", C.c_int64),
                 ("tri_incidence", C.c_int64), ("all_incidence", C.c_int64),
                 ("solid_edges", C.c_int64), ("max_slots", C.c_int32), ("max_tri", C.c_int32),
-                ("grid", C.c_int32), ("reserved", C.c_int32)]
+                ("grid", C.c_int32), ("max_tri2", C.c_int32), ("max_loc", C.c_int32),
+                ("fused", C.c_int32), ("halo_entries", C.c_int64),
+                ("halo_incidence", C.c_int64)]
 
 
 # every function the header declares, with its signature

@@ -17,9 +17,10 @@ def layout_stats(mesh) -> dict:
     """Block layout of a mesh after renumbering (host only)."""
     m = mesh if isinstance(mesh, MeshArrays) else MeshArrays(mesh)
     ms = m.struct()
-    out = (C.c_int64 * 6)()
+    out = (C.c_int64 * 10)()
     check(L.lib().fvm_layout_stats(C.byref(ms), out), "fvm_layout_stats")
-    keys = ["blocks", "edge_entries", "tri_entries", "max_slots", "max_tri", "boundary_entries"]
+    keys = ["blocks", "edge_entries", "tri_entries", "max_slots", "max_tri", "boundary_entries",
+            "max_tri2", "max_loc", "halo_entries", "layout_violations"]
     return dict(zip(keys, [int(x) for x in out]))
 
 

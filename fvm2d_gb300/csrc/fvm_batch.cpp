@@ -73,7 +73,7 @@ class RangeAlloc {
   std::map<int64_t, int64_t> free_;
 };
 
-enum Pool { P_V, P_BLK, P_BE, P_BB, P_BT, P_TRI, P_VE, P_VT, P_VA, P_SW, P_COUNT };
+enum Pool { P_V, P_BLK, P_BE, P_BB, P_BT, P_TRI, P_VE, P_VT, P_VA, P_SW, P_HALO, P_HP, P_HL, P_COUNT };
 
 struct Slot {
   bool used = false;
@@ -83,8 +83,8 @@ struct Slot {
   int64_t len[P_COUNT] = {0};
 };
 
-const char *kKernelNames[] = {"visc", "grad", "flux", "sa", "monitor"};
-enum { K_VISC, K_GRAD, K_FLUX, K_SA, K_MON, K_COUNT };
+const char *kKernelNames[] = {"visc", "grad", "flux", "sa", "monitor", "step"};
+enum { K_VISC, K_GRAD, K_FLUX, K_SA, K_MON, K_STEP, K_COUNT };
 
 }  // namespace
 
@@ -114,8 +114,12 @@ struct fvm_batch {
   D4 *be_csl = nullptr;
   int4 *bb_nodes = nullptr, *bt_nodes = nullptr;
   double *elarea = nullptr;
-  float2 *be_dxy = nullptr;
+  EdgeGeo32 *be_g32 = nullptr;
   TriGeo32 *tri_g32 = nullptr;
+  uint32_t *be_loc = nullptr;
+  int *halo_ids = nullptr, *hl_ptr = nullptr;
+  uint16_t *hl_list = nullptr;
+  bool fused = false;
   MeshConst *mc = nullptr;
   MeshCtl *ctl = nullptr;
   BlockPartial *part = nullptr;
@@ -196,8 +200,12 @@ ArenaPtrs<R> ptrs(const fvm_batch *b) {
   A.bb_nodes = b->bb_nodes;
   A.bt_nodes = b->bt_nodes;
   A.elarea = b->elarea;
-  A.be_dxy = b->be_dxy;
+  A.be_g32 = b->be_g32;
   A.tri_g32 = b->tri_g32;
+  A.be_loc = b->be_loc;
+  A.halo_ids = b->halo_ids;
+  A.hl_ptr = b->hl_ptr;
+  A.hl_list = b->hl_list;
   A.sw_nodes = b->sw_nodes;
   A.va_rng = b->va_rng;
   A.va_list = b->va_list;
@@ -368,12 +376,30 @@ int32_t update_work(fvm_batch *b) {
       flux = (flux == -1 || flux == s.par.iflux) ? s.par.iflux : 0;
     }
   if (flux < 0) flux = b->cfg.flux;   // empty batch: keep the current kernels
-  if (flux != b->cfg.flux) {
-    b->cfg.flux = flux;                // a different flux kernel: re-capture
-    if (b->graph) {
-      cudaGraphExecDestroy(b->graph);
-      b->graph = nullptr;
+  // Shared-memory tiles sized for the resident meshes (rounded up to 8, so
+  // small changes of the mix keep the graph), never above the arena's
+  // capacities: smaller tiles let more CTAs share an SM.
+  int tile[4] = {0, 0, 0, 0};
+  for (const Slot &s : b->slots)
+    if (s.used) {
+      tile[0] = std::max(tile[0], s.L.max_tri);
+      tile[1] = std::max(tile[1], s.L.max_slots);
+      tile[2] = std::max(tile[2], s.L.max_tri2);
+      tile[3] = std::max(tile[3], s.L.max_loc);
     }
+  const int cap[4] = {b->caps.max_tri, b->caps.max_slots, b->caps.max_tri2, b->caps.max_loc};
+  int *cur[4] = {&b->cfg.max_tri, &b->cfg.max_slots, &b->cfg.max_tri2, &b->cfg.max_loc};
+  bool changed = flux != b->cfg.flux;
+  b->cfg.flux = flux;
+  for (int i = 0; i < 4; i++) {
+    if (!tile[i]) continue;             // empty batch: keep the current tiles
+    const int t = std::min(cap[i], (tile[i] + 7) & ~7);
+    changed |= t != *cur[i];
+    *cur[i] = t;
+  }
+  if (changed && b->graph) {            // different kernels or tiles: re-capture
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
   }
   const int n = (int)work.size();
   if (n) FVM_TRY(b, cudaMemcpyAsync(b->work, work.data(), n * sizeof(int), cudaMemcpyHostToDevice, b->stream));
@@ -409,6 +435,14 @@ int32_t enqueue_iteration(fvm_batch *b, bool with_events) {
       FVM_TRY(b, mark(K_VISC));
       FVM_TRY(b, launch_visc(A, c, s, s == 1, 0));
       FVM_TRY(b, done());
+    }
+    if (b->fused) {
+      // one pass: gradients (own + halo), fluxes, RK stage; inviscid
+      // meshes take their time step in the stage-1 pass
+      FVM_TRY(b, mark(K_STEP));
+      FVM_TRY(b, launch_step(A, c, s));
+      FVM_TRY(b, done());
+      continue;
     }
     FVM_TRY(b, mark(K_GRAD));
     // inviscid meshes take their time step in the stage-1 gradient pass
@@ -465,8 +499,12 @@ void default_caps(fvm_batch_caps &c) {
   if (!c.tri_incidence) c.tri_incidence = 7 * V + 1024 * M;
   if (!c.all_incidence) c.all_incidence = 7 * V + 1024 * M;
   if (!c.solid_edges) c.solid_edges = V / 8 + 256 * M;
-  if (!c.max_slots) c.max_slots = 1536;
-  if (!c.max_tri) c.max_tri = 1024;
+  if (!c.max_slots) c.max_slots = 1152;
+  if (!c.max_tri) c.max_tri = 896;
+  if (!c.max_tri2) c.max_tri2 = 1280;
+  if (!c.max_loc) c.max_loc = 576;
+  if (!c.halo_entries) c.halo_entries = V / 2 + 1024 * M;
+  if (!c.halo_incidence) c.halo_incidence = 4 * V + 4096 * M;
 }
 
 }  // namespace
@@ -490,13 +528,16 @@ extern "C" int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *cap
   b->caps = *caps_in;
   default_caps(b->caps);
   const fvm_batch_caps &c = b->caps;
-  if (c.max_slots > (int)kSlotMask || c.max_tri > 0x3fff || c.vertices > INT_MAX / 8) {
+  if (c.max_slots > (int)kSlotMask || c.max_tri > 0x3fff || c.max_tri2 > 0x3fff ||
+      c.max_loc > (int)kBlockVerts * 8 || c.vertices > INT_MAX / 8) {
     delete b;
     return FVM_ERR_ARG;
   }
   const int64_t caps[P_COUNT] = {c.vertices, c.blocks, c.edge_entries, c.boundary_entries,
                                  c.tri_entries, c.triangles, c.edge_incidence,
-                                 c.tri_incidence, c.all_incidence, c.solid_edges};
+                                 c.tri_incidence, c.all_incidence, c.solid_edges,
+                                 c.halo_entries, c.halo_entries + c.blocks,
+                                 c.halo_incidence};
   for (int i = 0; i < P_COUNT; i++) {
     if (caps[i] > INT_MAX) {
       delete b;
@@ -545,13 +586,17 @@ extern "C" int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *cap
   TRYB(dalloc(O, &b->work, (size_t)c.blocks));
   TRYB(dalloc(O, &b->nwork, 1));
   TRYB(dalloc(O, &b->be_nodes, (size_t)c.edge_entries));
+  TRYB(dalloc(O, &b->be_loc, (size_t)c.edge_entries));
+  TRYB(dalloc(O, &b->halo_ids, (size_t)b->cap[P_HALO]));
+  TRYB(dalloc(O, &b->hl_ptr, (size_t)b->cap[P_HP]));
+  TRYB(dalloc(O, &b->hl_list, (size_t)b->cap[P_HL]));
   TRYB(dalloc(O, &b->be_ds, (size_t)c.edge_entries));
   if (precision == FVM_PREC_FP64) TRYB(dalloc(O, &b->be_csl, (size_t)c.edge_entries));
   TRYB(dalloc(O, &b->bb_nodes, (size_t)c.boundary_entries));
   TRYB(dalloc(O, &b->bt_nodes, (size_t)c.tri_entries));
   TRYB(dalloc(O, &b->elarea, (size_t)c.triangles));
   if (precision == FVM_PREC_FP32) {
-    TRYB(dalloc(O, &b->be_dxy, (size_t)c.edge_entries));
+    TRYB(dalloc(O, &b->be_g32, (size_t)c.edge_entries));
     TRYB(dalloc(O, &b->tri_g32, (size_t)c.tri_entries));
   }
   TRYB(dalloc(O, &b->sw_nodes, (size_t)c.solid_edges));
@@ -571,12 +616,17 @@ extern "C" int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *cap
 #undef TRYB
   b->cfg.max_slots = c.max_slots;
   b->cfg.max_tri = c.max_tri;
+  b->cfg.max_tri2 = c.max_tri2;
+  b->cfg.max_loc = c.max_loc;
+  b->fused = c.fused > 0;
   b->cfg.viscous = c.viscous != 0;
   b->cfg.stream = b->stream;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (sms <= 0) sms = 152;
+  b->cfg.sms = sms;
+  b->cfg.fit = c.grid <= 0;            // an explicit grid is taken as given
   b->cfg.grid = c.grid > 0 ? c.grid : std::max<int>(1, std::min<int64_t>(c.blocks, 8LL * sms));
   cudaError_t e = precision == FVM_PREC_FP64 ? prepare_attributes(b->cfg, (double *)nullptr)
                                              : prepare_attributes(b->cfg, (float *)nullptr);
@@ -606,7 +656,7 @@ struct fvm_prepared {
   std::vector<double> ais, cvarea, drmin, wd, elarea;
   std::vector<int> orig;
   std::vector<double2> be_ds;
-  std::vector<float2> be_dxy;      // FP32 batches
+  std::vector<EdgeGeo32> be_g32;   // FP32 batches (mesh-local vertex ids)
   std::vector<TriGeo32> tri_g32;   // FP32 batches
 };
 
@@ -647,14 +697,24 @@ extern "C" int32_t fvm_batch_prepare(const fvm_params *par, const fvm_mesh *m, f
   }
   P->elarea.assign(m->elarea, m->elarea + L.nt);
   P->be_ds.resize(L.be_edge.size());
-  P->be_dxy.resize(L.be_edge.size());
+  P->be_g32.resize(L.be_edge.size());
   for (size_t k = 0; k < L.be_edge.size(); k++) {
     const int e = L.be_edge[k];
-    P->be_ds[k] = make_double2(m->ds[2 * e], m->ds[2 * e + 1]);
-    // FP32 copies of FP64 differences, rounded once
+    const double dsx = m->ds[2 * e], dsy = m->ds[2 * e + 1];
+    P->be_ds[k] = make_double2(dsx, dsy);
+    // FP32 copies of FP64 quantities, rounded once
     const int n1 = m->edge[2 * e] - 1, n2 = m->edge[2 * e + 1] - 1;
-    P->be_dxy[k] = make_float2((float)(m->coord[2 * n2] - m->coord[2 * n1]),
-                               (float)(m->coord[2 * n2 + 1] - m->coord[2 * n1 + 1]));
+    const double len = std::sqrt(dsx * dsx + dsy * dsy);   // flux.f:10-13
+    EdgeGeo32 g;
+    g.n1 = L.be_nodes[k].x;
+    g.n2 = L.be_nodes[k].y;
+    g.dx = (float)(m->coord[2 * n2] - m->coord[2 * n1]);
+    g.dy = (float)(m->coord[2 * n2 + 1] - m->coord[2 * n1 + 1]);
+    g.ct = (float)(dsx / len);
+    g.st = (float)(dsy / len);
+    g.len = (float)len;
+    g.loc = L.be_loc[k];
+    P->be_g32[k] = g;
   }
   P->tri_g32.resize(L.bt_nodes.size());
   for (size_t k = 0; k < L.bt_nodes.size(); k++) {
@@ -689,11 +749,13 @@ extern "C" int64_t fvm_prepared_bytes(const fvm_prepared *prep, int32_t precisio
   const int64_t r = precision == FVM_PREC_FP64 ? 8 : 4;
   const int64_t V = L.np;
   int64_t bytes = V * (3 * 4 * r + 8 * r + 4 * r + 4 * r + 5 * r + 16 + 4 * 8 + 4 + 1 + 3 * 8);
-  bytes += (int64_t)L.be_nodes.size() * (8 + 16 + (precision == FVM_PREC_FP64 ? 32 : 8));
+  bytes += (int64_t)L.be_nodes.size() * (8 + 16 + 32);
   bytes += (int64_t)L.bb_nodes.size() * 16 + (int64_t)L.bt_nodes.size() * (16 + (r == 4 ? 32 : 0));
   bytes += (int64_t)L.nt * 8 + (int64_t)L.ve_list.size() * 2 + (int64_t)L.vt_list.size() * 2;
   bytes += (int64_t)L.va_list.size() * 4 + (int64_t)L.sw_nodes.size() * 8;
   bytes += (int64_t)L.nblk * (sizeof(BlockInfo) + sizeof(BlockPartial) + 4);
+  bytes += (int64_t)L.be_loc.size() * 4 + (int64_t)L.halo_ids.size() * 4;
+  bytes += (int64_t)L.hl_ptr.size() * 4 + (int64_t)L.hl_list.size() * 2;
   return bytes;
 }
 
@@ -711,11 +773,14 @@ extern "C" int32_t fvm_batch_add_prepared(fvm_batch *b, fvm_prepared *prep, int3
     }
   if (sid < 0) return FVM_ERR_CAPACITY;
   const MeshLayout &Lp = prep->L;
-  if (Lp.max_slots > b->cfg.max_slots || Lp.max_tri > b->cfg.max_tri) return FVM_ERR_CAPACITY;
+  if (Lp.max_slots > b->caps.max_slots || Lp.max_tri > b->caps.max_tri ||
+      Lp.max_tri2 > b->caps.max_tri2 || Lp.max_loc > b->caps.max_loc)
+    return FVM_ERR_CAPACITY;
   const int64_t need[P_COUNT] = {Lp.np, Lp.nblk, (int64_t)Lp.be_nodes.size(), (int64_t)Lp.bb_nodes.size(),
                                  (int64_t)Lp.bt_nodes.size(), Lp.nt, (int64_t)Lp.ve_list.size(),
                                  (int64_t)Lp.vt_list.size(), (int64_t)Lp.va_list.size(),
-                                 (int64_t)Lp.sw_nodes.size()};
+                                 (int64_t)Lp.sw_nodes.size(), (int64_t)Lp.halo_ids.size(),
+                                 (int64_t)Lp.hl_ptr.size(), (int64_t)Lp.hl_list.size()};
   int64_t off[P_COUNT];
   for (int i = 0; i < P_COUNT; i++) {
     off[i] = b->pool[i].alloc(need[i]);
@@ -749,8 +814,14 @@ extern "C" int32_t fvm_batch_add_prepared(fvm_batch *b, fvm_prepared *prep, int3
     bi.e0 += (int)S.off[P_BE];
     bi.b0 += (int)S.off[P_BB];
     bi.t0 += (int)S.off[P_BT];
+    bi.h0 += (int)S.off[P_HALO];
+    bi.hp0 += (int)S.off[P_HP];
     bi.part = (int)S.off[P_BLK] + k;
   }
+  std::vector<int> halo(L.halo_ids);
+  for (int &x : halo) x += v0;
+  std::vector<int> hlp(L.hl_ptr);
+  for (int &x : hlp) x += (int)S.off[P_HL];
   std::vector<int2> be(L.be_nodes);
   for (int2 &q : be) {
     q.x += v0;
@@ -815,13 +886,24 @@ extern "C" int32_t fvm_batch_add_prepared(fvm_batch *b, fvm_prepared *prep, int3
   PUT(put_range(b, b->va_list, S.off[P_VA], valist));
   PUT(put_range(b, b->blocks, S.off[P_BLK], blocks));
   PUT(put_range(b, b->be_nodes, S.off[P_BE], be));
+  PUT(put_range(b, b->be_loc, S.off[P_BE], L.be_loc));
+  PUT(put_range(b, b->halo_ids, S.off[P_HALO], halo));
+  PUT(put_range(b, b->hl_ptr, S.off[P_HP], hlp));
+  PUT(put_range(b, b->hl_list, S.off[P_HL], L.hl_list));
   PUT(put_range(b, b->be_ds, S.off[P_BE], prep->be_ds));
   if (b->be_csl)
     PUT(launch_edge_csl(b->be_ds + S.off[P_BE], b->be_csl + S.off[P_BE], (int)be.size(), b->stream));
   PUT(put_range(b, b->bb_nodes, S.off[P_BB], bb));
   PUT(put_range(b, b->bt_nodes, S.off[P_BT], bt));
   PUT(put_range(b, b->elarea, S.off[P_TRI], prep->elarea));
-  if (b->be_dxy) PUT(put_range(b, b->be_dxy, S.off[P_BE], prep->be_dxy));
+  if (b->be_g32) {
+    std::vector<EdgeGeo32> g(prep->be_g32);
+    for (EdgeGeo32 &x : g) {
+      x.n1 += v0;
+      x.n2 += v0;
+    }
+    PUT(put_range(b, b->be_g32, S.off[P_BE], g));
+  }
   if (b->tri_g32) PUT(put_range(b, b->tri_g32, S.off[P_BT], prep->tri_g32));
   PUT(put_range(b, b->sw_nodes, S.off[P_SW], sw));
   PUT(cudaMemcpyAsync(b->mc + sid, &mc, sizeof(mc), cudaMemcpyHostToDevice, b->stream));
@@ -1080,6 +1162,10 @@ extern "C" int32_t fvm_layout_stats(const fvm_mesh *m, int64_t *out) {
   out[3] = L.max_slots;
   out[4] = L.max_tri;
   out[5] = (int64_t)L.bb_nodes.size();
+  out[6] = L.max_tri2;
+  out[7] = L.max_loc;
+  out[8] = (int64_t)L.halo_ids.size();
+  out[9] = verify_layout(L);
   return FVM_OK;
 }
 
@@ -1154,6 +1240,10 @@ extern "C" int32_t fvm_gpu_create(const fvm_params *par, const fvm_mesh *m, fvm_
   c.solid_edges = std::max<int64_t>(1, L.sw_nodes.size());
   c.max_slots = std::max(1, L.max_slots);
   c.max_tri = std::max(1, L.max_tri);
+  c.max_tri2 = std::max(1, L.max_tri2);
+  c.max_loc = std::max(1, L.max_loc);
+  c.halo_entries = std::max<int64_t>(1, L.halo_ids.size());
+  c.halo_incidence = std::max<int64_t>(1, L.hl_list.size());
   c.grid = L.nblk;
   fvm_handle *h = new (std::nothrow) fvm_handle();
   if (!h) return FVM_ERR_NOMEM;

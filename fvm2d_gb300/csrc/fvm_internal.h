@@ -43,12 +43,15 @@ constexpr uint8_t kVtxFarfield = 2;
 
 struct BlockInfo {          // 16 ints, one per CTA
   int mesh;                 // mesh slot
-  int v0, nv;               // arena vertex range
+  int v0, nv;               // arena vertex range (local slots [0, nv))
   int e0, ne;               // interior edge entries (be_* arrays)
   int b0, nb;               // boundary edges (bb_* arrays); 2 slots each
-  int t0, nt;               // triangle entries (bt_* arrays)
+  int t0, nt;               // triangles touching the block (bt_* arrays)
   int part;                 // index of this block's partial-sum record
-  int pad[6];
+  int nt2;                  // nt + triangles touching only the halo (bt_* from t0)
+  int h0, nh;               // halo vertices (halo_ids): local slots [nv, nv+nh)
+  int hp0;                  // halo incidence pointers (hl_ptr, nh+1 entries)
+  int pad[2];
 };
 
 // Per-mesh constants (read-only during a solve).  Mirrors fvm_params plus
@@ -116,6 +119,17 @@ struct alignas(16) TriGeo32 {
   float pad;
 };
 
+// One interior edge entry of a block for the FP32 kernels: its ends, the
+// FP64 edge vector and dual-face normal rounded once to FP32 (flux.f:10-13
+// computes ct, st, len from ds), and the ends' local slots; 32 bytes, read
+// with two 16-byte loads.
+struct alignas(16) EdgeGeo32 {
+  int n1, n2;          // arena vertex ids
+  float dx, dy;        // x(n2)-x(n1), y(n2)-y(n1)
+  float ct, st, len;   // ds/|ds| and |ds|
+  uint32_t loc;        // local slots of n1 (low half) and n2 (high half)
+};
+
 // Device pointers of an arena (all arena-global indices).
 template <typename R>
 struct ArenaPtrs {
@@ -144,10 +158,16 @@ struct ArenaPtrs {
   const int4 *bb_nodes;   // boundary entries (n1, n2, type, -)
   const int4 *bt_nodes;   // triangle entries (n1, n2, n3, arena triangle)
   const double *elarea;   // per arena triangle
-  const float2 *be_dxy;   // FP32 path: x(n2)-x(n1), y(n2)-y(n1) of each edge entry
+  const EdgeGeo32 *be_g32; // FP32 path: ends, geometry and local slots of each edge entry
   const TriGeo32 *tri_g32; // FP32 path: per triangle entry of the blocks (bt_* order)
   // solid edges per mesh for clcd (n1, n2) in beindx order
   const int2 *sw_nodes;
+  // fused gradient+flux pass: local slots of edge ends, halo vertices and
+  // their triangle incidence (slot | pos << 14 in the block's bt list)
+  const uint32_t *be_loc;
+  const int *halo_ids;
+  const int *hl_ptr;      // per block, nh+1 absolute offsets into hl_list
+  const uint16_t *hl_list;
   // all-edge incidence (limitgrad.f loops over netot edges)
   const int2 *va_rng;
   const int *va_list;     // other vertex | (is n2) << 31

@@ -271,36 +271,38 @@ __device__ __forceinline__ FluxConst<R> flux_const(const MeshConst &mc) {
 template <typename R, int FLUX>
 __device__ __forceinline__ void edge_flux(const ArenaPtrs<R> &A, const FluxConst<R> &fc,
                                           const R4<R> *P, int e, R f[4], int &err) {
-  const int2 nn = A.be_nodes[e];
-  const R4<R> p1 = P[nn.x], p2 = P[nn.y];
-  const Grad<R> g1 = A.grad[nn.x], g2 = A.grad[nn.y];
-  R dx, dy;
+  int2 nn;
+  R dx, dy, ct, st, len;
   if constexpr (sizeof(R) == 4) {
-    const float2 d = A.be_dxy[e];
-    dx = d.x;
-    dy = d.y;
+    // first half of the entry (ends, edge vector) now, the normal after the
+    // reconstruction: fewer values live across it
+    const int4 h = reinterpret_cast<const int4 *>(A.be_g32 + e)[0];
+    nn = make_int2(h.x, h.y);
+    dx = __int_as_float(h.z);
+    dy = __int_as_float(h.w);
   } else {
+    nn = A.be_nodes[e];
     const double2 c1 = A.coord[nn.x], c2 = A.coord[nn.y];
     dx = c2.x - c1.x;
     dy = c2.y - c1.y;
   }
+  const R4<R> p1 = P[nn.x], p2 = P[nn.y];
+  const Grad<R> g1 = A.grad[nn.x], g2 = A.grad[nn.y];
   R pl[4], pr[4];
 #pragma unroll
   for (int q = 0; q < 4; q++)
     recon1<R>(comp(p1, q), comp(p2, q), g1.qx[q], g1.qy[q], g2.qx[q], g2.qy[q], dx, dy,
               fc.ilimit, fc.a11, fc.a12, fc.a21, fc.a22, fc.eps, pl[q], pr[q]);
-  R ct, st, len;
-  if constexpr (sizeof(R) == 8) {
+  if constexpr (sizeof(R) == 4) {
+    const float4 h = reinterpret_cast<const float4 *>(A.be_g32 + e)[1];
+    ct = h.x;
+    st = h.y;
+    len = h.z;
+  } else {
     const D4 csl = A.be_csl[e];
     ct = R(csl.x);
     st = R(csl.y);
     len = R(csl.z);
-  } else {
-    const double2 ds = A.be_ds[e];
-    const R d1 = R(ds.x), d2 = R(ds.y);
-    len = msqrt(d1 * d1 + d2 * d2);
-    ct = d1 / len;
-    st = d2 / len;
   }
   const int which = FLUX ? FLUX : fc.iflux;
   if (which == 1) {
@@ -332,11 +334,11 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_FLUX_MINB32 
       const BlockInfo *nb = next_block(A.blocks, A.work, w, nwork);
       if (nb) {
         const BlockInfo n = *nb;
-        prefetch_l2(A.be_nodes + n.e0, sizeof(int2) * n.ne);
-        if (sizeof(R) == 8) prefetch_l2(A.be_csl + n.e0, sizeof(D4) * n.ne);
-        else {
-          prefetch_l2(A.be_ds + n.e0, sizeof(double2) * n.ne);
-          prefetch_l2(A.be_dxy + n.e0, sizeof(float2) * n.ne);
+        if (sizeof(R) == 8) {
+          prefetch_l2(A.be_nodes + n.e0, sizeof(int2) * n.ne);
+          prefetch_l2(A.be_csl + n.e0, sizeof(D4) * n.ne);
+        } else {
+          prefetch_l2(A.be_g32 + n.e0, sizeof(EdgeGeo32) * n.ne);
         }
         prefetch_l2(P + n.v0, sizeof(R4<R>) * n.nv);
         prefetch_l2(A.grad + n.v0, sizeof(Grad<R>) * n.nv);
@@ -488,6 +490,371 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_FLUX_MINB32 
         }
         BlockPartial bp;
         bp.sumsq = s;
+        bp.maxabs = m;
+        bp.argmax = a;
+        bp.pad = 0;
+        A.part[bi.part] = bp;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Fused stage: gradients, fluxes and the RK stage of one block in one pass
+// (iterate mode).  Phase A computes dxt/dyt of every triangle touching the
+// block or its halo (and the tri_visc terms of the block's own triangles);
+// phase B sums them into the Green-Gauss gradients of the block's own and
+// halo vertices, each in ascending triangle order exactly as the owner
+// block would, so the halo gradients equal the owner's bit for bit; phase C
+// computes the edge fluxes from those gradients; phase D gathers and
+// updates.  Replaces k_grad + k_flux: the gradients never leave shared
+// memory except the own ones, written for the stage-3 consumers (clcd, SA).
+// ---------------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ void tri_dxy(const ArenaPtrs<R> &A, const int4 &t, int entry,
+                                        R dbxx[3], R dbyy[3]) {
+  if constexpr (sizeof(R) == 4) {
+    const TriGeo32 tg = A.tri_g32[entry];
+    for (int j = 0; j < 3; j++) {
+      dbxx[j] = tg.dbxx[j];
+      dbyy[j] = tg.dbyy[j];
+    }
+  } else {
+    const double2 c1 = A.coord[t.x], c2 = A.coord[t.y], c3 = A.coord[t.z];
+    dbxx[0] = c2.y - c3.y;
+    dbxx[1] = c3.y - c1.y;
+    dbxx[2] = c1.y - c2.y;
+    dbyy[0] = c3.x - c2.x;
+    dbyy[1] = c1.x - c3.x;
+    dbyy[2] = c2.x - c1.x;
+  }
+}
+
+// Shared memory: region 1 = max(max_tri2 triangle records [+ viscous terms of
+// max_tri], max_slots fluxes) (fluxes reuse the triangle area after phase B);
+// region 2 = max_loc gradients.
+template <typename R, int FLUX>
+__global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_FLUX_MINB32 : 2)
+    k_step(ArenaPtrs<R> A, int stage, int max_tri, int max_tri2, int max_slots, int max_loc,
+           int viscous) {
+  extern __shared__ __align__(32) unsigned char smem_raw[];
+  const size_t tri_bytes = size_t(max_tri2) * sizeof(TriSmem<R>) + (viscous ? size_t(max_tri) * 9 * sizeof(R) : 0);
+  const size_t flux_bytes = size_t(max_slots) * sizeof(R4<R>);
+  const size_t r1 = ((tri_bytes > flux_bytes ? tri_bytes : flux_bytes) + 63) & ~size_t(63);
+  TriSmem<R> *s_tri = reinterpret_cast<TriSmem<R> *>(smem_raw);
+  R *s_vis = reinterpret_cast<R *>(s_tri + max_tri2);
+  R4<R> *s_flux = reinterpret_cast<R4<R> *>(smem_raw);
+  Grad<R> *s_grad = reinterpret_cast<Grad<R> *>(smem_raw + r1);
+  __shared__ double s_red[kBlockVerts / 32];
+  __shared__ double s_max[kBlockVerts / 32];
+  __shared__ int s_arg[kBlockVerts / 32];
+  const int nwork = *A.nwork;
+  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+    const BlockInfo bi = A.blocks[A.work[w]];
+    MeshCtl &ctl = A.ctl[bi.mesh];
+    if (!ctl.active) continue;
+    const MeshConst &mc = A.mc[bi.mesh];
+    const bool visc = mc.iflow != 1;
+    const int p = ctl.phase;
+    const R4<R> *P = A.st[cur_buf(p, stage)];
+    if (threadIdx.x == 0) {
+      const BlockInfo *nb = next_block(A.blocks, A.work, w, nwork);
+      if (nb) {
+        const BlockInfo n = *nb;
+        prefetch_l2(A.bt_nodes + n.t0, sizeof(int4) * n.nt2);
+        if (sizeof(R) == 4) {
+          prefetch_l2(A.tri_g32 + n.t0, sizeof(TriGeo32) * n.nt2);
+          prefetch_l2(A.be_g32 + n.e0, sizeof(EdgeGeo32) * n.ne);
+        } else {
+          prefetch_l2(A.coord + n.v0, sizeof(double2) * n.nv);
+          prefetch_l2(A.be_csl + n.e0, sizeof(D4) * n.ne);
+          prefetch_l2(A.be_nodes + n.e0, sizeof(int2) * n.ne);
+          prefetch_l2(A.be_loc + n.e0, sizeof(uint32_t) * n.ne);
+        }
+        prefetch_l2(P + n.v0, sizeof(R4<R>) * n.nv);
+        prefetch_l2(A.vt_rng + n.v0, sizeof(int2) * n.nv);
+        prefetch_l2(A.ve_rng + n.v0, sizeof(int2) * n.nv);
+        prefetch_l2(A.ais + n.v0, sizeof(double) * n.nv);
+        prefetch_l2(A.st[old_buf(p, stage)] + n.v0, sizeof(R4<R>) * n.nv);
+        prefetch_l2(A.cvarea + n.v0, sizeof(double) * n.nv);
+      }
+    }
+    // phase A: triangles of the block and of its halo
+    for (int k = threadIdx.x; k < bi.nt2; k += blockDim.x) {
+      const int4 t = A.bt_nodes[bi.t0 + k];
+      const R4<R> p1 = P[t.x], p2 = P[t.y], p3 = P[t.z];
+      R dbxx[3], dbyy[3];
+      tri_dxy<R>(A, t, bi.t0 + k, dbxx, dbyy);
+      TriSmem<R> ts;
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const R a1 = comp(p1, q), a2 = comp(p2, q), a3 = comp(p3, q);
+        ts.dxt[q] = a1 * dbxx[0] + a2 * dbxx[1] + a3 * dbxx[2];
+        ts.dyt[q] = a1 * dbyy[0] + a2 * dbyy[1] + a3 * dbyy[2];
+      }
+      s_tri[k] = ts;
+      if (visc && k < bi.nt) {
+        // tri_visc (green_gauss.f:132-194)
+        const R n2b3 = R(2) / R(3);
+        const R en1 = p1.w / p1.x, en2 = p2.w / p2.x, en3 = p3.w / p3.x;
+        const R ext = en1 * dbxx[0] + en2 * dbxx[1] + en3 * dbxx[2];
+        const R eyt = en1 * dbyy[0] + en2 * dbyy[1] + en3 * dbyy[2];
+        const R um = (p1.y + p2.y + p3.y) / R(3);
+        const R vm = (p1.z + p2.z + p3.z) / R(3);
+        const int nbuf = ctl.nphase;
+        const R mut = (A.mu[t.x] + A.mu[t.y] + A.mu[t.z]) / R(3);
+        const R mult = (A.mul[t.x] + A.mul[t.y] + A.mul[t.z]) / R(3);
+        const R prim5t = (A.nut[nbuf][t.x] + A.nut[nbuf][t.y] + A.nut[nbuf][t.z]) / R(3);
+        const R rhot = (p1.x + p2.x + p3.x) / R(3);
+        const R chi = prim5t * rhot / mult;
+        const R chi3 = cube(chi);
+        const R fv1 = chi3 / (chi3 + R(mc.cv11));
+        const R txx = n2b3 * mut * (R(2) * ts.dxt[1] - ts.dyt[2]);
+        const R txy = mut * (ts.dyt[1] + ts.dxt[2]);
+        const R tyy = n2b3 * mut * (R(2) * ts.dyt[2] - ts.dxt[1]);
+        const R gpr = R(mc.gamma) * (mult / R(mc.prandtl) + rhot * prim5t * fv1 / R(mc.prandtl_turb)) /
+                      R(mc.gamma1);
+        const R efx = txx * um + txy * vm + gpr * ext;
+        const R efy = txy * um + tyy * vm + gpr * eyt;
+        R areat;
+        if constexpr (sizeof(R) == 4) areat = A.tri_g32[bi.t0 + k].areat;
+        else areat = 0.25 / A.elarea[t.w];
+        R *sv = s_vis + 9 * k;
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+          sv[3 * j + 0] = (txx * dbxx[j] + txy * dbyy[j]) * areat;
+          sv[3 * j + 1] = (txy * dbxx[j] + tyy * dbyy[j]) * areat;
+          sv[3 * j + 2] = (efx * dbxx[j] + efy * dbyy[j]) * areat;
+        }
+      }
+    }
+    __syncthreads();
+    // phase B: gradients of own vertices (thread t = own vertex t, which
+    // keeps its viscous residual part and time step in registers) and of
+    // the halo vertices
+    R rv[3] = {R(0), R(0), R(0)};
+    R dtv = R(0);
+    const int t = threadIdx.x;
+    if (t < bi.nv) {
+      const int v = bi.v0 + t;
+      R qx[4] = {R(0), R(0), R(0), R(0)}, qy[4] = {R(0), R(0), R(0), R(0)};
+      const int2 jr = A.vt_rng[v];
+      for (int j = jr.x; j < jr.y; j++) {
+        const uint16_t e = A.vt_list[j];
+        const int slot = e & 0x3fff;
+        const TriSmem<R> ts = s_tri[slot];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          qx[q] = qx[q] + ts.dxt[q];
+          qy[q] = qy[q] + ts.dyt[q];
+        }
+        if (visc) {
+          const R *sv = s_vis + 9 * slot + 3 * (e >> kTriPosShift);
+          rv[0] = rv[0] + sv[0];
+          rv[1] = rv[1] + sv[1];
+          rv[2] = rv[2] + sv[2];
+        }
+      }
+      const R ais = R(A.ais[v]);
+      Grad<R> g;
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        g.qx[q] = qx[q] * ais;
+        g.qy[q] = qy[q] * ais;
+      }
+      s_grad[t] = g;
+      A.grad[v] = g;
+      if (visc) dtv = A.dt[v];
+      else if (stage == 1) {
+        dtv = time_step<R>(mc, P[v], R(0), A.drmin[v]);
+        A.dt[v] = dtv;
+      } else {
+        dtv = A.dt[v];
+      }
+    }
+    for (int h = t; h < bi.nh; h += blockDim.x) {
+      const int g0 = A.hl_ptr[bi.hp0 + h], g1 = A.hl_ptr[bi.hp0 + h + 1];
+      R qx[4] = {R(0), R(0), R(0), R(0)}, qy[4] = {R(0), R(0), R(0), R(0)};
+      for (int j = g0; j < g1; j++) {
+        const TriSmem<R> ts = s_tri[A.hl_list[j] & 0x3fff];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          qx[q] = qx[q] + ts.dxt[q];
+          qy[q] = qy[q] + ts.dyt[q];
+        }
+      }
+      const R ais = R(A.ais[A.halo_ids[bi.h0 + h]]);
+      Grad<R> g;
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        g.qx[q] = qx[q] * ais;
+        g.qy[q] = qy[q] * ais;
+      }
+      s_grad[bi.nv + h] = g;
+    }
+    __syncthreads();
+    // phase C: interior edge fluxes from the shared gradients
+    int err = 0;
+    const FluxConst<R> fc = flux_const<R>(mc);
+    for (int k = threadIdx.x; k < bi.ne; k += blockDim.x) {
+      const int e = bi.e0 + k;
+      int2 nn;
+      uint32_t ll;
+      R dx, dy, ct, st, len;
+      if constexpr (sizeof(R) == 4) {
+        const EdgeGeo32 g = A.be_g32[e];
+        nn = make_int2(g.n1, g.n2);
+        ll = g.loc;
+        dx = g.dx;
+        dy = g.dy;
+        ct = g.ct;
+        st = g.st;
+        len = g.len;
+      } else {
+        nn = A.be_nodes[e];
+        ll = A.be_loc[e];
+        const double2 c1 = A.coord[nn.x], c2 = A.coord[nn.y];
+        dx = c2.x - c1.x;
+        dy = c2.y - c1.y;
+        const D4 csl = A.be_csl[e];
+        ct = R(csl.x);
+        st = R(csl.y);
+        len = R(csl.z);
+      }
+      const R4<R> p1 = P[nn.x], p2 = P[nn.y];
+      const Grad<R> g1 = s_grad[ll & 0xffff], g2 = s_grad[ll >> 16];
+      R pl[4], pr[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+        recon1<R>(comp(p1, q), comp(p2, q), g1.qx[q], g1.qy[q], g2.qx[q], g2.qy[q], dx, dy,
+                  fc.ilimit, fc.a11, fc.a12, fc.a21, fc.a22, fc.eps, pl[q], pr[q]);
+      R f[4];
+      const int which = FLUX ? FLUX : fc.iflux;
+      if (which == 1) {
+        if (!roe_flux<R>(ct, st, len, pl, pr, fc.gamma, fc.gamma1, f)) err = 1;
+      } else if (which == 2) {
+        kfvs_flux<R>(ct, st, len, pl, pr, fc.gamma1, fc.pi, f);
+      } else {
+        hllc_flux<R>(ct, st, len, pl, pr, fc.gamma, fc.gamma1, fc.rotate_back, f);
+      }
+      R4<R> o;
+      o.x = f[0];
+      o.y = f[1];
+      o.z = f[2];
+      o.w = f[3];
+      s_flux[k] = o;
+    }
+    // boundary edges, two slots each (contribution to n1, to n2)
+    for (int k = threadIdx.x; k < bi.nb; k += blockDim.x) {
+      const int4 b = A.bb_nodes[bi.b0 + k];
+      const double2 x1 = A.coord[b.x], x2 = A.coord[b.y];
+      const R4<R> p1 = P[b.x], p2 = P[b.y];
+      R4<R> o1, o2;
+      if (b.z == 1) {
+        // solid_flux.f:10-17
+        const R sx = R(0.5) * R(x2.y - x1.y);
+        const R sy = -R(0.5) * R(x2.x - x1.x);
+        const R pp1 = R(0.75) * p1.w + R(0.25) * p2.w;
+        const R pp2 = R(0.25) * p1.w + R(0.75) * p2.w;
+        o1.x = R(0);
+        o1.y = pp1 * sx;
+        o1.z = pp1 * sy;
+        o1.w = R(0);
+        o2.x = R(0);
+        o2.y = pp2 * sx;
+        o2.z = pp2 * sy;
+        o2.w = R(0);
+      } else {
+        R f1[4], f2[4];
+        farfield_flux<R>(mc, ctl.cl, x1, x2, p1, p2, f1, f2);
+        o1.x = f1[0];
+        o1.y = f1[1];
+        o1.z = f1[2];
+        o1.w = f1[3];
+        o2.x = f2[0];
+        o2.y = f2[1];
+        o2.z = f2[2];
+        o2.w = f2[3];
+      }
+      s_flux[bi.ne + 2 * k] = o1;
+      s_flux[bi.ne + 2 * k + 1] = o2;
+    }
+    if (err) atomicCAS(&ctl.err, 0, 4 /* FVM_ERR_ROE_SONIC */);
+    __syncthreads();
+    // phase D: gather per own vertex in Fortran order, RK stage
+    double d2 = 0.0, dabs = 0.0;
+    int darg = INT_MAX;
+    if (t < bi.nv) {
+      const int v = bi.v0 + t;
+      R acc[4];
+      acc[0] = R(0);
+      acc[1] = rv[0];
+      acc[2] = rv[1];
+      acc[3] = rv[2];
+      const int2 jr = A.ve_rng[v];
+      for (int j = jr.x; j < jr.y; j++) {
+        const uint16_t e = A.ve_list[j];
+        const R4<R> f = s_flux[e & kSlotMask];
+        if (e & kSolidBit) {
+          acc[1] = acc[1] + f.y;
+          acc[2] = acc[2] + f.z;
+        } else if (e & kNegBit) {
+          acc[0] = acc[0] - f.x;
+          acc[1] = acc[1] - f.y;
+          acc[2] = acc[2] - f.z;
+          acc[3] = acc[3] - f.w;
+        } else {
+          acc[0] = acc[0] + f.x;
+          acc[1] = acc[1] + f.y;
+          acc[2] = acc[2] + f.z;
+          acc[3] = acc[3] + f.w;
+        }
+      }
+      const R4<R> po = A.st[old_buf(p, stage)][v];
+      const R4<R> pc = P[v];
+      const bool noslip = visc && (A.vflag[v] & kVtxSolid);
+      const R4<R> pn = rk_update<R>(mc, stage, po, pc, dtv, A.cvarea[v], acc, noslip);
+      A.st[out_buf(p, stage)][v] = pn;
+      if (stage == 3) {
+        const double gra = double(pn.x) - double(po.x);
+        d2 = gra * gra;
+        dabs = fabs(gra);
+        if (dabs > 0.0) darg = A.orig[v];
+        if (pn.x <= R(0) || pn.w <= R(0)) atomicMin(&ctl.err_point, A.orig[v]);
+      }
+    }
+    if (stage == 3) {
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        const double o2 = __shfl_down_sync(0xffffffffu, d2, off);
+        const double om = __shfl_down_sync(0xffffffffu, dabs, off);
+        const int oa = __shfl_down_sync(0xffffffffu, darg, off);
+        d2 += o2;
+        if (om > dabs || (om == dabs && oa < darg)) {
+          dabs = om;
+          darg = oa;
+        }
+      }
+      const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+      if (lane == 0) {
+        s_red[wid] = d2;
+        s_max[wid] = dabs;
+        s_arg[wid] = darg;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double sacc = 0.0, m = 0.0;
+        int a = INT_MAX;
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++) {
+          sacc += s_red[i];
+          if (s_max[i] > m || (s_max[i] == m && s_arg[i] < a)) {
+            m = s_max[i];
+            a = s_arg[i];
+          }
+        }
+        BlockPartial bp;
+        bp.sumsq = sacc;
         bp.maxabs = m;
         bp.argmax = a;
         bp.pad = 0;

@@ -7,6 +7,21 @@
 
 namespace fvm {
 
+// Grid of a persistent per-block kernel: one wave of the CTAs that fit on
+// the device at once (its occupancy with this shared memory), so that no
+// partial second wave idles most SMs at the end of a launch.
+template <typename K>
+inline int fit_grid(const LaunchCfg &c, K kern, size_t smem) {
+  if (!c.fit) return c.grid;
+  int occ = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kBlockVerts, smem) != cudaSuccess) {
+    (void)cudaGetLastError();
+    occ = 1;
+  }
+  const int g = (occ < 1 ? 1 : occ) * c.sms;
+  return g < c.grid ? g : c.grid;
+}
+
 #define FVM_DEFINE_LAUNCHERS(R)                                                            \
   size_t smem_grad(const LaunchCfg &c, R *) {                                              \
     return size_t(c.max_tri) * (sizeof(TriSmem<R>) + (c.viscous ? 9 * sizeof(R) : 0));     \
@@ -17,14 +32,14 @@ namespace fvm {
   }                                                                                        \
   cudaError_t launch_visc(const ArenaPtrs<R> &A, const LaunchCfg &c, int stage, int do_dt,  \
                           int routine) {                                                   \
-    k_visc<R><<<c.grid, kBlockVerts, 0, c.stream>>>(A, stage, do_dt, routine);             \
+    k_visc<R><<<fit_grid(c, k_visc<R>, 0), kBlockVerts, 0, c.stream>>>(A, stage, do_dt, routine);             \
     return cudaGetLastError();                                                             \
   }                                                                                        \
   cudaError_t launch_grad(const ArenaPtrs<R> &A, const LaunchCfg &c, int stage, int do_dt,  \
                           int routine) {                                                   \
     size_t sm = smem_grad(c, (R *)nullptr);                                                \
     if (sm > kMaxSmem) return cudaErrorInvalidConfiguration;                              \
-    k_grad<R><<<c.grid, kBlockVerts, sm, c.stream>>>(A, stage, do_dt, routine, c.max_tri);  \
+    k_grad<R><<<fit_grid(c, k_grad<R>, sm), kBlockVerts, sm, c.stream>>>(A, stage, do_dt, routine, c.max_tri);  \
     return cudaGetLastError();                                                             \
   }                                                                                        \
   cudaError_t launch_flux(const ArenaPtrs<R> &A, const LaunchCfg &c, int stage, int mode,   \
@@ -32,17 +47,36 @@ namespace fvm {
     size_t sm = smem_flux(c, (R *)nullptr);                                                \
     if (sm > kMaxSmem) return cudaErrorInvalidConfiguration;                              \
     switch (c.flux) {                                                                      \
-      case 1: k_flux<R, 1><<<c.grid, kBlockVerts, sm, c.stream>>>(A, stage, mode, irk, routine); break; \
-      case 2: k_flux<R, 2><<<c.grid, kBlockVerts, sm, c.stream>>>(A, stage, mode, irk, routine); break; \
-      case 3: k_flux<R, 3><<<c.grid, kBlockVerts, sm, c.stream>>>(A, stage, mode, irk, routine); break; \
-      default: k_flux<R, 0><<<c.grid, kBlockVerts, sm, c.stream>>>(A, stage, mode, irk, routine); \
+      case 1: k_flux<R, 1><<<fit_grid(c, k_flux<R, 1>, sm), kBlockVerts, sm, c.stream>>>(A, stage, mode, irk, routine); break; \
+      case 2: k_flux<R, 2><<<fit_grid(c, k_flux<R, 2>, sm), kBlockVerts, sm, c.stream>>>(A, stage, mode, irk, routine); break; \
+      case 3: k_flux<R, 3><<<fit_grid(c, k_flux<R, 3>, sm), kBlockVerts, sm, c.stream>>>(A, stage, mode, irk, routine); break; \
+      default: k_flux<R, 0><<<fit_grid(c, k_flux<R, 0>, sm), kBlockVerts, sm, c.stream>>>(A, stage, mode, irk, routine); \
+    }                                                                                      \
+    return cudaGetLastError();                                                             \
+  }                                                                                        \
+  size_t smem_step(const LaunchCfg &c, R *) {                                              \
+    const size_t tri = size_t(c.max_tri2) * sizeof(TriSmem<R>) +                           \
+                       (c.viscous ? size_t(c.max_tri) * 9 * sizeof(R) : 0);                 \
+    const size_t flx = size_t(c.max_slots) * sizeof(R4<R>);                                \
+    const size_t r1 = ((tri > flx ? tri : flx) + 63) & ~size_t(63);                        \
+    return r1 + size_t(c.max_loc) * sizeof(Grad<R>);                                       \
+  }                                                                                        \
+  cudaError_t launch_step(const ArenaPtrs<R> &A, const LaunchCfg &c, int stage) {           \
+    const size_t sm = smem_step(c, (R *)nullptr);                                          \
+    if (sm > kMaxSmem) return cudaErrorInvalidConfiguration;                              \
+    const int v = c.viscous ? 1 : 0;                                                       \
+    switch (c.flux) {                                                                      \
+      case 1: k_step<R, 1><<<fit_grid(c, k_step<R, 1>, sm), kBlockVerts, sm, c.stream>>>(A, stage, c.max_tri, c.max_tri2, c.max_slots, c.max_loc, v); break; \
+      case 2: k_step<R, 2><<<fit_grid(c, k_step<R, 2>, sm), kBlockVerts, sm, c.stream>>>(A, stage, c.max_tri, c.max_tri2, c.max_slots, c.max_loc, v); break; \
+      case 3: k_step<R, 3><<<fit_grid(c, k_step<R, 3>, sm), kBlockVerts, sm, c.stream>>>(A, stage, c.max_tri, c.max_tri2, c.max_slots, c.max_loc, v); break; \
+      default: k_step<R, 0><<<fit_grid(c, k_step<R, 0>, sm), kBlockVerts, sm, c.stream>>>(A, stage, c.max_tri, c.max_tri2, c.max_slots, c.max_loc, v); \
     }                                                                                      \
     return cudaGetLastError();                                                             \
   }                                                                                        \
   cudaError_t launch_sa(const ArenaPtrs<R> &A, const LaunchCfg &c, int stage, int routine) {\
     size_t sm = smem_sa(c, (R *)nullptr);                                                  \
     if (sm > kMaxSmem) return cudaErrorInvalidConfiguration;                              \
-    k_sa<R><<<c.grid, kBlockVerts, sm, c.stream>>>(A, stage, routine, c.max_tri);           \
+    k_sa<R><<<fit_grid(c, k_sa<R>, sm), kBlockVerts, sm, c.stream>>>(A, stage, routine, c.max_tri);           \
     return cudaGetLastError();                                                             \
   }                                                                                        \
   cudaError_t launch_monitor(const ArenaPtrs<R> &A, const LaunchCfg &c, int serial_clcd) {  \
@@ -78,7 +112,17 @@ namespace fvm {
   cudaError_t prepare_attributes(const LaunchCfg &c, R *) {                                \
     const size_t g = smem_grad(c, (R *)nullptr), f = smem_flux(c, (R *)nullptr),           \
                  s = smem_sa(c, (R *)nullptr);                                             \
-    if (g > kMaxSmem || f > kMaxSmem || s > kMaxSmem) return cudaErrorInvalidConfiguration; \
+    const size_t st = smem_step(c, (R *)nullptr);                                          \
+    if (g > kMaxSmem || f > kMaxSmem || s > kMaxSmem || st > kMaxSmem)                     \
+      return cudaErrorInvalidConfiguration;                                                \
+    for (int k = 0; k < 4; k++) {                                                          \
+      cudaError_t e2 = cudaSuccess;                                                        \
+      if (k == 0) e2 = cudaFuncSetAttribute(k_step<R, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)st); \
+      if (k == 1) e2 = cudaFuncSetAttribute(k_step<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)st); \
+      if (k == 2) e2 = cudaFuncSetAttribute(k_step<R, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)st); \
+      if (k == 3) e2 = cudaFuncSetAttribute(k_step<R, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)st); \
+      if (e2 != cudaSuccess) return e2;                                                    \
+    }                                                                                      \
     cudaError_t e = cudaFuncSetAttribute(k_grad<R>,                                        \
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g); \
     if (e == cudaSuccess)                                                                  \

@@ -16,6 +16,10 @@ struct LaunchCfg {
   int max_slots;     // max edge slots (interior + 2 x boundary) of any block
   bool viscous;      // any mesh viscous (gradient-pass shared memory)
   int flux;          // 1/2/3: every mesh uses that Riemann solver; 0: mixed
+  int max_tri2;      // max triangles of a block plus those of its halo
+  int max_loc;       // max own + halo vertices of a block
+  int sms;           // multiprocessors of the device
+  bool fit;          // grid = CTAs resident at once (occupancy x sms), capped by grid
   cudaStream_t stream;
 };
 
@@ -27,6 +31,8 @@ struct LaunchCfg {
   cudaError_t launch_flux(const ArenaPtrs<R> &A, const LaunchCfg &c, int stage, int mode,  \
                           int irk, int routine);                                          \
   cudaError_t launch_sa(const ArenaPtrs<R> &A, const LaunchCfg &c, int stage, int routine);\
+  cudaError_t launch_step(const ArenaPtrs<R> &A, const LaunchCfg &c, int stage);           \
+  size_t smem_step(const LaunchCfg &c, R *);                                              \
   cudaError_t launch_monitor(const ArenaPtrs<R> &A, const LaunchCfg &c, int serial_clcd); \
   cudaError_t launch_update(const ArenaPtrs<R> &A, const LaunchCfg &c, int irk);           \
   cudaError_t launch_time_step(const ArenaPtrs<R> &A, const LaunchCfg &c);                 \

@@ -18,6 +18,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <unordered_map>
 
 namespace fvm {
 
@@ -189,6 +190,64 @@ int32_t build_layout(const fvm_mesh &m, int bv, MeshLayout &L) {
     if (bl[1] != bl[0]) btris[bl[1]].push_back(t);
     if (bl[2] != bl[0] && bl[2] != bl[1]) btris[bl[2]].push_back(t);
   }
+  // vertex -> triangles (ascending), for the halo's triangles
+  std::vector<int> vt_cnt(np + 1, 0);
+  for (int t = 0; t < nt; t++)
+    for (int k = 0; k < 3; k++) vt_cnt[L.iperm[m.elem[3 * t + k] - 1] + 1]++;
+  for (int v = 0; v < np; v++) vt_cnt[v + 1] += vt_cnt[v];
+  std::vector<int> vt_adj(vt_cnt[np]);
+  {
+    std::vector<int> fill(vt_cnt.begin(), vt_cnt.end() - 1);
+    for (int t = 0; t < nt; t++)
+      for (int k = 0; k < 3; k++) vt_adj[fill[L.iperm[m.elem[3 * t + k] - 1]]++] = t;
+  }
+  // halo of each block (vertices outside it sharing an edge or a triangle
+  // with it) and the triangles touching the halo but not the block, which
+  // follow the block's own triangles in its bt list
+  std::vector<int> loc(np, -1);
+  std::vector<std::vector<int>> btris_extra(nblk);
+  for (int b = 0; b < nblk; b++) {
+    const int v0 = L.blocks[b].v0, v1 = v0 + L.blocks[b].nv;
+    auto inblk = [&](int v) { return v >= v0 && v < v1; };
+    std::vector<int> halo;
+    auto want = [&](int v) {
+      if (!inblk(v) && loc[v] == -1) {
+        loc[v] = -2;
+        halo.push_back(v);
+      }
+    };
+    for (int t : btris[b])
+      for (int q = 0; q < 3; q++) want(L.iperm[m.elem[3 * t + q] - 1]);
+    for (int e : bedges[b]) {
+      want(L.iperm[m.edge[2 * e] - 1]);
+      want(L.iperm[m.edge[2 * e + 1] - 1]);
+    }
+    for (const int4 &q : bbnd[b]) {
+      want(q.x);
+      want(q.y);
+    }
+    std::sort(halo.begin(), halo.end());
+    for (int v : halo) loc[v] = -1;
+    BlockInfo &bi = L.blocks[b];
+    bi.h0 = (int)L.halo_ids.size();
+    bi.nh = (int)halo.size();
+    L.halo_ids.insert(L.halo_ids.end(), halo.begin(), halo.end());
+    const int nloc = bi.nv + bi.nh;
+    if (nloc > 0xffff) return FVM_ERR_CAPACITY;
+    L.max_loc = std::max(L.max_loc, nloc);
+    // triangles of halo vertices not already in the block's list
+    std::vector<int> extra;
+    for (int v : halo)
+      for (int j = vt_cnt[v]; j < vt_cnt[v + 1]; j++) {
+        const int t = vt_adj[j];
+        bool touches_block = false;
+        for (int q = 0; q < 3; q++) touches_block |= inblk(L.iperm[m.elem[3 * t + q] - 1]);
+        if (!touches_block) extra.push_back(t);
+      }
+    std::sort(extra.begin(), extra.end());
+    extra.erase(std::unique(extra.begin(), extra.end()), extra.end());
+    btris_extra[b] = std::move(extra);
+  }
   // per-vertex lists
   std::vector<std::vector<uint16_t>> vint(np), vbnd(np), vtri(np);
   for (int b = 0; b < nblk; b++) {
@@ -197,10 +256,16 @@ int32_t build_layout(const fvm_mesh &m, int bv, MeshLayout &L) {
     auto inblk = [&](int v) { return v >= v0 && v < v1; };
     bi.e0 = (int)L.be_nodes.size();
     bi.ne = (int)bedges[b].size();
+    const int *hbeg = L.halo_ids.data() + bi.h0, *hend = hbeg + bi.nh;
+    auto local = [&](int v) -> uint32_t {
+      if (inblk(v)) return (uint32_t)(v - v0);
+      return (uint32_t)(bi.nv + (std::lower_bound(hbeg, hend, v) - hbeg));
+    };
     for (int k = 0; k < bi.ne; k++) {
       const int e = bedges[b][k];
       const int a = L.iperm[m.edge[2 * e] - 1], c = L.iperm[m.edge[2 * e + 1] - 1];
       L.be_nodes.push_back(make_int2(a, c));
+      L.be_loc.push_back(local(a) | (local(c) << 16));
       L.be_edge.push_back(e);
       if (inblk(a)) vint[a].push_back((uint16_t)k);
       if (inblk(c)) vint[c].push_back((uint16_t)(k | kNegBit));
@@ -229,6 +294,36 @@ int32_t build_layout(const fvm_mesh &m, int bv, MeshLayout &L) {
       for (int q = 0; q < 3; q++)
         if (inblk(n[q])) vtri[n[q]].push_back((uint16_t)(k | (q << kTriPosShift)));
     }
+    // the halo's other triangles follow, then each halo vertex lists its
+    // triangles (ascending triangle number: the order green_gauss.f visits)
+    const std::vector<int> &extra = btris_extra[b];
+    bi.nt2 = bi.nt + (int)extra.size();
+    if (bi.nt2 > 0x3fff) return FVM_ERR_CAPACITY;
+    L.max_tri2 = std::max(L.max_tri2, bi.nt2);
+    for (int t : extra) {
+      int n[3];
+      for (int q = 0; q < 3; q++) n[q] = L.iperm[m.elem[3 * t + q] - 1];
+      L.bt_nodes.push_back(make_int4(n[0], n[1], n[2], t));
+    }
+    {
+      std::unordered_map<int, int> slot_of;
+      slot_of.reserve(2 * bi.nt2);
+      for (int k = 0; k < bi.nt; k++) slot_of[btris[b][k]] = k;
+      for (size_t k = 0; k < extra.size(); k++) slot_of[extra[k]] = bi.nt + (int)k;
+      bi.hp0 = (int)L.hl_ptr.size();
+      for (int h = 0; h < bi.nh; h++) {
+        const int v = hbeg[h];
+        L.hl_ptr.push_back((int)L.hl_list.size());
+        for (int j = vt_cnt[v]; j < vt_cnt[v + 1]; j++) {
+          const int t = vt_adj[j];
+          int pos = 0;
+          for (int q = 0; q < 3; q++)
+            if (L.iperm[m.elem[3 * t + q] - 1] == v) pos = q;
+          L.hl_list.push_back((uint16_t)(slot_of.at(t) | (pos << kTriPosShift)));
+        }
+      }
+      L.hl_ptr.push_back((int)L.hl_list.size());
+    }
   }
   L.ve_ptr.assign(np + 1, 0);
   L.vt_ptr.assign(np + 1, 0);
@@ -255,6 +350,87 @@ int32_t build_layout(const fvm_mesh &m, int bv, MeshLayout &L) {
   L.va_list.reserve(L.va_ptr[np]);
   for (int v = 0; v < np; v++) L.va_list.insert(L.va_list.end(), vall[v].begin(), vall[v].end());
   return FVM_OK;
+}
+
+int64_t verify_layout(const MeshLayout &L) {
+  int64_t bad = 0;
+  auto has = [](const int4 &t, int v, int pos) {
+    return (pos == 0 ? t.x : pos == 1 ? t.y : t.z) == v;
+  };
+  for (const BlockInfo &bi : L.blocks) {
+    const int nloc = bi.nv + bi.nh, nslot = bi.ne + 2 * bi.nb;
+    if (bi.nv > kBlockVerts || nloc > L.max_loc || bi.nt > L.max_tri || bi.nt2 > L.max_tri2 ||
+        bi.nt2 < bi.nt || nslot > L.max_slots) {
+      bad++;
+      continue;
+    }
+    auto vert_of = [&](uint32_t l) {
+      return (int)l < bi.nv ? bi.v0 + (int)l : L.halo_ids[bi.h0 + (int)l - bi.nv];
+    };
+    for (int k = 0; k < bi.ne; k++) {
+      const uint32_t ll = L.be_loc[bi.e0 + k];
+      const int2 nn = L.be_nodes[bi.e0 + k];
+      if ((int)(ll & 0xffff) >= nloc || (int)(ll >> 16) >= nloc ||
+          vert_of(ll & 0xffff) != nn.x || vert_of(ll >> 16) != nn.y)
+        bad++;
+    }
+    for (int h = 1; h < bi.nh; h++)
+      if (L.halo_ids[bi.h0 + h] <= L.halo_ids[bi.h0 + h - 1]) bad++;
+    // own vertices: triangles among the block's own, ascending
+    for (int v = bi.v0; v < bi.v0 + bi.nv; v++) {
+      int last = -1;
+      for (int j = L.vt_ptr[v]; j < L.vt_ptr[v + 1]; j++) {
+        const int slot = L.vt_list[j] & 0x3fff, pos = L.vt_list[j] >> kTriPosShift;
+        if (slot >= bi.nt || pos > 2 || !has(L.bt_nodes[bi.t0 + slot], v, pos) ||
+            L.bt_nodes[bi.t0 + slot].w <= last) {
+          bad++;
+          break;
+        }
+        last = L.bt_nodes[bi.t0 + slot].w;
+      }
+      for (int j = L.ve_ptr[v]; j < L.ve_ptr[v + 1]; j++)
+        if ((L.ve_list[j] & kSlotMask) >= nslot) bad++;
+    }
+    // halo vertices: the owner's triangles, in the owner's order
+    for (int h = 0; h < bi.nh; h++) {
+      const int v = L.halo_ids[bi.h0 + h];
+      const int g0 = L.hl_ptr[bi.hp0 + h], g1 = L.hl_ptr[bi.hp0 + h + 1];
+      const int o0 = L.vt_ptr[v], o1 = L.vt_ptr[v + 1];
+      if (g1 - g0 != o1 - o0) {
+        bad++;
+        continue;
+      }
+      for (int j = 0; j < g1 - g0; j++) {
+        const int slot = L.hl_list[g0 + j] & 0x3fff, pos = L.hl_list[g0 + j] >> kTriPosShift;
+        if (slot >= bi.nt2 || pos > 2 || !has(L.bt_nodes[bi.t0 + slot], v, pos)) {
+          bad++;
+          break;
+        }
+      }
+    }
+  }
+  // halo triangle order equals the owner's: compare driver triangle ids
+  std::vector<int> owner(L.np, -1);
+  for (int b = 0; b < L.nblk; b++)
+    for (int v = L.blocks[b].v0; v < L.blocks[b].v0 + L.blocks[b].nv; v++) owner[v] = b;
+  for (const BlockInfo &bi : L.blocks)
+    for (int h = 0; h < bi.nh; h++) {
+      const int v = L.halo_ids[bi.h0 + h];
+      if (v < 0 || v >= L.np || owner[v] < 0) {
+        bad++;
+        continue;
+      }
+      const BlockInfo &ob = L.blocks[owner[v]];
+      const int g0 = L.hl_ptr[bi.hp0 + h], o0 = L.vt_ptr[v], n = L.vt_ptr[v + 1] - o0;
+      if (L.hl_ptr[bi.hp0 + h + 1] - g0 != n) continue;   // counted above
+      for (int j = 0; j < n; j++)
+        if (L.bt_nodes[bi.t0 + (L.hl_list[g0 + j] & 0x3fff)].w !=
+            L.bt_nodes[ob.t0 + (L.vt_list[o0 + j] & 0x3fff)].w) {
+          bad++;
+          break;
+        }
+    }
+  return bad;
 }
 
 }  // namespace fvm

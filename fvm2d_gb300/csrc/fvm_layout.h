@@ -31,13 +31,23 @@ struct MeshLayout {
   std::vector<int> va_list;
   std::vector<int2> sw_nodes;     // solid edges in beindx order (new ids)
   std::vector<uint8_t> vflag;     // kVtxSolid / kVtxFarfield
-  int max_tri = 0, max_slots = 0;
+  // fused gradient+flux pass
+  std::vector<uint32_t> be_loc;   // local slots of each edge entry's ends
+  std::vector<int> halo_ids;      // per block: halo vertices (new ids), ascending
+  std::vector<int> hl_ptr;        // per block: nh+1 offsets (relative) into hl_list
+  std::vector<uint16_t> hl_list;  // halo vertex triangles: slot | pos << 14
+  int max_tri = 0, max_slots = 0, max_tri2 = 0, max_loc = 0;
 };
 
 // Builds the layout; returns FVM_OK or FVM_ERR_ARG (bad connectivity) /
 // FVM_ERR_CAPACITY (a block needs more slots than the incidence entries can
 // address).
 int32_t build_layout(const fvm_mesh &m, int block_verts, MeshLayout &L);
+
+// Checks the fused-pass invariants of a built layout (local slots decode to
+// the edge ends, halo triangle lists equal the owners' lists in order,
+// every index inside its block's tiles); returns the number of violations.
+int64_t verify_layout(const MeshLayout &L);
 
 // Vertex order only (exposed for tests of the partitioner).
 void order_vertices(int np, const std::vector<int> &adj_ptr, const std::vector<int> &adj,

@@ -270,7 +270,12 @@ typedef struct fvm_batch_caps {
   int64_t edge_incidence, tri_incidence, all_incidence, solid_edges;
   int32_t max_slots, max_tri;   /* per-block shared-memory sizing           */
   int32_t grid;                 /* CTAs of the block kernels (0 = occupancy) */
-  int32_t reserved;
+  int32_t max_tri2;             /* triangles of a block and of its halo      */
+  int32_t max_loc;              /* own + halo vertices of a block            */
+  int32_t fused;                /* 1: one fused gradient+flux pass per stage
+                                   (recomputes halo gradients in shared
+                                   memory); 0 (default): separate passes    */
+  int64_t halo_entries, halo_incidence;
 } fvm_batch_caps;
 
 int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *caps,
@@ -333,8 +338,11 @@ int64_t fvm_batch_launch_count(fvm_batch *b);
 
 /* Layout statistics of a mesh after renumbering (no GPU needed):
  * out[0] blocks, [1] interior edge entries (cut edges counted in both
- * blocks), [2] triangle entries, [3] max slots of a block, [4] max
- * triangles of a block, [5] boundary edge entries. */
+ * blocks), [2] triangle entries (block and halo), [3] max slots of a
+ * block, [4] max triangles of a block, [5] boundary edge entries, [6] max
+ * triangles of a block and its halo, [7] max own + halo vertices, [8] halo
+ * vertices, [9] violations of the layout's invariants (0 for a valid
+ * layout).  out has 10 elements. */
 int32_t fvm_layout_stats(const fvm_mesh *m, int64_t *out);
 
 #ifdef __cplusplus

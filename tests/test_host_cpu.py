@@ -88,6 +88,26 @@ def test_host_geometry_equals_oracle(oracle_lib, fvm_lib, case):
         assert m.ne < m.netot      # zero-length Barth faces dropped (flength.f:84-98)
 
 
+@pytest.mark.parametrize("case", ["median", "barth", "jitter", "tiny"])
+def test_block_layout_invariants(fvm_lib, case):
+    """The fused pass reads halo gradients that it computes itself: every
+    edge's local slots must decode to its ends, and every halo vertex must
+    list the same triangles in the same order as its owner block (so both
+    sum them in the same order).  Checked by the library on the host."""
+    from fvm2d_gb300.batch import layout_stats
+    g = {"median": lambda: workload_grid("euler_160x48"),
+         "barth": lambda: naca_ogrid(96, 32),
+         "jitter": lambda: naca_ogrid(96, 40, jitter=0.1, seed=3),
+         "tiny": lambda: naca_ogrid(20, 8)}[case]()
+    cell = L.BARTH if case == "barth" else L.MEDIAN
+    m = fvm_lib.build_geometry(g.coord, g.elem, g.ptype, cell_type=cell, setup_on_gpu=False)
+    st = layout_stats(m)
+    assert st["layout_violations"] == 0
+    assert st["max_loc"] <= 576 and st["max_tri2"] <= 1280       # default tiles
+    assert st["max_tri2"] >= st["max_tri"]
+    assert (st["halo_entries"] > 0) == (st["blocks"] > 1)
+
+
 def test_geometry_rejects_degenerate(fvm_lib):
     coord = np.array([[0.0, 0.0], [1.0, 0.0], [2.0, 0.0], [0.0, 1.0]])
     elem = np.array([[1, 2, 3], [1, 2, 4]], dtype=np.int32)
