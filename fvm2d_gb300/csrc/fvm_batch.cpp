@@ -103,6 +103,7 @@ struct fvm_batch {
   void *dt = nullptr, *mu = nullptr, *mul = nullptr, *nut[2] = {nullptr, nullptr};
   double2 *coord = nullptr;
   double *ais = nullptr, *cvarea = nullptr, *drmin = nullptr, *wd = nullptr;
+  float *ais32 = nullptr, *cvarea32 = nullptr, *drmin32 = nullptr;   // FP32 batches
   int *orig = nullptr;
   uint8_t *vflag = nullptr;
   int2 *ve_rng = nullptr, *vt_rng = nullptr, *va_rng = nullptr;
@@ -186,6 +187,9 @@ ArenaPtrs<R> ptrs(const fvm_batch *b) {
   A.ais = b->ais;
   A.cvarea = b->cvarea;
   A.drmin = b->drmin;
+  A.ais32 = b->ais32;
+  A.cvarea32 = b->cvarea32;
+  A.drmin32 = b->drmin32;
   A.wd = b->wd;
   A.orig = b->orig;
   A.vflag = b->vflag;
@@ -279,6 +283,20 @@ MeshConst make_const(const fvm_params &p) {
   }
   c.sin_aoa = std::sin(p.aoa);
   c.cos_aoa = std::cos(p.aoa);
+  MeshConstF &f = c.f;
+#define F32(x) f.x = (float)c.x
+  F32(gamma); F32(gamma1); F32(gas_const); F32(pi); F32(prandtl); F32(prandtl_turb);
+  F32(albada11); F32(albada12); F32(albada21); F32(albada22); F32(epsilon);
+  F32(cb1); F32(cb2); F32(sigma_sa); F32(kolm); F32(cw1); F32(cw2); F32(cw3); F32(cv1); F32(cv2);
+  F32(cv11); F32(cw31); F32(cw32); F32(kolm2); F32(cb2sig1); F32(cb2sig2);
+  F32(mach_inf); F32(aoa); F32(rey); F32(cfl);
+  F32(q_inf); F32(r_inf); F32(p_inf); F32(t_inf); F32(u_inf); F32(v_inf); F32(a_inf);
+  F32(sconst); F32(nut_inf);
+  for (int k = 0; k < 3; k++) {
+    F32(airk[k]);
+    F32(birk[k]);
+  }
+#undef F32
   return c;
 }
 
@@ -597,6 +615,9 @@ extern "C" int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *cap
   TRYB(dalloc(O, &b->elarea, (size_t)c.triangles));
   if (precision == FVM_PREC_FP32) {
     TRYB(dalloc(O, &b->be_g32, (size_t)c.edge_entries));
+    TRYB(dalloc(O, &b->ais32, V));
+    TRYB(dalloc(O, &b->cvarea32, V));
+    TRYB(dalloc(O, &b->drmin32, V));
     TRYB(dalloc(O, &b->tri_g32, (size_t)c.tri_entries));
   }
   TRYB(dalloc(O, &b->sw_nodes, (size_t)c.solid_edges));
@@ -619,6 +640,7 @@ extern "C" int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *cap
   b->cfg.max_tri2 = c.max_tri2;
   b->cfg.max_loc = c.max_loc;
   b->fused = c.fused > 0;
+  b->cfg.grad_vertex = c.grad_vertex > 0;
   b->cfg.viscous = c.viscous != 0;
   b->cfg.stream = b->stream;
   int dev = 0, sms = 0;
@@ -875,6 +897,15 @@ extern "C" int32_t fvm_batch_add_prepared(fvm_batch *b, fvm_prepared *prep, int3
   PUT(put_range(b, b->ais, v0, prep->ais));
   PUT(put_range(b, b->cvarea, v0, prep->cvarea));
   PUT(put_range(b, b->drmin, v0, prep->drmin));
+  if (b->ais32) {
+    std::vector<float> f(prep->ais.size());
+    for (size_t i = 0; i < f.size(); i++) f[i] = (float)prep->ais[i];
+    PUT(put_range(b, b->ais32, v0, f));
+    for (size_t i = 0; i < f.size(); i++) f[i] = (float)prep->cvarea[i];
+    PUT(put_range(b, b->cvarea32, v0, f));
+    for (size_t i = 0; i < f.size(); i++) f[i] = (float)prep->drmin[i];
+    PUT(put_range(b, b->drmin32, v0, f));
+  }
   PUT(put_range(b, b->wd, v0, prep->wd));
   PUT(put_range(b, b->orig, v0, prep->orig));
   PUT(put_range(b, b->vflag, v0, L.vflag));

@@ -296,7 +296,7 @@ template <typename R>
 __device__ __forceinline__ void farfield_flux(const MeshConst &mc, double cl, double2 x1,
                                               double2 x2, const R4<R> &P1, const R4<R> &P2,
                                               R flux1[4], R flux2[4]) {
-  const R GAMMA = R(mc.gamma), gamma1 = R(mc.gamma1);
+  const R GAMMA = MCR(R, gamma), gamma1 = MCR(R, gamma1);
   R uinf, vinf, q2inf, pinf, rinf;
   if (mc.mach_inf < 1.0 && mc.vortex == 1) {
     // point-vortex correction (farfield_flux.f:28-44), evaluated in FP64
@@ -322,11 +322,11 @@ __device__ __forceinline__ void farfield_flux(const MeshConst &mc, double cl, do
     rinf = R(ri);
     pinf = R(pi_);
   } else {
-    uinf = R(mc.u_inf);
-    vinf = R(mc.v_inf);
+    uinf = MCR(R, u_inf);
+    vinf = MCR(R, v_inf);
     q2inf = sq(uinf) + sq(vinf);
-    pinf = R(mc.p_inf);
-    rinf = R(mc.r_inf);
+    pinf = MCR(R, p_inf);
+    rinf = MCR(R, r_inf);
   }
   R Uout[4] = {rinf, rinf * uinf, rinf * vinf, pinf / gamma1 + R(0.5) * rinf * q2inf};
   R ra = R(0.5) * (P1.x + P2.x);
@@ -408,31 +408,31 @@ __device__ __forceinline__ void farfield_flux(const MeshConst &mc, double cl, do
 // ------------------------------------------------------------ viscosity.f
 template <typename R>
 __device__ __forceinline__ R sutherland_viscosity(const MeshConst &mc, R density, R pressure) {
-  R temp = pressure / density / R(mc.gas_const);
-  R num = R(mc.t_inf) + R(mc.sconst);
-  R den = temp + R(mc.sconst);
-  return mpow(temp / R(mc.t_inf), R(1.5)) * (num / den) / R(mc.rey);
+  R temp = pressure / density / MCR(R, gas_const);
+  R num = MCR(R, t_inf) + MCR(R, sconst);
+  R den = temp + MCR(R, sconst);
+  return mpow(temp / MCR(R, t_inf), R(1.5)) * (num / den) / MCR(R, rey);
 }
 
 template <typename R>
 __device__ __forceinline__ R mu_turb(const MeshConst &mc, R mu_lam, R density, R nu_tilde) {
   R chi = nu_tilde * density / mu_lam;
   R chi3 = cube(chi);
-  R fv1 = chi3 / (chi3 + R(mc.cv11));
+  R fv1 = chi3 / (chi3 + MCR(R, cv11));
   return density * nu_tilde * fv1;
 }
 
 // ------------------------------------------------------------ time_step.f
 template <typename R>
-__device__ __forceinline__ R time_step(const MeshConst &mc, const R4<R> &P, R mu, double drmin) {
+__device__ __forceinline__ R time_step(const MeshConst &mc, const R4<R> &P, R mu, R drmin) {
   R q = msqrt(sq(P.y) + sq(P.z));
-  R a = msqrt(R(mc.gamma) * P.w / P.x);
-  R dr = R(drmin);
+  R a = msqrt(MCR(R, gamma) * P.w / P.x);
+  R dr = drmin;
   if (mc.iflow != 1) {
-    R dtv = R(2) * R(mc.gamma) * mu / (P.x * R(mc.prandtl));
-    return R(mc.cfl) * sq(dr) / (dr * (q + a) + dtv);
+    R dtv = R(2) * MCR(R, gamma) * mu / (P.x * MCR(R, prandtl));
+    return MCR(R, cfl) * sq(dr) / (dr * (q + a) + dtv);
   }
-  return R(mc.cfl) * dr / (q + a);
+  return MCR(R, cfl) * dr / (q + a);
 }
 
 // ---------------------------------------------------- update.f, convert.f
@@ -446,14 +446,14 @@ __device__ __forceinline__ void prim2con(const R4<R> &P, R gamma1, R c[4]) {
 
 template <typename R>
 __device__ __forceinline__ R4<R> rk_update(const MeshConst &mc, int irk, const R4<R> &Po,
-                                           const R4<R> &Pc, R dt, double cvarea,
+                                           const R4<R> &Pc, R dt, R cvarea,
                                            const R res[4], bool noslip) {
-  const R gamma1 = R(mc.gamma1);
-  R a = R(mc.airk[irk - 1]), b = R(mc.birk[irk - 1]);
+  const R gamma1 = MCR(R, gamma1);
+  R a = MCR(R, airk[irk - 1]), b = MCR(R, birk[irk - 1]);
   R c0[4], c1[4], cn[4];
   prim2con(Po, gamma1, c0);
   prim2con(Pc, gamma1, c1);
-  R f = dt / R(cvarea);
+  R f = dt / cvarea;
 #pragma unroll
   for (int j = 0; j < 4; j++) cn[j] = a * c0[j] + b * (c1[j] - f * res[j]);
   if (noslip) {
@@ -475,17 +475,17 @@ __device__ __forceinline__ R update_sa(const MeshConst &mc, R nut, R rho, R mul,
   R wd = R(wd_);
   R chi = nut * rho / mul;
   R chi3 = cube(chi);
-  R fv1 = chi3 / (chi3 + R(mc.cv11));
-  R fv2 = R(1) / cube(R(1) + chi / R(mc.cv2));
-  R r = nut / wd / (wd * R(mc.kolm2));
+  R fv1 = chi3 / (chi3 + MCR(R, cv11));
+  R fv2 = R(1) / cube(R(1) + chi / MCR(R, cv2));
+  R r = nut / wd / (wd * MCR(R, kolm2));
   R fv3 = (R(1) + chi * fv1) * (R(1) - fv2) / dmax1(chi, R(0.001));
   R S = fv3 * mfabs(omega) + r * fv2;
   r = r / S;
   r = dmin1(r, R(2));
-  R g = r + R(mc.cw2) * (pow6(r) - r);
-  R fw = g * mpow(R(mc.cw31) / (pow6(g) + R(mc.cw32)), R(1) / R(6));
-  R source = R(mc.cb1) * S * nut;
-  R fact = R(1) + R(mc.cw1) * fw * (nut / wd) * (dt / wd);
+  R g = r + MCR(R, cw2) * (pow6(r) - r);
+  R fw = g * mpow(MCR(R, cw31) / (pow6(g) + MCR(R, cw32)), R(1) / R(6));
+  R source = MCR(R, cb1) * S * nut;
+  R fact = R(1) + MCR(R, cw1) * fw * (nut / wd) * (dt / wd);
   return (nut - (dt / R(cvarea)) * divf + dt * source) / fact;
 }
 

@@ -56,6 +56,18 @@ struct BlockInfo {          // 16 ints, one per CTA
 
 // Per-mesh constants (read-only during a solve).  Mirrors fvm_params plus
 // arena placement.
+// FP32 copies of a mesh's constants (each the FP64 value rounded once, as a
+// conversion in the kernel would give), so the FP32 kernels convert nothing.
+struct MeshConstF {
+  float gamma, gamma1, gas_const, pi, prandtl, prandtl_turb;
+  float albada11, albada12, albada21, albada22, epsilon;
+  float cb1, cb2, sigma_sa, kolm, cw1, cw2, cw3, cv1, cv2;
+  float cv11, cw31, cw32, kolm2, cb2sig1, cb2sig2;
+  float mach_inf, aoa, rey, cfl;
+  float q_inf, r_inf, p_inf, t_inf, u_inf, v_inf, a_inf, sconst, nut_inf;
+  float airk[3], birk[3];
+};
+
 struct MeshConst {
   int iflow, iflux, ilimit, vortex, bugcompat, precision;
   int v0, nv;                       // vertex range
@@ -72,7 +84,11 @@ struct MeshConst {
   double xref, yref;
   double airk[3], birk[3];
   double sin_aoa, cos_aoa;          // host libm values (clcd.f:45-46)
+  MeshConstF f;
 };
+
+// A mesh constant in the kernel's precision: the FP32 copy for R = float.
+#define MCR(R, name) (sizeof(R) == 4 ? R(mc.f.name) : R(mc.name))
 
 // Per-mesh mutable control block.
 struct MeshCtl {
@@ -159,6 +175,7 @@ struct ArenaPtrs {
   const int4 *bt_nodes;   // triangle entries (n1, n2, n3, arena triangle)
   const double *elarea;   // per arena triangle
   const EdgeGeo32 *be_g32; // FP32 path: ends, geometry and local slots of each edge entry
+  const float *ais32, *cvarea32, *drmin32;   // FP32 path: per-vertex copies
   const TriGeo32 *tri_g32; // FP32 path: per triangle entry of the blocks (bt_* order)
   // solid edges per mesh for clcd (n1, n2) in beindx order
   const int2 *sw_nodes;

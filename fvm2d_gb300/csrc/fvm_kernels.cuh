@@ -15,7 +15,13 @@
 #include "fvm_device.cuh"
 
 #ifndef FVM_FLUX_MINB32
-#define FVM_FLUX_MINB32 4   // resident CTAs per SM asked of the FP32 flux kernel
+#define FVM_FLUX_MINB32 6   // resident CTAs per SM asked of the FP32 flux kernel
+#endif
+#ifndef FVM_GRAD_MINB32
+#define FVM_GRAD_MINB32 5   // resident CTAs per SM asked of the FP32 gradient kernel
+#endif
+#ifndef FVM_GRADV_MINB32
+#define FVM_GRADV_MINB32 4  // the same for its per-vertex form
 #endif
 
 namespace fvm {
@@ -64,6 +70,23 @@ __device__ __forceinline__ const BlockInfo *next_block(const BlockInfo *blocks, 
 // Viscosity (viscosity.f:2-55) and, at stage 1, the viscous time step
 // (time_step.f:13-20) from the previous mu.  One thread per vertex.
 // ---------------------------------------------------------------------------
+// Per-vertex geometry in the kernel's precision (FP32 copies for R = float).
+template <typename R>
+__device__ __forceinline__ R v_ais(const ArenaPtrs<R> &A, int v) {
+  if constexpr (sizeof(R) == 4) return A.ais32[v];
+  else return A.ais[v];
+}
+template <typename R>
+__device__ __forceinline__ R v_cvarea(const ArenaPtrs<R> &A, int v) {
+  if constexpr (sizeof(R) == 4) return A.cvarea32[v];
+  else return A.cvarea[v];
+}
+template <typename R>
+__device__ __forceinline__ R v_drmin(const ArenaPtrs<R> &A, int v) {
+  if constexpr (sizeof(R) == 4) return A.drmin32[v];
+  else return A.drmin[v];
+}
+
 template <typename R>
 __global__ void __launch_bounds__(kBlockVerts) k_visc(ArenaPtrs<R> A, int stage, int do_dt,
                                                       int routine) {
@@ -76,7 +99,7 @@ __global__ void __launch_bounds__(kBlockVerts) k_visc(ArenaPtrs<R> A, int stage,
     if (mc.iflow == 1 || threadIdx.x >= bi.nv) continue;   // inviscid: mu stays 0
     const int v = bi.v0 + threadIdx.x;
     const R4<R> P = A.st[cur_buf(ctl.phase, stage)][v];
-    if (do_dt) A.dt[v] = time_step<R>(mc, P, A.mu[v], A.drmin[v]);
+    if (do_dt) A.dt[v] = time_step<R>(mc, P, A.mu[v], v_drmin(A, v));
     R mul = sutherland_viscosity<R>(mc, P.x, P.w);
     A.mul[v] = mul;
     if (mc.iflow == 2) {
@@ -99,8 +122,93 @@ struct TriSmem {
   R dyt[4];
 };
 
+// a + b rounded as written (never fused with a product that forms b)
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+
+// Green-Gauss terms of one triangle (green_gauss.f:100-127): dbxx/dbyy of
+// its vertices and the sums dxt/dyt of the four primitive variables.
 template <typename R>
-__global__ void __launch_bounds__(kBlockVerts) k_grad(ArenaPtrs<R> A, int stage, int do_dt,
+__device__ __forceinline__ void tri_geom(const ArenaPtrs<R> &A, const int4 &t, int entry,
+                                         R dbxx[3], R dbyy[3]) {
+  if constexpr (sizeof(R) == 4) {
+    const TriGeo32 tg = A.tri_g32[entry];
+    for (int j = 0; j < 3; j++) {
+      dbxx[j] = tg.dbxx[j];
+      dbyy[j] = tg.dbyy[j];
+    }
+  } else {
+    const double2 c1 = A.coord[t.x], c2 = A.coord[t.y], c3 = A.coord[t.z];
+    dbxx[0] = c2.y - c3.y;
+    dbxx[1] = c3.y - c1.y;
+    dbxx[2] = c1.y - c2.y;
+    dbyy[0] = c3.x - c2.x;
+    dbyy[1] = c1.x - c3.x;
+    dbyy[2] = c2.x - c1.x;
+  }
+}
+
+template <typename R>
+__device__ __forceinline__ void tri_sums(const R4<R> &p1, const R4<R> &p2, const R4<R> &p3,
+                                         const R dbxx[3], const R dbyy[3], TriSmem<R> &ts) {
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    const R a1 = comp(p1, q), a2 = comp(p2, q), a3 = comp(p3, q);
+    ts.dxt[q] = a1 * dbxx[0] + a2 * dbxx[1] + a3 * dbxx[2];
+    ts.dyt[q] = a1 * dbyy[0] + a2 * dbyy[1] + a3 * dbyy[2];
+  }
+}
+
+// tri_visc (green_gauss.f:132-194): stresses and heat flux of one triangle;
+// the contribution to its vertex at position j is
+// ((txx, txy, efx) . dbxx[j] + (txy, tyy, efy) . dbyy[j]) * areat.
+template <typename R>
+struct TriVisc {
+  R txx, txy, tyy, efx, efy, areat;
+};
+
+template <typename R>
+__device__ __forceinline__ TriVisc<R> tri_visc(const ArenaPtrs<R> &A, const MeshConst &mc,
+                                               int nbuf, const int4 &t, int entry,
+                                               const R4<R> &p1, const R4<R> &p2,
+                                               const R4<R> &p3, const R dbxx[3],
+                                               const R dbyy[3], const TriSmem<R> &ts) {
+  const R n2b3 = R(2) / R(3);
+  const R en1 = p1.w / p1.x, en2 = p2.w / p2.x, en3 = p3.w / p3.x;
+  const R ext = en1 * dbxx[0] + en2 * dbxx[1] + en3 * dbxx[2];
+  const R eyt = en1 * dbyy[0] + en2 * dbyy[1] + en3 * dbyy[2];
+  const R um = (p1.y + p2.y + p3.y) / R(3);
+  const R vm = (p1.z + p2.z + p3.z) / R(3);
+  const R mut = (A.mu[t.x] + A.mu[t.y] + A.mu[t.z]) / R(3);
+  const R mult = (A.mul[t.x] + A.mul[t.y] + A.mul[t.z]) / R(3);
+  const R prim5t = (A.nut[nbuf][t.x] + A.nut[nbuf][t.y] + A.nut[nbuf][t.z]) / R(3);
+  const R rhot = (p1.x + p2.x + p3.x) / R(3);
+  const R chi = prim5t * rhot / mult;
+  const R chi3 = cube(chi);
+  const R fv1 = chi3 / (chi3 + MCR(R, cv11));
+  TriVisc<R> o;
+  o.txx = n2b3 * mut * (R(2) * ts.dxt[1] - ts.dyt[2]);
+  o.txy = mut * (ts.dyt[1] + ts.dxt[2]);
+  o.tyy = n2b3 * mut * (R(2) * ts.dyt[2] - ts.dxt[1]);
+  const R gpr = MCR(R, gamma) * (mult / MCR(R, prandtl) + rhot * prim5t * fv1 / MCR(R, prandtl_turb)) /
+                MCR(R, gamma1);
+  o.efx = o.txx * um + o.txy * vm + gpr * ext;
+  o.efy = o.txy * um + o.tyy * vm + gpr * eyt;
+  if constexpr (sizeof(R) == 4) o.areat = A.tri_g32[entry].areat;
+  else o.areat = 0.25 / A.elarea[t.w];
+  return o;
+}
+
+template <typename R>
+__device__ __forceinline__ void tri_visc_term(const TriVisc<R> &tv, R dbx, R dby, R out[3]) {
+  out[0] = (tv.txx * dbx + tv.txy * dby) * tv.areat;
+  out[1] = (tv.txy * dbx + tv.tyy * dby) * tv.areat;
+  out[2] = (tv.efx * dbx + tv.efy * dby) * tv.areat;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRAD_MINB32 : 1)
+    k_grad(ArenaPtrs<R> A, int stage, int do_dt,
                                                       int routine, int max_tri) {
   extern __shared__ __align__(32) unsigned char smem_raw[];
   TriSmem<R> *s_tri = reinterpret_cast<TriSmem<R> *>(smem_raw);
@@ -122,7 +230,7 @@ __global__ void __launch_bounds__(kBlockVerts) k_grad(ArenaPtrs<R> A, int stage,
         prefetch_l2(P + n.v0, sizeof(R4<R>) * n.nv);
         if (sizeof(R) == 8) prefetch_l2(A.coord + n.v0, sizeof(double2) * n.nv);
         prefetch_l2(A.vt_rng + n.v0, sizeof(int2) * n.nv);
-        prefetch_l2(A.ais + n.v0, sizeof(double) * n.nv);
+        prefetch_l2(sizeof(R) == 4 ? (const void *)(A.ais32 + n.v0) : (const void *)(A.ais + n.v0), sizeof(R) * n.nv);
       }
     }
     // phase 1: one thread per triangle touching the block
@@ -130,62 +238,15 @@ __global__ void __launch_bounds__(kBlockVerts) k_grad(ArenaPtrs<R> A, int stage,
       const int4 t = A.bt_nodes[bi.t0 + k];
       const R4<R> p1 = P[t.x], p2 = P[t.y], p3 = P[t.z];
       R dbxx[3], dbyy[3];
-      if constexpr (sizeof(R) == 4) {
-        const TriGeo32 tg = A.tri_g32[bi.t0 + k];
-        for (int j = 0; j < 3; j++) {
-          dbxx[j] = tg.dbxx[j];
-          dbyy[j] = tg.dbyy[j];
-        }
-      } else {
-        const double2 c1 = A.coord[t.x], c2 = A.coord[t.y], c3 = A.coord[t.z];
-        dbxx[0] = c2.y - c3.y;
-        dbxx[1] = c3.y - c1.y;
-        dbxx[2] = c1.y - c2.y;
-        dbyy[0] = c3.x - c2.x;
-        dbyy[1] = c1.x - c3.x;
-        dbyy[2] = c2.x - c1.x;
-      }
+      tri_geom<R>(A, t, bi.t0 + k, dbxx, dbyy);
       TriSmem<R> ts;
-#pragma unroll
-      for (int q = 0; q < 4; q++) {
-        const R a1 = comp(p1, q), a2 = comp(p2, q), a3 = comp(p3, q);
-        ts.dxt[q] = a1 * dbxx[0] + a2 * dbxx[1] + a3 * dbxx[2];
-        ts.dyt[q] = a1 * dbyy[0] + a2 * dbyy[1] + a3 * dbyy[2];
-      }
+      tri_sums<R>(p1, p2, p3, dbxx, dbyy, ts);
       s_tri[k] = ts;
       if (visc) {
-        // tri_visc (green_gauss.f:132-194)
-        const R n2b3 = R(2) / R(3);
-        const R en1 = p1.w / p1.x, en2 = p2.w / p2.x, en3 = p3.w / p3.x;
-        const R ext = en1 * dbxx[0] + en2 * dbxx[1] + en3 * dbxx[2];
-        const R eyt = en1 * dbyy[0] + en2 * dbyy[1] + en3 * dbyy[2];
-        const R um = (p1.y + p2.y + p3.y) / R(3);
-        const R vm = (p1.z + p2.z + p3.z) / R(3);
-        const int nb = ctl.nphase;
-        const R mut = (A.mu[t.x] + A.mu[t.y] + A.mu[t.z]) / R(3);
-        const R mult = (A.mul[t.x] + A.mul[t.y] + A.mul[t.z]) / R(3);
-        const R prim5t = (A.nut[nb][t.x] + A.nut[nb][t.y] + A.nut[nb][t.z]) / R(3);
-        const R rhot = (p1.x + p2.x + p3.x) / R(3);
-        const R chi = prim5t * rhot / mult;
-        const R chi3 = cube(chi);
-        const R fv1 = chi3 / (chi3 + R(mc.cv11));
-        const R txx = n2b3 * mut * (R(2) * ts.dxt[1] - ts.dyt[2]);
-        const R txy = mut * (ts.dyt[1] + ts.dxt[2]);
-        const R tyy = n2b3 * mut * (R(2) * ts.dyt[2] - ts.dxt[1]);
-        const R gpr = R(mc.gamma) * (mult / R(mc.prandtl) + rhot * prim5t * fv1 / R(mc.prandtl_turb)) /
-                      R(mc.gamma1);
-        const R efx = txx * um + txy * vm + gpr * ext;
-        const R efy = txy * um + tyy * vm + gpr * eyt;
-        R areat;
-        if constexpr (sizeof(R) == 4) areat = A.tri_g32[bi.t0 + k].areat;
-        else areat = 0.25 / A.elarea[t.w];
+        const TriVisc<R> tv = tri_visc<R>(A, mc, ctl.nphase, t, bi.t0 + k, p1, p2, p3, dbxx, dbyy, ts);
         R *sv = s_vis + 9 * k;
 #pragma unroll
-        for (int j = 0; j < 3; j++) {
-          sv[3 * j + 0] = (txx * dbxx[j] + txy * dbyy[j]) * areat;
-          sv[3 * j + 1] = (txy * dbxx[j] + tyy * dbyy[j]) * areat;
-          sv[3 * j + 2] = (efx * dbxx[j] + efy * dbyy[j]) * areat;
-        }
+        for (int j = 0; j < 3; j++) tri_visc_term<R>(tv, dbxx[j], dbyy[j], sv + 3 * j);
       }
     }
     __syncthreads();
@@ -211,7 +272,7 @@ __global__ void __launch_bounds__(kBlockVerts) k_grad(ArenaPtrs<R> A, int stage,
           rv[2] = rv[2] + sv[2];
         }
       }
-      const R ais = R(A.ais[v]);
+      const R ais = v_ais(A, v);
       Grad<R> g;
 #pragma unroll
       for (int q = 0; q < 4; q++) {
@@ -227,10 +288,91 @@ __global__ void __launch_bounds__(kBlockVerts) k_grad(ArenaPtrs<R> A, int stage,
         r.w = rv[2];
         A.resv[v] = r;
       } else if (do_dt) {
-        A.dt[v] = time_step<R>(mc, P[v], R(0), A.drmin[v]);
+        A.dt[v] = time_step<R>(mc, P[v], R(0), v_drmin(A, v));
       }
     }
     __syncthreads();
+  }
+}
+
+// Gradient pass, per-vertex form: each thread walks its vertex's triangles
+// (ascending, as green_gauss.f visits them) and computes each triangle's
+// terms itself, straight from the triangle entries; no shared memory and no
+// barrier, at the price of computing every triangle once per vertex.  The
+// arithmetic of each term is that of k_grad, so both give the same sums.
+template <typename R>
+__global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRADV_MINB32 : 1)
+    k_grad_v(ArenaPtrs<R> A, int stage, int do_dt, int routine) {
+  const int nwork = *A.nwork;
+  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+    const BlockInfo bi = A.blocks[A.work[w]];
+    const MeshCtl &ctl = A.ctl[bi.mesh];
+    if (!routine && !ctl.active) continue;
+    const MeshConst &mc = A.mc[bi.mesh];
+    const bool visc = mc.iflow != 1;
+    const R4<R> *P = A.st[cur_buf(ctl.phase, stage)];
+    if (threadIdx.x == 0) {
+      const BlockInfo *nb = next_block(A.blocks, A.work, w, nwork);
+      if (nb) {
+        const BlockInfo n = *nb;
+        prefetch_l2(A.bt_nodes + n.t0, sizeof(int4) * n.nt);
+        if (sizeof(R) == 4) prefetch_l2(A.tri_g32 + n.t0, sizeof(TriGeo32) * n.nt);
+        prefetch_l2(P + n.v0, sizeof(R4<R>) * n.nv);
+        if (sizeof(R) == 8) prefetch_l2(A.coord + n.v0, sizeof(double2) * n.nv);
+        prefetch_l2(A.vt_rng + n.v0, sizeof(int2) * n.nv);
+        prefetch_l2(sizeof(R) == 4 ? (const void *)(A.ais32 + n.v0) : (const void *)(A.ais + n.v0), sizeof(R) * n.nv);
+      }
+    }
+    if (threadIdx.x >= bi.nv) continue;   // no barrier follows
+    const int v = bi.v0 + threadIdx.x;
+    R qx[4] = {R(0), R(0), R(0), R(0)}, qy[4] = {R(0), R(0), R(0), R(0)};
+    R rv[3] = {R(0), R(0), R(0)};
+    const int2 jr = A.vt_rng[v];
+    for (int j = jr.x; j < jr.y; j++) {
+      const uint16_t e = A.vt_list[j];
+      const int entry = bi.t0 + (e & 0x3fff);
+      const int4 t = A.bt_nodes[entry];
+      const R4<R> p1 = P[t.x], p2 = P[t.y], p3 = P[t.z];
+      R dbxx[3], dbyy[3];
+      tri_geom<R>(A, t, entry, dbxx, dbyy);
+      TriSmem<R> ts;
+      tri_sums<R>(p1, p2, p3, dbxx, dbyy, ts);
+      // plain (uncontracted) adds: each term is rounded before it is
+      // summed, as when k_grad reads it back from shared memory
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        qx[q] = add_rn(qx[q], ts.dxt[q]);
+        qy[q] = add_rn(qy[q], ts.dyt[q]);
+      }
+      if (visc) {
+        const int pos = e >> kTriPosShift;
+        const TriVisc<R> tv = tri_visc<R>(A, mc, ctl.nphase, t, entry, p1, p2, p3, dbxx, dbyy, ts);
+        R sv[3];
+        tri_visc_term<R>(tv, pos == 0 ? dbxx[0] : pos == 1 ? dbxx[1] : dbxx[2],
+                         pos == 0 ? dbyy[0] : pos == 1 ? dbyy[1] : dbyy[2], sv);
+        rv[0] = add_rn(rv[0], sv[0]);
+        rv[1] = add_rn(rv[1], sv[1]);
+        rv[2] = add_rn(rv[2], sv[2]);
+      }
+    }
+    const R ais = v_ais(A, v);
+    Grad<R> g;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      g.qx[q] = qx[q] * ais;
+      g.qy[q] = qy[q] * ais;
+    }
+    A.grad[v] = g;
+    if (visc) {
+      R4<R> r;
+      r.x = R(0);
+      r.y = rv[0];
+      r.z = rv[1];
+      r.w = rv[2];
+      A.resv[v] = r;
+    } else if (do_dt) {
+      A.dt[v] = time_step<R>(mc, P[v], R(0), v_drmin(A, v));
+    }
   }
 }
 
@@ -252,14 +394,14 @@ struct FluxConst {
 template <typename R>
 __device__ __forceinline__ FluxConst<R> flux_const(const MeshConst &mc) {
   FluxConst<R> c;
-  c.a11 = R(mc.albada11);
-  c.a12 = R(mc.albada12);
-  c.a21 = R(mc.albada21);
-  c.a22 = R(mc.albada22);
-  c.eps = R(mc.epsilon);
-  c.gamma = R(mc.gamma);
-  c.gamma1 = R(mc.gamma1);
-  c.pi = R(mc.pi);
+  c.a11 = MCR(R, albada11);
+  c.a12 = MCR(R, albada12);
+  c.a21 = MCR(R, albada21);
+  c.a22 = MCR(R, albada22);
+  c.eps = MCR(R, epsilon);
+  c.gamma = MCR(R, gamma);
+  c.gamma1 = MCR(R, gamma1);
+  c.pi = MCR(R, pi);
   c.ilimit = mc.ilimit;
   c.iflux = mc.iflux;
   c.rotate_back = mc.bugcompat ? 0 : 1;
@@ -347,7 +489,7 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_FLUX_MINB32 
         if (mode == MODE_UPDATE) {
           prefetch_l2(A.st[old_buf(p, stage)] + n.v0, sizeof(R4<R>) * n.nv);
           prefetch_l2(A.dt + n.v0, sizeof(R) * n.nv);
-          prefetch_l2(A.cvarea + n.v0, sizeof(double) * n.nv);
+          prefetch_l2(sizeof(R) == 4 ? (const void *)(A.cvarea32 + n.v0) : (const void *)(A.cvarea + n.v0), sizeof(R) * n.nv);
         }
       }
     }
@@ -446,7 +588,7 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_FLUX_MINB32 
         const R4<R> po = A.st[old_buf(p, stage)][v];
         const R4<R> pc = P[v];
         const bool noslip = (mc.iflow != 1) && (A.vflag[v] & kVtxSolid);
-        const R4<R> pn = rk_update<R>(mc, irk, po, pc, A.dt[v], A.cvarea[v], acc, noslip);
+        const R4<R> pn = rk_update<R>(mc, irk, po, pc, A.dt[v], v_cvarea(A, v), acc, noslip);
         A.st[out_buf(p, stage)][v] = pn;
         if (stage == 3) {
           // conres.f:14-22 partials and check_positivity.f:13-14 (rho, p)
@@ -511,26 +653,6 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_FLUX_MINB32 
 // updates.  Replaces k_grad + k_flux: the gradients never leave shared
 // memory except the own ones, written for the stage-3 consumers (clcd, SA).
 // ---------------------------------------------------------------------------
-template <typename R>
-__device__ __forceinline__ void tri_dxy(const ArenaPtrs<R> &A, const int4 &t, int entry,
-                                        R dbxx[3], R dbyy[3]) {
-  if constexpr (sizeof(R) == 4) {
-    const TriGeo32 tg = A.tri_g32[entry];
-    for (int j = 0; j < 3; j++) {
-      dbxx[j] = tg.dbxx[j];
-      dbyy[j] = tg.dbyy[j];
-    }
-  } else {
-    const double2 c1 = A.coord[t.x], c2 = A.coord[t.y], c3 = A.coord[t.z];
-    dbxx[0] = c2.y - c3.y;
-    dbxx[1] = c3.y - c1.y;
-    dbxx[2] = c1.y - c2.y;
-    dbyy[0] = c3.x - c2.x;
-    dbyy[1] = c1.x - c3.x;
-    dbyy[2] = c2.x - c1.x;
-  }
-}
-
 // Shared memory: region 1 = max(max_tri2 triangle records [+ viscous terms of
 // max_tri], max_slots fluxes) (fluxes reuse the triangle area after phase B);
 // region 2 = max_loc gradients.
@@ -575,9 +697,9 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_FLUX_MINB32 
         prefetch_l2(P + n.v0, sizeof(R4<R>) * n.nv);
         prefetch_l2(A.vt_rng + n.v0, sizeof(int2) * n.nv);
         prefetch_l2(A.ve_rng + n.v0, sizeof(int2) * n.nv);
-        prefetch_l2(A.ais + n.v0, sizeof(double) * n.nv);
+        prefetch_l2(sizeof(R) == 4 ? (const void *)(A.ais32 + n.v0) : (const void *)(A.ais + n.v0), sizeof(R) * n.nv);
         prefetch_l2(A.st[old_buf(p, stage)] + n.v0, sizeof(R4<R>) * n.nv);
-        prefetch_l2(A.cvarea + n.v0, sizeof(double) * n.nv);
+        prefetch_l2(sizeof(R) == 4 ? (const void *)(A.cvarea32 + n.v0) : (const void *)(A.cvarea + n.v0), sizeof(R) * n.nv);
       }
     }
     // phase A: triangles of the block and of its halo
@@ -585,48 +707,15 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_FLUX_MINB32 
       const int4 t = A.bt_nodes[bi.t0 + k];
       const R4<R> p1 = P[t.x], p2 = P[t.y], p3 = P[t.z];
       R dbxx[3], dbyy[3];
-      tri_dxy<R>(A, t, bi.t0 + k, dbxx, dbyy);
+      tri_geom<R>(A, t, bi.t0 + k, dbxx, dbyy);
       TriSmem<R> ts;
-#pragma unroll
-      for (int q = 0; q < 4; q++) {
-        const R a1 = comp(p1, q), a2 = comp(p2, q), a3 = comp(p3, q);
-        ts.dxt[q] = a1 * dbxx[0] + a2 * dbxx[1] + a3 * dbxx[2];
-        ts.dyt[q] = a1 * dbyy[0] + a2 * dbyy[1] + a3 * dbyy[2];
-      }
+      tri_sums<R>(p1, p2, p3, dbxx, dbyy, ts);
       s_tri[k] = ts;
       if (visc && k < bi.nt) {
-        // tri_visc (green_gauss.f:132-194)
-        const R n2b3 = R(2) / R(3);
-        const R en1 = p1.w / p1.x, en2 = p2.w / p2.x, en3 = p3.w / p3.x;
-        const R ext = en1 * dbxx[0] + en2 * dbxx[1] + en3 * dbxx[2];
-        const R eyt = en1 * dbyy[0] + en2 * dbyy[1] + en3 * dbyy[2];
-        const R um = (p1.y + p2.y + p3.y) / R(3);
-        const R vm = (p1.z + p2.z + p3.z) / R(3);
-        const int nbuf = ctl.nphase;
-        const R mut = (A.mu[t.x] + A.mu[t.y] + A.mu[t.z]) / R(3);
-        const R mult = (A.mul[t.x] + A.mul[t.y] + A.mul[t.z]) / R(3);
-        const R prim5t = (A.nut[nbuf][t.x] + A.nut[nbuf][t.y] + A.nut[nbuf][t.z]) / R(3);
-        const R rhot = (p1.x + p2.x + p3.x) / R(3);
-        const R chi = prim5t * rhot / mult;
-        const R chi3 = cube(chi);
-        const R fv1 = chi3 / (chi3 + R(mc.cv11));
-        const R txx = n2b3 * mut * (R(2) * ts.dxt[1] - ts.dyt[2]);
-        const R txy = mut * (ts.dyt[1] + ts.dxt[2]);
-        const R tyy = n2b3 * mut * (R(2) * ts.dyt[2] - ts.dxt[1]);
-        const R gpr = R(mc.gamma) * (mult / R(mc.prandtl) + rhot * prim5t * fv1 / R(mc.prandtl_turb)) /
-                      R(mc.gamma1);
-        const R efx = txx * um + txy * vm + gpr * ext;
-        const R efy = txy * um + tyy * vm + gpr * eyt;
-        R areat;
-        if constexpr (sizeof(R) == 4) areat = A.tri_g32[bi.t0 + k].areat;
-        else areat = 0.25 / A.elarea[t.w];
+        const TriVisc<R> tv = tri_visc<R>(A, mc, ctl.nphase, t, bi.t0 + k, p1, p2, p3, dbxx, dbyy, ts);
         R *sv = s_vis + 9 * k;
 #pragma unroll
-        for (int j = 0; j < 3; j++) {
-          sv[3 * j + 0] = (txx * dbxx[j] + txy * dbyy[j]) * areat;
-          sv[3 * j + 1] = (txy * dbxx[j] + tyy * dbyy[j]) * areat;
-          sv[3 * j + 2] = (efx * dbxx[j] + efy * dbyy[j]) * areat;
-        }
+        for (int j = 0; j < 3; j++) tri_visc_term<R>(tv, dbxx[j], dbyy[j], sv + 3 * j);
       }
     }
     __syncthreads();
@@ -656,7 +745,7 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_FLUX_MINB32 
           rv[2] = rv[2] + sv[2];
         }
       }
-      const R ais = R(A.ais[v]);
+      const R ais = v_ais(A, v);
       Grad<R> g;
 #pragma unroll
       for (int q = 0; q < 4; q++) {
@@ -667,7 +756,7 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_FLUX_MINB32 
       A.grad[v] = g;
       if (visc) dtv = A.dt[v];
       else if (stage == 1) {
-        dtv = time_step<R>(mc, P[v], R(0), A.drmin[v]);
+        dtv = time_step<R>(mc, P[v], R(0), v_drmin(A, v));
         A.dt[v] = dtv;
       } else {
         dtv = A.dt[v];
@@ -684,7 +773,7 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_FLUX_MINB32 
           qy[q] = qy[q] + ts.dyt[q];
         }
       }
-      const R ais = R(A.ais[A.halo_ids[bi.h0 + h]]);
+      const R ais = v_ais(A, A.halo_ids[bi.h0 + h]);
       Grad<R> g;
 #pragma unroll
       for (int q = 0; q < 4; q++) {
@@ -814,7 +903,7 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_FLUX_MINB32 
       const R4<R> po = A.st[old_buf(p, stage)][v];
       const R4<R> pc = P[v];
       const bool noslip = visc && (A.vflag[v] & kVtxSolid);
-      const R4<R> pn = rk_update<R>(mc, stage, po, pc, dtv, A.cvarea[v], acc, noslip);
+      const R4<R> pn = rk_update<R>(mc, stage, po, pc, dtv, v_cvarea(A, v), acc, noslip);
       A.st[out_buf(p, stage)][v] = pn;
       if (stage == 3) {
         const double gra = double(pn.x) - double(po.x);
@@ -910,7 +999,7 @@ __global__ void __launch_bounds__(kBlockVerts) k_sa(ArenaPtrs<R> A, int stage, i
       const R prim5t = (n1 + n2 + n3) / R(3);
       const R rhot = (r1 + r2 + r3) / R(3);
       const R mutb = mult / rhot + prim5t;
-      const R cs1 = R(mc.cb2sig1), cs2 = R(mc.cb2sig2);
+      const R cs1 = MCR(R, cb2sig1), cs2 = MCR(R, cb2sig2);
       s_t[3 * k + 0] = (cs1 * mutb - cs2 * (mul1 / r1 + n1)) * (nux * dbxx[0] + nuy * dbyy[0]) * areat;
       s_t[3 * k + 1] = (cs1 * mutb - cs2 * (mul2 / r2 + n2)) * (nux * dbxx[1] + nuy * dbyy[1]) * areat;
       s_t[3 * k + 2] = (cs1 * mutb - cs2 * (mul3 / r3 + n3)) * (nux * dbxx[2] + nuy * dbyy[2]) * areat;
@@ -941,8 +1030,8 @@ __global__ void __launch_bounds__(kBlockVerts) k_sa(ArenaPtrs<R> A, int stage, i
           f1 = un * nut[b.x];
           f2 = un * nut[b.y];
         } else {
-          f1 = un * R(mc.nut_inf);
-          f2 = un * R(mc.nut_inf);
+          f1 = un * MCR(R, nut_inf);
+          f2 = un * MCR(R, nut_inf);
         }
         f1 = R(0.5) * f1;
         f2 = R(0.5) * f2;
@@ -1161,7 +1250,7 @@ __global__ void __launch_bounds__(kBlockVerts) k_update(ArenaPtrs<R> A, int irk)
     const R4<R> r4 = A.res[v];
     const R res[4] = {r4.x, r4.y, r4.z, r4.w};
     const bool noslip = (mc.iflow != 1) && (A.vflag[v] & kVtxSolid);
-    A.st[p][v] = rk_update<R>(mc, irk, A.st[(p + 2) % 3][v], A.st[p][v], A.dt[v], A.cvarea[v],
+    A.st[p][v] = rk_update<R>(mc, irk, A.st[(p + 2) % 3][v], A.st[p][v], A.dt[v], v_cvarea(A, v),
                               res, noslip);
   }
 }
@@ -1174,7 +1263,7 @@ __global__ void __launch_bounds__(kBlockVerts) k_time_step(ArenaPtrs<R> A) {
     if (threadIdx.x >= bi.nv) continue;
     const MeshCtl &ctl = A.ctl[bi.mesh];
     const int v = bi.v0 + threadIdx.x;
-    A.dt[v] = time_step<R>(A.mc[bi.mesh], A.st[ctl.phase][v], A.mu[v], A.drmin[v]);
+    A.dt[v] = time_step<R>(A.mc[bi.mesh], A.st[ctl.phase][v], A.mu[v], v_drmin(A, v));
   }
 }
 

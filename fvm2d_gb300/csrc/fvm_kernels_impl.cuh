@@ -39,6 +39,10 @@ inline int fit_grid(const LaunchCfg &c, K kern, size_t smem) {
                           int routine) {                                                   \
     size_t sm = smem_grad(c, (R *)nullptr);                                                \
     if (sm > kMaxSmem) return cudaErrorInvalidConfiguration;                              \
+    if (c.grad_vertex) {                                                                   \
+      k_grad_v<R><<<fit_grid(c, k_grad_v<R>, 0), kBlockVerts, 0, c.stream>>>(A, stage, do_dt, routine); \
+      return cudaGetLastError();                                                           \
+    }                                                                                      \
     k_grad<R><<<fit_grid(c, k_grad<R>, sm), kBlockVerts, sm, c.stream>>>(A, stage, do_dt, routine, c.max_tri);  \
     return cudaGetLastError();                                                             \
   }                                                                                        \

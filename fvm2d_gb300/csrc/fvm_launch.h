@@ -20,6 +20,7 @@ struct LaunchCfg {
   int max_loc;       // max own + halo vertices of a block
   int sms;           // multiprocessors of the device
   bool fit;          // grid = CTAs resident at once (occupancy x sms), capped by grid
+  bool grad_vertex;  // gradient pass in its per-vertex form (k_grad_v)
   cudaStream_t stream;
 };
 

@@ -276,6 +276,10 @@ typedef struct fvm_batch_caps {
                                    (recomputes halo gradients in shared
                                    memory); 0 (default): separate passes    */
   int64_t halo_entries, halo_incidence;
+  int32_t grad_vertex;          /* 1: gradient pass walks each vertex's
+                                   triangles itself (no shared memory);
+                                   0 (default): triangles staged per block  */
+  int32_t reserved;
 } fvm_batch_caps;
 
 int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *caps,
