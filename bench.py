@@ -216,7 +216,8 @@ def run_gpu(args):
     achieved = alg_flux / flux_avg_s / 1e9
     peak, peak_kind = measured_peaks()
     tr = profile_traffic()
-    roofline = {"bound": "hbm", "kernel": "k_flux<float> (recon + Roe flux + gather + RK stage)",
+    roofline = {"bound": "hbm", "kernel": f"k_flux<float, {FLUX_CODES[args.flux]}> (recon + "
+                f"{args.flux} flux + gather + RK stage)",
                 "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} hbm_gbs",
                 "traffic": (round(tr * V, 0) if tr is not None else None),
@@ -224,6 +225,16 @@ def run_gpu(args):
                 "avg_launch_ms": round(flux_avg_s * 1e3, 4),
                 "kernel_ms_share": {k: round(v[0] / max(sum(x[0] for x in kt.values()), 1e-9), 4)
                                     for k, v in kt.items() if v[1]}}
+
+    # the whole stage (gradient pass + flux pass + monitor) against the
+    # per-vertex-stage byte model
+    stage_bytes = sum(bytes_per_vertex_stage(m.np, m.nt, m.ne) * m.np for m in meshes)
+    stage_gbs = stage_bytes * 3 * args.steps / (ms_local / 1e3) / 1e9
+    stage_roofline = {"bound": "hbm", "achieved": round(stage_gbs, 1), "peak": peak,
+                      "unit": "GB/s", "frac": round(stage_gbs / peak, 4),
+                      "algorithmic_bytes_per_stage": round(stage_bytes, 0),
+                      "what": "P(36s + 19g/3) + 12T + E(8 + 2g) bytes per stage over the "
+                              "device time of whole iterations"}
 
     # ---- e2e through the C ABI with host buffers -----------------------------
     import numpy as np
@@ -325,7 +336,8 @@ def run_gpu(args):
                                  f"~{bytes_per_vertex_stage(P, T, E) * V / 1e9:.2f} GB "
                                  "touched per stage > 129 MB L2); no flush",
                            "parallelism": f"replicas x{size} (no data-path collective)"},
-                "roofline": roofline, "e2e": e2e, "clocks": clk.summary(),
+                "roofline": roofline, "stage_roofline": stage_roofline, "e2e": e2e,
+                "clocks": clk.summary(),
                 "gpu_launches": launches, "all_solves_ok": ok,
                 "bytes_per_vertex_stage": round(bytes_per_vertex_stage(P, T, E), 1)}
         line.update(extra)

@@ -66,7 +66,7 @@ class FvmBatchCaps(C.Structure):
                 ("solid_edges", C.c_int64), ("max_slots", C.c_int32), ("max_tri", C.c_int32),
                 ("grid", C.c_int32), ("max_tri2", C.c_int32), ("max_loc", C.c_int32),
                 ("fused", C.c_int32), ("halo_entries", C.c_int64),
-                ("halo_incidence", C.c_int64), ("grad_vertex", C.c_int32),
+                ("halo_incidence", C.c_int64), ("grad_mode", C.c_int32),
                 ("reserved", C.c_int32)]
 
 

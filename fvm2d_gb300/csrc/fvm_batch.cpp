@@ -551,7 +551,10 @@ extern "C" int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *cap
     delete b;
     return FVM_ERR_ARG;
   }
-  const int64_t caps[P_COUNT] = {c.vertices, c.blocks, c.edge_entries, c.boundary_entries,
+  // vertex ranges are rounded up to kVertAlign per mesh
+  const int64_t vcap = (c.vertices + kVertAlign - 1) / kVertAlign * kVertAlign +
+                       (int64_t)kVertAlign * c.meshes;
+  const int64_t caps[P_COUNT] = {vcap, c.blocks, c.edge_entries, c.boundary_entries,
                                  c.tri_entries, c.triangles, c.edge_incidence,
                                  c.tri_incidence, c.all_incidence, c.solid_edges,
                                  c.halo_entries, c.halo_entries + c.blocks,
@@ -576,7 +579,7 @@ extern "C" int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *cap
   } while (0)
   TRYB(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
   auto &O = b->owned;
-  const size_t V = (size_t)c.vertices, r = b->rsz;
+  const size_t V = (size_t)b->cap[P_V] + kVertAlign, r = b->rsz;   // with slack
   for (int i = 0; i < 3; i++) TRYB(dalloc(O, (unsigned char **)&b->st[i], 4 * r * V));
   TRYB(dalloc(O, (unsigned char **)&b->grad, 8 * r * V));
   TRYB(dalloc(O, (unsigned char **)&b->resv, 4 * r * V));
@@ -597,7 +600,7 @@ extern "C" int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *cap
   TRYB(dalloc(O, &b->vt_rng, V));
   TRYB(dalloc(O, &b->va_rng, V));
   TRYB(dalloc(O, &b->ve_list, (size_t)c.edge_incidence));
-  TRYB(dalloc(O, &b->vt_list, (size_t)c.tri_incidence));
+  TRYB(dalloc(O, &b->vt_list, (size_t)c.tri_incidence + 16));   // slack: 16-byte copies
   TRYB(dalloc(O, &b->va_list, (size_t)c.all_incidence));
   TRYB(dalloc(O, &b->blocks, (size_t)c.blocks));
   TRYB(dalloc(O, &b->part, (size_t)c.blocks));
@@ -640,7 +643,14 @@ extern "C" int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *cap
   b->cfg.max_tri2 = c.max_tri2;
   b->cfg.max_loc = c.max_loc;
   b->fused = c.fused > 0;
-  b->cfg.grad_vertex = c.grad_vertex > 0;
+  // gradient pass: bulk-copy staging by default in FP32 (when its shared
+  // memory fits), per-thread loads in FP64
+  const bool bulk_fits = grad_bulk_layout(c.max_tri, c.viscous != 0).total <= kMaxSmem;
+  b->cfg.grad_mode = c.grad_mode > 0 ? c.grad_mode
+                                      : (precision == FVM_PREC_FP32 && bulk_fits ? 3 : 1);
+  if (b->cfg.grad_mode < 1 || b->cfg.grad_mode > 3 ||
+      (b->cfg.grad_mode == 3 && (precision != FVM_PREC_FP32 || !bulk_fits)))
+    return fail(FVM_ERR_ARG);
   b->cfg.viscous = c.viscous != 0;
   b->cfg.stream = b->stream;
   int dev = 0, sms = 0;
@@ -798,7 +808,7 @@ extern "C" int32_t fvm_batch_add_prepared(fvm_batch *b, fvm_prepared *prep, int3
   if (Lp.max_slots > b->caps.max_slots || Lp.max_tri > b->caps.max_tri ||
       Lp.max_tri2 > b->caps.max_tri2 || Lp.max_loc > b->caps.max_loc)
     return FVM_ERR_CAPACITY;
-  const int64_t need[P_COUNT] = {Lp.np, Lp.nblk, (int64_t)Lp.be_nodes.size(), (int64_t)Lp.bb_nodes.size(),
+  const int64_t need[P_COUNT] = {(Lp.np + kVertAlign - 1) / kVertAlign * kVertAlign, Lp.nblk, (int64_t)Lp.be_nodes.size(), (int64_t)Lp.bb_nodes.size(),
                                  (int64_t)Lp.bt_nodes.size(), Lp.nt, (int64_t)Lp.ve_list.size(),
                                  (int64_t)Lp.vt_list.size(), (int64_t)Lp.va_list.size(),
                                  (int64_t)Lp.sw_nodes.size(), (int64_t)Lp.halo_ids.size(),
@@ -836,6 +846,7 @@ extern "C" int32_t fvm_batch_add_prepared(fvm_batch *b, fvm_prepared *prep, int3
     bi.e0 += (int)S.off[P_BE];
     bi.b0 += (int)S.off[P_BB];
     bi.t0 += (int)S.off[P_BT];
+    bi.vt0 += (int)S.off[P_VT];
     bi.h0 += (int)S.off[P_HALO];
     bi.hp0 += (int)S.off[P_HP];
     bi.part = (int)S.off[P_BLK] + k;

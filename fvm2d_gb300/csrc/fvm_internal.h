@@ -51,8 +51,42 @@ struct BlockInfo {          // 16 ints, one per CTA
   int nt2;                  // nt + triangles touching only the halo (bt_* from t0)
   int h0, nh;               // halo vertices (halo_ids): local slots [nv, nv+nh)
   int hp0;                  // halo incidence pointers (hl_ptr, nh+1 entries)
-  int pad[2];
+  int vt0, nvt;             // the block's vertex-triangle incidence (vt_list range)
 };
+
+// Vertex ranges of meshes start on multiples of kVertAlign, so per-vertex
+// arrays of 2- to 16-byte elements can be copied block by block in 16-byte
+// units (bulk copies); every per-vertex array has kVertAlign entries of
+// slack at its end for the rounded-up copies.
+constexpr int kVertAlign = 8;
+
+#ifdef __CUDACC__
+#define FVM_HD __host__ __device__
+#else
+#define FVM_HD
+#endif
+
+// Shared memory of the bulk-copy gradient pass (FP32): the block's triangle
+// entries (16 B), their geometry (32 B, overwritten in place by the
+// triangle sums), the viscous terms (9 values), the vertices' incidence
+// ranges and the incidence list (both copied in 16-byte units), and the
+// states of the block's own vertices.
+struct GradBulkLayout {
+  uint32_t bt, geo, vis, vtr, vtl, pv, total;
+};
+FVM_HD inline uint32_t fvm_up16(uint32_t x) { return (x + 15u) & ~15u; }
+FVM_HD inline GradBulkLayout grad_bulk_layout(int max_tri, bool viscous) {
+  GradBulkLayout l;
+  const uint32_t mt = (uint32_t)max_tri;
+  l.bt = 0;
+  l.geo = fvm_up16(mt * 16u);
+  l.vis = l.geo + fvm_up16(mt * 32u);
+  l.vtr = l.vis + (viscous ? fvm_up16(mt * 36u) : 0u);
+  l.vtl = l.vtr + fvm_up16((uint32_t)(kBlockVerts + kVertAlign) * 8u);
+  l.pv = l.vtl + fvm_up16((3u * mt + 16u) * 2u);
+  l.total = l.pv + (uint32_t)kBlockVerts * 16u;
+  return l;
+}
 
 // Per-mesh constants (read-only during a solve).  Mirrors fvm_params plus
 // arena placement.

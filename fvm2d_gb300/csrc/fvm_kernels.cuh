@@ -70,6 +70,53 @@ __device__ __forceinline__ const BlockInfo *next_block(const BlockInfo *blocks, 
 // Viscosity (viscosity.f:2-55) and, at stage 1, the viscous time step
 // (time_step.f:13-20) from the previous mu.  One thread per vertex.
 // ---------------------------------------------------------------------------
+// mbarrier and bulk-copy primitives (sm_90+ PTX) for staging a block's
+// contiguous ranges in shared memory.
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+               : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+// global -> shared bulk copy; addresses 16-byte aligned, bytes a multiple of 16
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes,
+                                         uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// waits for the phase with the given parity; false after about a second
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, parity))
+    if (clock64() - t0 > (1LL << 31)) return false;
+  return true;
+}
+// orders this thread's generic-proxy shared-memory accesses before later
+// async-proxy (bulk copy) writes to the same bytes
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
 // Per-vertex geometry in the kernel's precision (FP32 copies for R = float).
 template <typename R>
 __device__ __forceinline__ R v_ais(const ArenaPtrs<R> &A, int v) {
@@ -168,8 +215,14 @@ struct TriVisc {
 };
 
 template <typename R>
+__device__ __forceinline__ R tri_areat(const ArenaPtrs<R> &A, const int4 &t, int entry) {
+  if constexpr (sizeof(R) == 4) return A.tri_g32[entry].areat;
+  else return 0.25 / A.elarea[t.w];   // green_gauss.f:180
+}
+
+template <typename R>
 __device__ __forceinline__ TriVisc<R> tri_visc(const ArenaPtrs<R> &A, const MeshConst &mc,
-                                               int nbuf, const int4 &t, int entry,
+                                               int nbuf, const int4 &t, R areat,
                                                const R4<R> &p1, const R4<R> &p2,
                                                const R4<R> &p3, const R dbxx[3],
                                                const R dbyy[3], const TriSmem<R> &ts) {
@@ -194,8 +247,7 @@ __device__ __forceinline__ TriVisc<R> tri_visc(const ArenaPtrs<R> &A, const Mesh
                 MCR(R, gamma1);
   o.efx = o.txx * um + o.txy * vm + gpr * ext;
   o.efy = o.txy * um + o.tyy * vm + gpr * eyt;
-  if constexpr (sizeof(R) == 4) o.areat = A.tri_g32[entry].areat;
-  else o.areat = 0.25 / A.elarea[t.w];
+  o.areat = areat;
   return o;
 }
 
@@ -210,7 +262,7 @@ template <typename R>
 __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRAD_MINB32 : 1)
     k_grad(ArenaPtrs<R> A, int stage, int do_dt,
                                                       int routine, int max_tri) {
-  extern __shared__ __align__(32) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   TriSmem<R> *s_tri = reinterpret_cast<TriSmem<R> *>(smem_raw);
   R *s_vis = reinterpret_cast<R *>(s_tri + max_tri);   // [max_tri][3 pos][3 comp]
   const int nwork = *A.nwork;
@@ -243,7 +295,7 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRAD_MINB32 
       tri_sums<R>(p1, p2, p3, dbxx, dbyy, ts);
       s_tri[k] = ts;
       if (visc) {
-        const TriVisc<R> tv = tri_visc<R>(A, mc, ctl.nphase, t, bi.t0 + k, p1, p2, p3, dbxx, dbyy, ts);
+        const TriVisc<R> tv = tri_visc<R>(A, mc, ctl.nphase, t, tri_areat<R>(A, t, bi.t0 + k), p1, p2, p3, dbxx, dbyy, ts);
         R *sv = s_vis + 9 * k;
 #pragma unroll
         for (int j = 0; j < 3; j++) tri_visc_term<R>(tv, dbxx[j], dbyy[j], sv + 3 * j);
@@ -292,6 +344,141 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRAD_MINB32 
       }
     }
     __syncthreads();
+  }
+}
+
+// Gradient pass with the block's contiguous inputs staged by bulk copies
+// (FP32): one thread issues cp.async.bulk copies of the triangle entries,
+// their geometry, the vertices' incidence ranges and the incidence list
+// into shared memory (a few tens of KB in flight per CTA, tracked by one
+// mbarrier); the threads then only gather the three states of each
+// triangle.  Same arithmetic and order as k_grad.  Wait on the copies is
+// bounded: after about a second the mesh gets FVM_ERR_TIMEOUT and the CTA
+// returns.
+template <typename R>
+__global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRAD_MINB32 : 1)
+    k_grad_bulk(ArenaPtrs<R> A, int stage, int do_dt, int routine, int max_tri, int viscous) {
+  if constexpr (sizeof(R) == 4) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t bar;
+    const GradBulkLayout lay = grad_bulk_layout(max_tri, viscous != 0);
+    int4 *s_bt = reinterpret_cast<int4 *>(smem_raw + lay.bt);
+    const TriGeo32 *s_geo = reinterpret_cast<const TriGeo32 *>(smem_raw + lay.geo);
+    TriSmem<R> *s_tri = reinterpret_cast<TriSmem<R> *>(smem_raw + lay.geo);   // in place
+    R *s_vis = reinterpret_cast<R *>(smem_raw + lay.vis);
+    int2 *s_vtr = reinterpret_cast<int2 *>(smem_raw + lay.vtr);
+    uint16_t *s_vtl = reinterpret_cast<uint16_t *>(smem_raw + lay.vtl);
+    R4<R> *s_pv = reinterpret_cast<R4<R> *>(smem_raw + lay.pv);
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    __syncthreads();
+    uint32_t parity = 0;
+    const int nwork = *A.nwork;
+    for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+      const BlockInfo bi = A.blocks[A.work[w]];
+      const MeshCtl &ctl = A.ctl[bi.mesh];
+      if (!routine && !ctl.active) continue;
+      const MeshConst &mc = A.mc[bi.mesh];
+      const bool visc = mc.iflow != 1;
+      const R4<R> *P = A.st[cur_buf(ctl.phase, stage)];
+      const int vt_a = bi.vt0 & ~7;                       // 16-byte units of uint16
+      const int vt_b = (bi.vt0 + bi.nvt + 7) & ~7;
+      if (threadIdx.x == 0) {
+        const uint32_t nbt = 16u * bi.nt, ngeo = 32u * bi.nt;
+        const uint32_t nvtr = 8u * ((bi.nv + 1) & ~1), nvtl = 2u * (vt_b - vt_a);
+        const uint32_t npv = 16u * bi.nv;
+        mbar_expect_tx(&bar, nbt + ngeo + nvtr + nvtl + npv);
+        if (nbt) bulk_g2s(s_bt, A.bt_nodes + bi.t0, nbt, &bar);
+        if (ngeo) bulk_g2s((void *)s_geo, A.tri_g32 + bi.t0, ngeo, &bar);
+        bulk_g2s(s_vtr, A.vt_rng + bi.v0, nvtr, &bar);
+        if (nvtl) bulk_g2s(s_vtl, A.vt_list + vt_a, nvtl, &bar);
+        bulk_g2s(s_pv, P + bi.v0, npv, &bar);
+        const BlockInfo *nb = next_block(A.blocks, A.work, w, nwork);
+        if (nb) {
+          const BlockInfo n = *nb;
+          prefetch_l2(A.bt_nodes + n.t0, sizeof(int4) * n.nt);
+          prefetch_l2(A.tri_g32 + n.t0, sizeof(TriGeo32) * n.nt);
+          prefetch_l2(P + n.v0, sizeof(R4<R>) * n.nv);
+          prefetch_l2(A.vt_rng + n.v0, sizeof(int2) * n.nv);
+          prefetch_l2(A.vt_list + n.vt0, sizeof(uint16_t) * n.nvt);
+          prefetch_l2(A.ais32 + n.v0, sizeof(float) * n.nv);
+        }
+      }
+      const bool late = !mbar_wait_bounded(&bar, parity);
+      parity ^= 1u;
+      if (__syncthreads_or(late)) {
+        if (threadIdx.x == 0) atomicCAS(&A.ctl[bi.mesh].err, 0, 6 /* FVM_ERR_TIMEOUT */);
+        return;
+      }
+      // phase 1: one thread per triangle touching the block
+      auto state = [&](int v) {   // own vertices from shared memory
+        const unsigned l = (unsigned)(v - bi.v0);
+        return l < (unsigned)bi.nv ? s_pv[l] : P[v];
+      };
+      for (int k = threadIdx.x; k < bi.nt; k += blockDim.x) {
+        const int4 t = s_bt[k];
+        const R4<R> p1 = state(t.x), p2 = state(t.y), p3 = state(t.z);
+        const TriGeo32 tg = s_geo[k];
+        R dbxx[3], dbyy[3];
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+          dbxx[j] = tg.dbxx[j];
+          dbyy[j] = tg.dbyy[j];
+        }
+        TriSmem<R> ts;
+        tri_sums<R>(p1, p2, p3, dbxx, dbyy, ts);
+        if (visc) {
+          const TriVisc<R> tv = tri_visc<R>(A, mc, ctl.nphase, t, tg.areat, p1, p2, p3, dbxx, dbyy, ts);
+          R *sv = s_vis + 9 * k;
+#pragma unroll
+          for (int j = 0; j < 3; j++) tri_visc_term<R>(tv, dbxx[j], dbyy[j], sv + 3 * j);
+        }
+        s_tri[k] = ts;   // over this thread's own geometry entry
+      }
+      __syncthreads();
+      // phase 2: one thread per vertex, triangles in original order
+      if (threadIdx.x < bi.nv) {
+        const int v = bi.v0 + threadIdx.x;
+        R qx[4] = {R(0), R(0), R(0), R(0)}, qy[4] = {R(0), R(0), R(0), R(0)};
+        R rv[3] = {R(0), R(0), R(0)};
+        const int2 jr = s_vtr[threadIdx.x];
+        for (int j = jr.x - vt_a; j < jr.y - vt_a; j++) {
+          const uint16_t e = s_vtl[j];
+          const int slot = e & 0x3fff;
+          const TriSmem<R> ts = s_tri[slot];
+#pragma unroll
+          for (int q = 0; q < 4; q++) {
+            qx[q] = qx[q] + ts.dxt[q];
+            qy[q] = qy[q] + ts.dyt[q];
+          }
+          if (visc) {
+            const R *sv = s_vis + 9 * slot + 3 * (e >> kTriPosShift);
+            rv[0] = rv[0] + sv[0];
+            rv[1] = rv[1] + sv[1];
+            rv[2] = rv[2] + sv[2];
+          }
+        }
+        const R ais = v_ais(A, v);
+        Grad<R> g;
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          g.qx[q] = qx[q] * ais;
+          g.qy[q] = qy[q] * ais;
+        }
+        A.grad[v] = g;
+        if (visc) {
+          R4<R> r;
+          r.x = R(0);
+          r.y = rv[0];
+          r.z = rv[1];
+          r.w = rv[2];
+          A.resv[v] = r;
+        } else if (do_dt) {
+          A.dt[v] = time_step<R>(mc, s_pv[threadIdx.x], R(0), v_drmin(A, v));
+        }
+      }
+      fence_proxy_async_smem();   // before the next block's copies land here
+      __syncthreads();
+    }
   }
 }
 
@@ -346,7 +533,7 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRADV_MINB32
       }
       if (visc) {
         const int pos = e >> kTriPosShift;
-        const TriVisc<R> tv = tri_visc<R>(A, mc, ctl.nphase, t, entry, p1, p2, p3, dbxx, dbyy, ts);
+        const TriVisc<R> tv = tri_visc<R>(A, mc, ctl.nphase, t, tri_areat<R>(A, t, entry), p1, p2, p3, dbxx, dbyy, ts);
         R sv[3];
         tri_visc_term<R>(tv, pos == 0 ? dbxx[0] : pos == 1 ? dbxx[1] : dbxx[2],
                          pos == 0 ? dbyy[0] : pos == 1 ? dbyy[1] : dbyy[2], sv);
@@ -459,7 +646,7 @@ __device__ __forceinline__ void edge_flux(const ArenaPtrs<R> &A, const FluxConst
 template <typename R, int FLUX>
 __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_FLUX_MINB32 : 2) k_flux(ArenaPtrs<R> A, int stage, int mode,
                                                       int irk, int routine) {
-  extern __shared__ __align__(32) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   R4<R> *s_flux = reinterpret_cast<R4<R> *>(smem_raw);
   __shared__ double s_red[kBlockVerts / 32];
   __shared__ double s_max[kBlockVerts / 32];
@@ -660,7 +847,7 @@ template <typename R, int FLUX>
 __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_FLUX_MINB32 : 2)
     k_step(ArenaPtrs<R> A, int stage, int max_tri, int max_tri2, int max_slots, int max_loc,
            int viscous) {
-  extern __shared__ __align__(32) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   const size_t tri_bytes = size_t(max_tri2) * sizeof(TriSmem<R>) + (viscous ? size_t(max_tri) * 9 * sizeof(R) : 0);
   const size_t flux_bytes = size_t(max_slots) * sizeof(R4<R>);
   const size_t r1 = ((tri_bytes > flux_bytes ? tri_bytes : flux_bytes) + 63) & ~size_t(63);
@@ -712,7 +899,7 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_FLUX_MINB32 
       tri_sums<R>(p1, p2, p3, dbxx, dbyy, ts);
       s_tri[k] = ts;
       if (visc && k < bi.nt) {
-        const TriVisc<R> tv = tri_visc<R>(A, mc, ctl.nphase, t, bi.t0 + k, p1, p2, p3, dbxx, dbyy, ts);
+        const TriVisc<R> tv = tri_visc<R>(A, mc, ctl.nphase, t, tri_areat<R>(A, t, bi.t0 + k), p1, p2, p3, dbxx, dbyy, ts);
         R *sv = s_vis + 9 * k;
 #pragma unroll
         for (int j = 0; j < 3; j++) tri_visc_term<R>(tv, dbxx[j], dbyy[j], sv + 3 * j);
@@ -963,7 +1150,7 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_FLUX_MINB32 
 template <typename R>
 __global__ void __launch_bounds__(kBlockVerts) k_sa(ArenaPtrs<R> A, int stage, int routine,
                                                     int max_tri) {
-  extern __shared__ __align__(32) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   R *s_t = reinterpret_cast<R *>(smem_raw);   // [max_tri][3]
   R *s_e = s_t + 3 * max_tri;                  // [slots]
   const int nwork = *A.nwork;

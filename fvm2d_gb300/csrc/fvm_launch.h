@@ -20,7 +20,8 @@ struct LaunchCfg {
   int max_loc;       // max own + halo vertices of a block
   int sms;           // multiprocessors of the device
   bool fit;          // grid = CTAs resident at once (occupancy x sms), capped by grid
-  bool grad_vertex;  // gradient pass in its per-vertex form (k_grad_v)
+  int grad_mode;     // gradient pass: 1 loads per thread (k_grad), 2 per vertex
+                     // (k_grad_v), 3 bulk copies to shared memory (k_grad_bulk, FP32)
   cudaStream_t stream;
 };
 

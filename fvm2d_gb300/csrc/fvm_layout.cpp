@@ -331,6 +331,10 @@ int32_t build_layout(const fvm_mesh &m, int bv, MeshLayout &L) {
     L.ve_ptr[v + 1] = L.ve_ptr[v] + (int)(vint[v].size() + vbnd[v].size());
     L.vt_ptr[v + 1] = L.vt_ptr[v] + (int)vtri[v].size();
   }
+  for (BlockInfo &bi : L.blocks) {
+    bi.vt0 = L.vt_ptr[bi.v0];
+    bi.nvt = L.vt_ptr[bi.v0 + bi.nv] - bi.vt0;
+  }
   L.ve_list.reserve(L.ve_ptr[np]);
   L.vt_list.reserve(L.vt_ptr[np]);
   for (int v = 0; v < np; v++) {
@@ -376,6 +380,11 @@ int64_t verify_layout(const MeshLayout &L) {
     }
     for (int h = 1; h < bi.nh; h++)
       if (L.halo_ids[bi.h0 + h] <= L.halo_ids[bi.h0 + h - 1]) bad++;
+    // the bulk-copy gradient pass stages [vt0, vt0 + nvt) in a tile of
+    // 3 * max_tri + 16 entries and the block's vertex ranges from v0
+    if (bi.vt0 != L.vt_ptr[bi.v0] || bi.nvt != L.vt_ptr[bi.v0 + bi.nv] - bi.vt0 ||
+        bi.nvt > 3 * bi.nt || bi.v0 % kBlockVerts != 0)
+      bad++;
     // own vertices: triangles among the block's own, ascending
     for (int v = bi.v0; v < bi.v0 + bi.nv; v++) {
       int last = -1;

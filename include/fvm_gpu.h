@@ -276,9 +276,12 @@ typedef struct fvm_batch_caps {
                                    (recomputes halo gradients in shared
                                    memory); 0 (default): separate passes    */
   int64_t halo_entries, halo_incidence;
-  int32_t grad_vertex;          /* 1: gradient pass walks each vertex's
-                                   triangles itself (no shared memory);
-                                   0 (default): triangles staged per block  */
+  int32_t grad_mode;            /* gradient pass: 1 per-thread loads of the
+                                   block's triangles; 2 each vertex walks its
+                                   triangles itself (no shared memory); 3 the
+                                   block's triangles and incidence staged by
+                                   bulk copies (FP32 only); 0 (default): 3 in
+                                   FP32, 1 in FP64                           */
   int32_t reserved;
 } fvm_batch_caps;
 

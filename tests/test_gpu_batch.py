@@ -173,17 +173,21 @@ def run_variant(fvm_lib, prec, ms, flows, n, viscous=False, **caps):
 @pytest.mark.parametrize("prec", [L.FP64, L.FP32])
 def test_fused_pass_and_grid_give_identical_results(fvm_lib, prec):
     """The fused gradient+flux pass recomputes each halo gradient in the
-    owner's triangle order, the per-vertex gradient pass sums the same
-    triangle terms in the same order, and the grid only changes which CTA
-    takes a block: every variant must give the same bits, Euler and
-    laminar."""
+    owner's triangle order; the three forms of the gradient pass (per-thread
+    loads, per-vertex walks, bulk-copy staging) sum the same triangle terms
+    in the same order; the grid only changes which CTA takes a block: every
+    variant must give the same bits, Euler and laminar."""
     g1, g2 = naca_ogrid(96, 40, jitter=0.1, seed=3), naca_ogrid(64, 24)
     ms = [fvm_lib.build_geometry(g.coord, g.elem, g.ptype) for g in (g1, g2)]
     flows = [dict(mach=0.8, aoa_deg=1.25),
              dict(iflow=L.LAMINAR, mach=0.5, aoa_deg=1.0, rey=5000.0, cfl=0.8)]
     n = 30
     ref = run_variant(fvm_lib, prec, ms, flows, n, viscous=True)
-    for caps in (dict(fused=1), dict(fused=1, grid=7), dict(grid=3), dict(grad_vertex=1)):
+    variants = [dict(fused=1), dict(fused=1, grid=7), dict(grid=3), dict(grad_mode=1),
+                dict(grad_mode=2)]
+    if prec == L.FP32:
+        variants += [dict(grad_mode=3, grid=5)]
+    for caps in variants:
         got = run_variant(fvm_lib, prec, ms, flows, n, viscous=True, **caps)
         for (h, st), (h0, st0) in zip(got, ref):
             np.testing.assert_array_equal(h["fres"], h0["fres"], err_msg=str(caps))
