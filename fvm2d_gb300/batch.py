@@ -177,3 +177,17 @@ class Batch:
 
     def launch_count(self) -> int:
         return int(L.lib().fvm_batch_launch_count(self.h))
+
+    TUNE_CANDIDATES = ("bulk", "loads", "vertex", "fused")
+
+    def tune(self, iters: int = 10) -> dict:
+        """Time each form of the iteration on the resident solves (ordinary
+        iterations: every form gives the same bits) and keep the fastest.
+        Returns {"choice": name, "ms_per_iter": {name: ms or None}}."""
+        n = len(self.TUNE_CANDIDATES)
+        ms = (C.c_double * n)()
+        ch = C.c_int32(-1)
+        check(L.lib().fvm_batch_tune(self.h, int(iters), n, ms, C.byref(ch)), "fvm_batch_tune")
+        return {"choice": self.TUNE_CANDIDATES[ch.value],
+                "ms_per_iter": {k: (float(ms[i]) if ms[i] > 0 else None)
+                                for i, k in enumerate(self.TUNE_CANDIDATES)}}

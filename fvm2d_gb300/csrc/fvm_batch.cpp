@@ -1096,6 +1096,66 @@ extern "C" int32_t fvm_batch_step(fvm_batch *b, int32_t niter) {
   return FVM_OK;
 }
 
+extern "C" int32_t fvm_batch_tune(fvm_batch *b, int32_t iters, int32_t max, double *ms_per_iter,
+                                  int32_t *choice) {
+  if (!b || iters < 1 || max < 0 || (max > 0 && !ms_per_iter)) return FVM_ERR_ARG;
+  struct Cand {
+    bool fused;
+    int grad;
+  };
+  const Cand cands[4] = {{false, 3}, {false, 1}, {false, 2}, {true, 1}};
+  const bool fp32 = b->prec == FVM_PREC_FP32;
+  const bool bulk_ok = fp32 && grad_bulk_layout(b->caps.max_tri, b->caps.viscous != 0).total <= kMaxSmem;
+  const size_t step_smem = fp32 ? smem_step(b->cfg, (float *)nullptr) : smem_step(b->cfg, (double *)nullptr);
+  const bool fused_ok = step_smem <= kMaxSmem;
+  for (int i = 0; i < max; i++) ms_per_iter[i] = 0.0;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  FVM_TRY(b, cudaEventCreate(&e0));
+  cudaError_t ce = cudaEventCreate(&e1);
+  if (ce != cudaSuccess) {
+    cudaEventDestroy(e0);
+    FVM_TRY(b, ce);
+  }
+  int best = -1;
+  double best_ms = 0.0;
+  int32_t st = FVM_OK;
+  for (int i = 0; i < 4 && st == FVM_OK; i++) {
+    if ((i == 0 && !bulk_ok) || (i == 3 && !fused_ok)) continue;
+    b->fused = cands[i].fused;
+    b->cfg.grad_mode = cands[i].grad;
+    if (b->graph) {
+      cudaGraphExecDestroy(b->graph);
+      b->graph = nullptr;
+    }
+    if ((st = fvm_batch_step(b, 1))) break;   // capture + one untimed iteration
+    cudaError_t e = cudaEventRecord(e0, b->stream);
+    if (e == cudaSuccess) st = fvm_batch_step(b, iters);
+    if (e == cudaSuccess && st == FVM_OK) e = cudaEventRecord(e1, b->stream);
+    if (e == cudaSuccess && st == FVM_OK) e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess && st == FVM_OK) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e != cudaSuccess) st = cuda_status(b, e);
+    if (st) break;
+    const double per = (double)ms / iters;
+    if (i < max) ms_per_iter[i] = per;
+    if (best < 0 || per < best_ms) {
+      best = i;
+      best_ms = per;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (best < 0) best = bulk_ok ? 0 : 1;
+  b->fused = cands[best].fused;
+  b->cfg.grad_mode = cands[best].grad;
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  if (choice) *choice = best;
+  return st;
+}
+
 extern "C" int32_t fvm_batch_sync(fvm_batch *b) {
   if (!b) return FVM_ERR_ARG;
   FVM_TRY(b, cudaStreamSynchronize(b->stream));

@@ -343,6 +343,18 @@ int32_t fvm_batch_timing_read(fvm_batch *b, int32_t max, char *names,
 /* Launches of this library's kernels since the batch was created. */
 int64_t fvm_batch_launch_count(fvm_batch *b);
 
+/* Autotuner (no counterpart in the reference): runs `iters` timed
+ * iterations of the resident solves under each form of the iteration (the
+ * gradient pass staged by bulk copies, by per-thread loads or walked per
+ * vertex; or the fused gradient+flux pass) and keeps the fastest.  Every
+ * form gives the same bits, so the tuning iterations are ordinary
+ * iterations of the solves (they count toward each solve's iterations).
+ * ms_per_iter[i] (i < max) receives candidate i's device time per
+ * iteration (0 for a candidate that does not fit), *choice the candidate
+ * kept: 0 bulk, 1 loads, 2 per vertex, 3 fused. */
+int32_t fvm_batch_tune(fvm_batch *b, int32_t iters, int32_t max, double *ms_per_iter,
+                       int32_t *choice);
+
 /* Layout statistics of a mesh after renumbering (no GPU needed):
  * out[0] blocks, [1] interior edge entries (cut edges counted in both
  * blocks), [2] triangle entries (block and halo), [3] max slots of a

@@ -193,3 +193,33 @@ def test_fused_pass_and_grid_give_identical_results(fvm_lib, prec):
             np.testing.assert_array_equal(h["fres"], h0["fres"], err_msg=str(caps))
             np.testing.assert_array_equal(h["cl"], h0["cl"], err_msg=str(caps))
             np.testing.assert_array_equal(st["prim"], st0["prim"], err_msg=str(caps))
+
+
+@pytest.mark.parametrize("prec", [L.FP64, L.FP32])
+def test_autotuner_changes_no_result(fvm_lib, prec):
+    """The tuner times each form of the iteration on the resident solves;
+    its iterations are ordinary iterations, so a tuned solve equals an
+    untuned one bit for bit."""
+    from fvm2d_gb300.batch import Batch
+    g1, g2 = naca_ogrid(96, 40, jitter=0.1, seed=3), naca_ogrid(64, 24)
+    ms = [fvm_lib.build_geometry(g.coord, g.elem, g.ptype) for g in (g1, g2)]
+    flows = [dict(mach=0.8, aoa_deg=1.25),
+             dict(iflow=L.LAMINAR, mach=0.5, aoa_deg=1.0, rey=5000.0, cfl=0.8)]
+    n = 40
+    ref = run_variant(fvm_lib, prec, ms, flows, n, viscous=True)
+    b = Batch(prec, vertices=sum(m.np for m in ms), meshes=2, viscous=True)
+    slots = [b.add(fvm_lib.make_params(precision=prec, **f), m) for m, f in zip(ms, flows)]
+    for s in slots:
+        b.start(s, n)
+    t = b.tune(iters=3)
+    assert t["choice"] in Batch.TUNE_CANDIDATES
+    timed = [k for k, v in t["ms_per_iter"].items() if v is not None]
+    assert t["choice"] in timed and len(timed) >= 3
+    assert ("bulk" in timed) == (prec == L.FP32)
+    b.step(n)
+    for s, (h0, st0) in zip(slots, ref):
+        p = b.poll(s)
+        assert p["niter"] == n and p["status"] == 0
+        np.testing.assert_array_equal(b.history(s, 0, n)["fres"], h0["fres"])
+        np.testing.assert_array_equal(b.get_state(s)["prim"], st0["prim"])
+    b.close()
