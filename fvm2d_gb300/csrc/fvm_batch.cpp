@@ -120,7 +120,9 @@ struct fvm_batch {
   uint32_t *be_loc = nullptr;
   int *halo_ids = nullptr, *hl_ptr = nullptr;
   uint16_t *hl_list = nullptr;
-  bool fused = false;
+  bool fused = false;          // the fused pass runs (wanted and fits)
+  bool fused_wanted = false;   // asked for by the caps or chosen by the tuner
+  bool fused_fits = true;      // resident halo tiles within max_tri2 / max_loc
   MeshConst *mc = nullptr;
   MeshCtl *ctl = nullptr;
   BlockPartial *part = nullptr;
@@ -415,6 +417,11 @@ int32_t update_work(fvm_batch *b) {
     changed |= t != *cur[i];
     *cur[i] = t;
   }
+  // the fused pass needs every resident block's halo within its tiles
+  b->fused_fits = tile[2] <= cap[2] && tile[3] <= cap[3];
+  const bool use_fused = b->fused_wanted && b->fused_fits;
+  changed |= use_fused != b->fused;
+  b->fused = use_fused;
   if (changed && b->graph) {            // different kernels or tiles: re-capture
     cudaGraphExecDestroy(b->graph);
     b->graph = nullptr;
@@ -517,8 +524,8 @@ void default_caps(fvm_batch_caps &c) {
   if (!c.tri_incidence) c.tri_incidence = 7 * V + 1024 * M;
   if (!c.all_incidence) c.all_incidence = 7 * V + 1024 * M;
   if (!c.solid_edges) c.solid_edges = V / 8 + 256 * M;
-  if (!c.max_slots) c.max_slots = 1152;
-  if (!c.max_tri) c.max_tri = 896;
+  if (!c.max_slots) c.max_slots = 1280;
+  if (!c.max_tri) c.max_tri = 1024;
   if (!c.max_tri2) c.max_tri2 = 1280;
   if (!c.max_loc) c.max_loc = 576;
   if (!c.halo_entries) c.halo_entries = V / 2 + 1024 * M;
@@ -642,7 +649,7 @@ extern "C" int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *cap
   b->cfg.max_tri = c.max_tri;
   b->cfg.max_tri2 = c.max_tri2;
   b->cfg.max_loc = c.max_loc;
-  b->fused = c.fused > 0;
+  b->fused = b->fused_wanted = c.fused > 0;
   // gradient pass: bulk-copy staging by default in FP32 (when its shared
   // memory fits), per-thread loads in FP64
   const bool bulk_fits = grad_bulk_layout(c.max_tri, c.viscous != 0).total <= kMaxSmem;
@@ -805,9 +812,9 @@ extern "C" int32_t fvm_batch_add_prepared(fvm_batch *b, fvm_prepared *prep, int3
     }
   if (sid < 0) return FVM_ERR_CAPACITY;
   const MeshLayout &Lp = prep->L;
-  if (Lp.max_slots > b->caps.max_slots || Lp.max_tri > b->caps.max_tri ||
-      Lp.max_tri2 > b->caps.max_tri2 || Lp.max_loc > b->caps.max_loc)
-    return FVM_ERR_CAPACITY;
+  // (a mesh whose halo tiles exceed max_tri2 / max_loc is admitted; the
+  // fused pass is then off while it is resident)
+  if (Lp.max_slots > b->caps.max_slots || Lp.max_tri > b->caps.max_tri) return FVM_ERR_CAPACITY;
   const int64_t need[P_COUNT] = {(Lp.np + kVertAlign - 1) / kVertAlign * kVertAlign, Lp.nblk, (int64_t)Lp.be_nodes.size(), (int64_t)Lp.bb_nodes.size(),
                                  (int64_t)Lp.bt_nodes.size(), Lp.nt, (int64_t)Lp.ve_list.size(),
                                  (int64_t)Lp.vt_list.size(), (int64_t)Lp.va_list.size(),
@@ -1107,7 +1114,7 @@ extern "C" int32_t fvm_batch_tune(fvm_batch *b, int32_t iters, int32_t max, doub
   const bool fp32 = b->prec == FVM_PREC_FP32;
   const bool bulk_ok = fp32 && grad_bulk_layout(b->caps.max_tri, b->caps.viscous != 0).total <= kMaxSmem;
   const size_t step_smem = fp32 ? smem_step(b->cfg, (float *)nullptr) : smem_step(b->cfg, (double *)nullptr);
-  const bool fused_ok = step_smem <= kMaxSmem;
+  const bool fused_ok = step_smem <= kMaxSmem && b->fused_fits;
   for (int i = 0; i < max; i++) ms_per_iter[i] = 0.0;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   FVM_TRY(b, cudaEventCreate(&e0));
@@ -1121,7 +1128,7 @@ extern "C" int32_t fvm_batch_tune(fvm_batch *b, int32_t iters, int32_t max, doub
   int32_t st = FVM_OK;
   for (int i = 0; i < 4 && st == FVM_OK; i++) {
     if ((i == 0 && !bulk_ok) || (i == 3 && !fused_ok)) continue;
-    b->fused = cands[i].fused;
+    b->fused = b->fused_wanted = cands[i].fused;
     b->cfg.grad_mode = cands[i].grad;
     if (b->graph) {
       cudaGraphExecDestroy(b->graph);
@@ -1146,7 +1153,7 @@ extern "C" int32_t fvm_batch_tune(fvm_batch *b, int32_t iters, int32_t max, doub
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (best < 0) best = bulk_ok ? 0 : 1;
-  b->fused = cands[best].fused;
+  b->fused = b->fused_wanted = cands[best].fused;
   b->cfg.grad_mode = cands[best].grad;
   if (b->graph) {
     cudaGraphExecDestroy(b->graph);

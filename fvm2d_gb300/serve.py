@@ -63,6 +63,10 @@ class Result:
     cd: float = math.nan
     status: int = 0
     converged: bool = False
+    cl_tail: float = math.nan   # mean cl, cd over the last TAIL iterations
+    cd_tail: float = math.nan
+
+    TAIL = 256
 
     @property
     def latency(self) -> float:
@@ -155,10 +159,18 @@ class Server:
                 req, prep = ready[0]
                 slot = b.add_prepared(prep)
                 if slot is None:
-                    if not resident:
-                        raise RuntimeError(f"request {req.rid} ({req.npts} vertices) "
-                                           "does not fit an empty arena")
-                    break
+                    if resident:
+                        break                              # waits for room
+                    # too large for an empty arena: refused with a status
+                    ready.popleft()
+                    prep.release()
+                    r = results[req.rid]
+                    r.admitted = r.finished = time.perf_counter() - t0
+                    r.status = L.ERR_CAPACITY
+                    done += 1
+                    if log:
+                        log(r)
+                    continue
                 ready.popleft()
                 b.start(slot, self.max_iter, self.minres)
                 resident[slot] = req
@@ -183,6 +195,10 @@ class Server:
                 r.niter, r.fres, r.cl, r.cd, r.status = (p["niter"], p["fres"], p["cl"],
                                                          p["cd"], p["status"])
                 r.converged = p["status"] == 0 and p["fres"] <= self.minres
+                if r.niter > 0:
+                    k = min(Result.TAIL, r.niter)
+                    h = b.history(slot, r.niter - k, k)
+                    r.cl_tail, r.cd_tail = float(np.mean(h["cl"])), float(np.mean(h["cd"]))
                 b.remove(slot)
                 done += 1
                 if log:

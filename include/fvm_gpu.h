@@ -274,7 +274,9 @@ typedef struct fvm_batch_caps {
   int32_t max_loc;              /* own + halo vertices of a block            */
   int32_t fused;                /* 1: one fused gradient+flux pass per stage
                                    (recomputes halo gradients in shared
-                                   memory); 0 (default): separate passes    */
+                                   memory) while every resident mesh's halo
+                                   tiles fit max_tri2 / max_loc; 0
+                                   (default): separate passes               */
   int64_t halo_entries, halo_incidence;
   int32_t grad_mode;            /* gradient pass: 1 per-thread loads of the
                                    block's triangles; 2 each vertex walks its

@@ -41,3 +41,14 @@ def test_prepared_refused_then_admitted(fvm_lib):
     assert b.add_prepared(p1) is None        # no room: p1 stays with the caller
     b.remove(s0)
     assert b.add_prepared(p1) is not None    # and is admitted once room frees
+
+
+def test_request_larger_than_the_arena_is_refused_with_a_status(fvm_lib):
+    from fvm2d_gb300 import serve
+    reqs = serve.generate_requests(n=3, rate=100.0, seed=5, pmin=2000, pmax=2000)
+    reqs[1].npts = 40000                        # cannot fit a 12k-vertex arena
+    srv = serve.Server(vertices=12000, meshes=2, chunk=10, workers=2, max_iter=20, minres=1e-6)
+    res, stats = srv.run(reqs)
+    srv.close()
+    assert [r.status for r in res] == [0, L.ERR_CAPACITY, 0]
+    assert stats["completed_ok"] == 2 and len(stats["failures"]) == 1
