@@ -67,7 +67,7 @@ class FvmBatchCaps(C.Structure):
                 ("grid", C.c_int32), ("max_tri2", C.c_int32), ("max_loc", C.c_int32),
                 ("fused", C.c_int32), ("halo_entries", C.c_int64),
                 ("halo_incidence", C.c_int64), ("grad_mode", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("overlap", C.c_int32)]
 
 
 # every function the header declares, with its signature

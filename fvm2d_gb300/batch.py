@@ -178,7 +178,7 @@ class Batch:
     def launch_count(self) -> int:
         return int(L.lib().fvm_batch_launch_count(self.h))
 
-    TUNE_CANDIDATES = ("bulk", "loads", "vertex", "fused")
+    TUNE_CANDIDATES = ("bulk", "loads", "vertex", "fused", "split+overlap", "fused+overlap")
 
     def tune(self, iters: int = 10) -> dict:
         """Time each form of the iteration on the resident solves (ordinary

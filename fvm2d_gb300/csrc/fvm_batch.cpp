@@ -96,6 +96,9 @@ struct fvm_batch {
   RangeAlloc pool[P_COUNT];
   std::vector<Slot> slots;
   cudaStream_t stream = nullptr;
+  cudaStream_t stream2 = nullptr;          // second chain of the overlapped iteration
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  bool overlap = false;                    // two chains over the halves of the meshes
   std::vector<void *> owned;
   // device arrays
   void *st[3] = {nullptr, nullptr, nullptr};
@@ -123,6 +126,7 @@ struct fvm_batch {
   bool fused = false;          // the fused pass runs (wanted and fits)
   bool fused_wanted = false;   // asked for by the caps or chosen by the tuner
   bool fused_fits = true;      // resident halo tiles within max_tri2 / max_loc
+  bool run_sa = false;         // a turbulent mesh is resident
   MeshConst *mc = nullptr;
   MeshCtl *ctl = nullptr;
   BlockPartial *part = nullptr;
@@ -225,6 +229,7 @@ ArenaPtrs<R> ptrs(const fvm_batch *b) {
   A.h_iresi = b->h_iresi;
   A.work = b->work;
   A.nwork = b->nwork;
+  A.wpart = 0;
   A.nslots = (int)b->slots.size();
   return A;
 }
@@ -388,10 +393,11 @@ cudaError_t put_range(fvm_batch *b, T *base, int64_t off, const std::vector<T> &
 }
 
 int32_t update_work(fvm_batch *b) {
-  std::vector<int> work;
+  std::vector<int> work, mesh_first;
   int flux = -1;
   for (const Slot &s : b->slots)
     if (s.used) {
+      mesh_first.push_back((int)work.size());
       for (int k = 0; k < s.L.nblk; k++) work.push_back((int)(s.off[P_BLK] + k));
       flux = (flux == -1 || flux == s.par.iflux) ? s.par.iflux : 0;
     }
@@ -400,8 +406,11 @@ int32_t update_work(fvm_batch *b) {
   // small changes of the mix keep the graph), never above the arena's
   // capacities: smaller tiles let more CTAs share an SM.
   int tile[4] = {0, 0, 0, 0};
+  bool any_visc = false, any_turb = false;
   for (const Slot &s : b->slots)
     if (s.used) {
+      any_visc |= s.par.iflow != FVM_INVISCID;
+      any_turb |= s.par.iflow == FVM_TURBULENT;
       tile[0] = std::max(tile[0], s.L.max_tri);
       tile[1] = std::max(tile[1], s.L.max_slots);
       tile[2] = std::max(tile[2], s.L.max_tri2);
@@ -417,6 +426,12 @@ int32_t update_work(fvm_batch *b) {
     changed |= t != *cur[i];
     *cur[i] = t;
   }
+  // kernels for viscous terms and the SA model only while such meshes are
+  // resident (the shared memory of viscous terms likewise)
+  const bool visc_now = b->caps.viscous != 0 && any_visc;
+  changed |= visc_now != b->cfg.viscous || any_turb != b->run_sa;
+  b->cfg.viscous = visc_now;
+  b->run_sa = any_turb;
   // the fused pass needs every resident block's halo within its tiles
   b->fused_fits = tile[2] <= cap[2] && tile[3] <= cap[3];
   const bool use_fused = b->fused_wanted && b->fused_fits;
@@ -427,8 +442,13 @@ int32_t update_work(fvm_batch *b) {
     b->graph = nullptr;
   }
   const int n = (int)work.size();
+  // split of the work list at the mesh boundary nearest its middle
+  int split = 0;
+  for (int x : mesh_first)
+    if (std::abs(2 * x - n) < std::abs(2 * split - n)) split = x;
+  const int head[2] = {n, split};
   if (n) FVM_TRY(b, cudaMemcpyAsync(b->work, work.data(), n * sizeof(int), cudaMemcpyHostToDevice, b->stream));
-  FVM_TRY(b, cudaMemcpyAsync(b->nwork, &n, sizeof(int), cudaMemcpyHostToDevice, b->stream));
+  FVM_TRY(b, cudaMemcpyAsync(b->nwork, head, sizeof(head), cudaMemcpyHostToDevice, b->stream));
   FVM_TRY(b, cudaStreamSynchronize(b->stream));
   return FVM_OK;
 }
@@ -438,53 +458,80 @@ template <typename R>
 int32_t enqueue_iteration(fvm_batch *b, bool with_events) {
   const ArenaPtrs<R> A = ptrs<R>(b);
   const LaunchCfg &c = b->cfg;
-  const bool visc = b->caps.viscous != 0;
+  const bool visc = c.viscous;   // a viscous mesh is resident
   int k = 0;
-  auto mark = [&](int kind) -> cudaError_t {
+  // per-kernel timing events, recorded on the kernel's own stream
+  auto mark = [&](int kind, cudaStream_t st) -> cudaError_t {
     if (!with_events) return cudaSuccess;
     if ((size_t)(2 * k + 1) >= b->ev.size()) return cudaErrorInvalidValue;
     b->ev_kind[k] = kind;
-    return cudaEventRecordWithFlags(b->ev[2 * k], b->stream, cudaEventRecordExternal);
+    return cudaEventRecordWithFlags(b->ev[2 * k], st, cudaEventRecordExternal);
   };
-  auto done = [&]() -> cudaError_t {
+  auto done = [&](cudaStream_t st) -> cudaError_t {
     if (!with_events) {
       k++;
       return cudaSuccess;
     }
-    cudaError_t e = cudaEventRecordWithFlags(b->ev[2 * k + 1], b->stream, cudaEventRecordExternal);
+    cudaError_t e = cudaEventRecordWithFlags(b->ev[2 * k + 1], st, cudaEventRecordExternal);
     k++;
     return e;
   };
-  for (int s = 1; s <= 3; s++) {
-    if (visc) {
-      FVM_TRY(b, mark(K_VISC));
-      FVM_TRY(b, launch_visc(A, c, s, s == 1, 0));
-      FVM_TRY(b, done());
+  // the three RK stages of the blocks of one part of the work list; with
+  // fork set, an event after the first gradient pass lets the other part
+  // start then, so the two parts' passes overlap on the device
+  auto stages = [&](const ArenaPtrs<R> &Ap, const LaunchCfg &cp, cudaEvent_t fork) -> int32_t {
+    cudaStream_t st = cp.stream;
+    for (int s = 1; s <= 3; s++) {
+      if (visc) {
+        FVM_TRY(b, mark(K_VISC, st));
+        FVM_TRY(b, launch_visc(Ap, cp, s, s == 1, 0));
+        FVM_TRY(b, done(st));
+      }
+      if (b->fused) {
+        // one pass: gradients (own + halo), fluxes, RK stage; inviscid
+        // meshes take their time step in the stage-1 pass
+        FVM_TRY(b, mark(K_STEP, st));
+        FVM_TRY(b, launch_step(Ap, cp, s));
+        FVM_TRY(b, done(st));
+      } else {
+        FVM_TRY(b, mark(K_GRAD, st));
+        // inviscid meshes take their time step in the stage-1 gradient pass
+        FVM_TRY(b, launch_grad(Ap, cp, s, s == 1 ? 1 : 0, 0));
+        FVM_TRY(b, done(st));
+        if (s == 1 && fork) FVM_TRY(b, cudaEventRecord(fork, st));
+        FVM_TRY(b, mark(K_FLUX, st));
+        FVM_TRY(b, launch_flux(Ap, cp, s, 1 /*MODE_UPDATE*/, s, 0));
+        FVM_TRY(b, done(st));
+      }
+      if (s == 1 && fork && b->fused) FVM_TRY(b, cudaEventRecord(fork, st));
     }
-    if (b->fused) {
-      // one pass: gradients (own + halo), fluxes, RK stage; inviscid
-      // meshes take their time step in the stage-1 pass
-      FVM_TRY(b, mark(K_STEP));
-      FVM_TRY(b, launch_step(A, c, s));
-      FVM_TRY(b, done());
-      continue;
-    }
-    FVM_TRY(b, mark(K_GRAD));
-    // inviscid meshes take their time step in the stage-1 gradient pass
-    FVM_TRY(b, launch_grad(A, c, s, s == 1 ? 1 : 0, 0));
-    FVM_TRY(b, done());
-    FVM_TRY(b, mark(K_FLUX));
-    FVM_TRY(b, launch_flux(A, c, s, 1 /*MODE_UPDATE*/, s, 0));
-    FVM_TRY(b, done());
+    return FVM_OK;
+  };
+  if (b->overlap) {
+    // two independent chains over the meshes before / from the split
+    ArenaPtrs<R> A1 = A, A2 = A;
+    A1.wpart = 1;
+    A2.wpart = 2;
+    LaunchCfg c2 = c;
+    c2.stream = b->stream2;
+    int32_t st = stages(A1, c, b->ev_fork);
+    if (st) return st;
+    FVM_TRY(b, cudaStreamWaitEvent(b->stream2, b->ev_fork, 0));
+    if ((st = stages(A2, c2, nullptr))) return st;
+    FVM_TRY(b, cudaEventRecord(b->ev_join, b->stream2));
+    FVM_TRY(b, cudaStreamWaitEvent(b->stream, b->ev_join, 0));
+  } else {
+    int32_t st = stages(A, c, nullptr);
+    if (st) return st;
   }
-  if (visc) {
-    FVM_TRY(b, mark(K_SA));
+  if (b->run_sa) {
+    FVM_TRY(b, mark(K_SA, b->stream));
     FVM_TRY(b, launch_sa(A, c, 3, 0));
-    FVM_TRY(b, done());
+    FVM_TRY(b, done(b->stream));
   }
-  FVM_TRY(b, mark(K_MON));
+  FVM_TRY(b, mark(K_MON, b->stream));
   FVM_TRY(b, launch_monitor(A, c, b->prec == FVM_PREC_FP64 ? 1 : 0));
-  FVM_TRY(b, done());
+  FVM_TRY(b, done(b->stream));
   b->kernels_per_iter = k;
   return FVM_OK;
 }
@@ -585,6 +632,9 @@ extern "C" int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *cap
     if (_e != cudaSuccess) return fail(cuda_status(b, _e));  \
   } while (0)
   TRYB(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+  TRYB(cudaStreamCreateWithFlags(&b->stream2, cudaStreamNonBlocking));
+  TRYB(cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming));
+  TRYB(cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming));
   auto &O = b->owned;
   const size_t V = (size_t)b->cap[P_V] + kVertAlign, r = b->rsz;   // with slack
   for (int i = 0; i < 3; i++) TRYB(dalloc(O, (unsigned char **)&b->st[i], 4 * r * V));
@@ -612,7 +662,7 @@ extern "C" int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *cap
   TRYB(dalloc(O, &b->blocks, (size_t)c.blocks));
   TRYB(dalloc(O, &b->part, (size_t)c.blocks));
   TRYB(dalloc(O, &b->work, (size_t)c.blocks));
-  TRYB(dalloc(O, &b->nwork, 1));
+  TRYB(dalloc(O, &b->nwork, 2));
   TRYB(dalloc(O, &b->be_nodes, (size_t)c.edge_entries));
   TRYB(dalloc(O, &b->be_loc, (size_t)c.edge_entries));
   TRYB(dalloc(O, &b->halo_ids, (size_t)b->cap[P_HALO]));
@@ -640,7 +690,7 @@ extern "C" int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *cap
   TRYB(dalloc(O, &b->h_cd, H));
   TRYB(dalloc(O, &b->h_iresi, H));
   TRYB(cudaMemsetAsync(b->ctl, 0, sizeof(MeshCtl) * c.meshes, b->stream));
-  TRYB(cudaMemsetAsync(b->nwork, 0, sizeof(int), b->stream));
+  TRYB(cudaMemsetAsync(b->nwork, 0, 2 * sizeof(int), b->stream));
   TRYB(cudaMemsetAsync(b->grad, 0, 8 * r * V, b->stream));
   TRYB(cudaMemsetAsync(b->resv, 0, 4 * r * V, b->stream));
   TRYB(cudaStreamSynchronize(b->stream));
@@ -650,6 +700,7 @@ extern "C" int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *cap
   b->cfg.max_tri2 = c.max_tri2;
   b->cfg.max_loc = c.max_loc;
   b->fused = b->fused_wanted = c.fused > 0;
+  b->overlap = c.overlap > 0;
   // gradient pass: bulk-copy staging by default in FP32 (when its shared
   // memory fits), per-thread loads in FP64
   const bool bulk_fits = grad_bulk_layout(c.max_tri, c.viscous != 0).total <= kMaxSmem;
@@ -682,6 +733,9 @@ extern "C" int32_t fvm_batch_destroy(fvm_batch *b) {
   for (void *p : b->owned) cudaFree(p);
   if (b->pinned) cudaFreeHost(b->pinned);
   if (b->stream) cudaStreamDestroy(b->stream);
+  if (b->stream2) cudaStreamDestroy(b->stream2);
+  if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+  if (b->ev_join) cudaEventDestroy(b->ev_join);
   delete b;
   return FVM_OK;
 }
@@ -1109,8 +1163,14 @@ extern "C" int32_t fvm_batch_tune(fvm_batch *b, int32_t iters, int32_t max, doub
   struct Cand {
     bool fused;
     int grad;
+    bool overlap;
   };
-  const Cand cands[4] = {{false, 3}, {false, 1}, {false, 2}, {true, 1}};
+  constexpr int kCands = 6;
+  const bool fp32_ = b->prec == FVM_PREC_FP32;
+  const bool bulk_ok_ = fp32_ && grad_bulk_layout(b->caps.max_tri, b->caps.viscous != 0).total <= kMaxSmem;
+  const Cand cands[kCands] = {{false, 3, false}, {false, 1, false}, {false, 2, false},
+                              {true, 1, false},  {false, bulk_ok_ ? 3 : 1, true},
+                              {true, 1, true}};
   const bool fp32 = b->prec == FVM_PREC_FP32;
   const bool bulk_ok = fp32 && grad_bulk_layout(b->caps.max_tri, b->caps.viscous != 0).total <= kMaxSmem;
   const size_t step_smem = fp32 ? smem_step(b->cfg, (float *)nullptr) : smem_step(b->cfg, (double *)nullptr);
@@ -1126,10 +1186,11 @@ extern "C" int32_t fvm_batch_tune(fvm_batch *b, int32_t iters, int32_t max, doub
   int best = -1;
   double best_ms = 0.0;
   int32_t st = FVM_OK;
-  for (int i = 0; i < 4 && st == FVM_OK; i++) {
-    if ((i == 0 && !bulk_ok) || (i == 3 && !fused_ok)) continue;
+  for (int i = 0; i < kCands && st == FVM_OK; i++) {
+    if ((cands[i].grad == 3 && !bulk_ok) || (cands[i].fused && !fused_ok)) continue;
     b->fused = b->fused_wanted = cands[i].fused;
     b->cfg.grad_mode = cands[i].grad;
+    b->overlap = cands[i].overlap;
     if (b->graph) {
       cudaGraphExecDestroy(b->graph);
       b->graph = nullptr;
@@ -1155,6 +1216,7 @@ extern "C" int32_t fvm_batch_tune(fvm_batch *b, int32_t iters, int32_t max, doub
   if (best < 0) best = bulk_ok ? 0 : 1;
   b->fused = b->fused_wanted = cands[best].fused;
   b->cfg.grad_mode = cands[best].grad;
+  b->overlap = cands[best].overlap;
   if (b->graph) {
     cudaGraphExecDestroy(b->graph);
     b->graph = nullptr;
@@ -1232,7 +1294,7 @@ extern "C" int32_t fvm_batch_timing(fvm_batch *b, int32_t on) {
   if (want == b->timing) return FVM_OK;
   FVM_TRY(b, cudaStreamSynchronize(b->stream));
   if (want && b->ev.empty()) {
-    const int pairs = 16;
+    const int pairs = 32;
     b->ev.resize(2 * pairs);
     b->ev_kind.assign(pairs, 0);
     for (auto &e : b->ev) FVM_TRY(b, cudaEventCreate(&e));

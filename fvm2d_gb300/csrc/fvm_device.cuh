@@ -22,9 +22,11 @@ __device__ __forceinline__ float msqrt(float x) { return sqrtf(x); }
 __device__ __forceinline__ double msqrt(double x) { return sqrt(x); }
 __device__ __forceinline__ float merf(float x) { return erff(x); }
 __device__ __forceinline__ double merf(double x) { return erf(x); }
-__device__ __forceinline__ float mexp(float x) { return expf(x); }
+// FP32: the fast hardware approximations (a few ulp), like the approximate
+// division and square root of the FP32 build
+__device__ __forceinline__ float mexp(float x) { return __expf(x); }
 __device__ __forceinline__ double mexp(double x) { return exp(x); }
-__device__ __forceinline__ float mpow(float x, float y) { return powf(x, y); }
+__device__ __forceinline__ float mpow(float x, float y) { return __powf(x, y); }
 __device__ __forceinline__ double mpow(double x, double y) { return pow(x, y); }
 __device__ __forceinline__ float mfabs(float x) { return fabsf(x); }
 __device__ __forceinline__ double mfabs(double x) { return fabs(x); }

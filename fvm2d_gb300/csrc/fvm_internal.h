@@ -231,7 +231,8 @@ struct ArenaPtrs {
   int *h_iresi;
   // block work list (indices into blocks[]) and its length
   const int *work;
-  const int *nwork;
+  const int *nwork;    // [0] blocks in the work list, [1] split (a mesh boundary)
+  int wpart;           // 0 whole list, 1 before the split, 2 from it
   int nslots;             // mesh slots (monitor grid)
 };
 

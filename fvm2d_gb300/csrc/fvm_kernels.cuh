@@ -60,6 +60,15 @@ __device__ __forceinline__ void prefetch_l2(const void *p, size_t bytes) {
 }
 
 // The next block this CTA will process (persistent loop), for prefetching.
+// The blocks a launch covers: the whole work list (part 0), or the part of
+// it before (1) or from (2) the split, a mesh boundary.
+template <typename R>
+__device__ __forceinline__ void work_range(const ArenaPtrs<R> &A, int &w0, int &w1) {
+  const int n = A.nwork[0], s = A.nwork[1];
+  w0 = A.wpart == 2 ? s : 0;
+  w1 = A.wpart == 1 ? s : n;
+}
+
 __device__ __forceinline__ const BlockInfo *next_block(const BlockInfo *blocks, const int *work,
                                                        int w, int nwork) {
   const int nw = w + gridDim.x;
@@ -137,8 +146,9 @@ __device__ __forceinline__ R v_drmin(const ArenaPtrs<R> &A, int v) {
 template <typename R>
 __global__ void __launch_bounds__(kBlockVerts) k_visc(ArenaPtrs<R> A, int stage, int do_dt,
                                                       int routine) {
-  const int nwork = *A.nwork;
-  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+  int w0, nwork;
+  work_range(A, w0, nwork);
+  for (int w = w0 + blockIdx.x; w < nwork; w += gridDim.x) {
     const BlockInfo bi = A.blocks[A.work[w]];
     const MeshCtl &ctl = A.ctl[bi.mesh];
     if (!routine && !ctl.active) continue;
@@ -265,8 +275,9 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRAD_MINB32 
   extern __shared__ __align__(128) unsigned char smem_raw[];
   TriSmem<R> *s_tri = reinterpret_cast<TriSmem<R> *>(smem_raw);
   R *s_vis = reinterpret_cast<R *>(s_tri + max_tri);   // [max_tri][3 pos][3 comp]
-  const int nwork = *A.nwork;
-  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+  int w0, nwork;
+  work_range(A, w0, nwork);
+  for (int w = w0 + blockIdx.x; w < nwork; w += gridDim.x) {
     const BlockInfo bi = A.blocks[A.work[w]];
     const MeshCtl &ctl = A.ctl[bi.mesh];
     if (!routine && !ctl.active) continue;
@@ -372,8 +383,9 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRAD_MINB32 
     if (threadIdx.x == 0) mbar_init(&bar, 1);
     __syncthreads();
     uint32_t parity = 0;
-    const int nwork = *A.nwork;
-    for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+    int w0, nwork;
+  work_range(A, w0, nwork);
+    for (int w = w0 + blockIdx.x; w < nwork; w += gridDim.x) {
       const BlockInfo bi = A.blocks[A.work[w]];
       const MeshCtl &ctl = A.ctl[bi.mesh];
       if (!routine && !ctl.active) continue;
@@ -490,8 +502,9 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRAD_MINB32 
 template <typename R>
 __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRADV_MINB32 : 1)
     k_grad_v(ArenaPtrs<R> A, int stage, int do_dt, int routine) {
-  const int nwork = *A.nwork;
-  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+  int w0, nwork;
+  work_range(A, w0, nwork);
+  for (int w = w0 + blockIdx.x; w < nwork; w += gridDim.x) {
     const BlockInfo bi = A.blocks[A.work[w]];
     const MeshCtl &ctl = A.ctl[bi.mesh];
     if (!routine && !ctl.active) continue;
@@ -651,8 +664,9 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_FLUX_MINB32 
   __shared__ double s_red[kBlockVerts / 32];
   __shared__ double s_max[kBlockVerts / 32];
   __shared__ int s_arg[kBlockVerts / 32];
-  const int nwork = *A.nwork;
-  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+  int w0, nwork;
+  work_range(A, w0, nwork);
+  for (int w = w0 + blockIdx.x; w < nwork; w += gridDim.x) {
     const BlockInfo bi = A.blocks[A.work[w]];
     MeshCtl &ctl = A.ctl[bi.mesh];
     if (!routine && !ctl.active) continue;
@@ -858,8 +872,9 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_FLUX_MINB32 
   __shared__ double s_red[kBlockVerts / 32];
   __shared__ double s_max[kBlockVerts / 32];
   __shared__ int s_arg[kBlockVerts / 32];
-  const int nwork = *A.nwork;
-  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+  int w0, nwork;
+  work_range(A, w0, nwork);
+  for (int w = w0 + blockIdx.x; w < nwork; w += gridDim.x) {
     const BlockInfo bi = A.blocks[A.work[w]];
     MeshCtl &ctl = A.ctl[bi.mesh];
     if (!ctl.active) continue;
@@ -1153,8 +1168,9 @@ __global__ void __launch_bounds__(kBlockVerts) k_sa(ArenaPtrs<R> A, int stage, i
   extern __shared__ __align__(128) unsigned char smem_raw[];
   R *s_t = reinterpret_cast<R *>(smem_raw);   // [max_tri][3]
   R *s_e = s_t + 3 * max_tri;                  // [slots]
-  const int nwork = *A.nwork;
-  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+  int w0, nwork;
+  work_range(A, w0, nwork);
+  for (int w = w0 + blockIdx.x; w < nwork; w += gridDim.x) {
     const BlockInfo bi = A.blocks[A.work[w]];
     MeshCtl &ctl = A.ctl[bi.mesh];
     if (!routine && !ctl.active) continue;
@@ -1426,8 +1442,9 @@ __global__ void __launch_bounds__(256) k_monitor(ArenaPtrs<R> A, int serial_clcd
 // ---------------------------------------------------------------------------
 template <typename R>
 __global__ void __launch_bounds__(kBlockVerts) k_update(ArenaPtrs<R> A, int irk) {
-  const int nwork = *A.nwork;
-  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+  int w0, nwork;
+  work_range(A, w0, nwork);
+  for (int w = w0 + blockIdx.x; w < nwork; w += gridDim.x) {
     const BlockInfo bi = A.blocks[A.work[w]];
     if (threadIdx.x >= bi.nv) continue;
     const MeshCtl &ctl = A.ctl[bi.mesh];
@@ -1444,8 +1461,9 @@ __global__ void __launch_bounds__(kBlockVerts) k_update(ArenaPtrs<R> A, int irk)
 
 template <typename R>
 __global__ void __launch_bounds__(kBlockVerts) k_time_step(ArenaPtrs<R> A) {
-  const int nwork = *A.nwork;
-  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+  int w0, nwork;
+  work_range(A, w0, nwork);
+  for (int w = w0 + blockIdx.x; w < nwork; w += gridDim.x) {
     const BlockInfo bi = A.blocks[A.work[w]];
     if (threadIdx.x >= bi.nv) continue;
     const MeshCtl &ctl = A.ctl[bi.mesh];
@@ -1456,8 +1474,9 @@ __global__ void __launch_bounds__(kBlockVerts) k_time_step(ArenaPtrs<R> A) {
 
 template <typename R>
 __global__ void __launch_bounds__(kBlockVerts) k_positivity(ArenaPtrs<R> A) {
-  const int nwork = *A.nwork;
-  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+  int w0, nwork;
+  work_range(A, w0, nwork);
+  for (int w = w0 + blockIdx.x; w < nwork; w += gridDim.x) {
     const BlockInfo bi = A.blocks[A.work[w]];
     if (threadIdx.x >= bi.nv) continue;
     MeshCtl &ctl = A.ctl[bi.mesh];
@@ -1473,8 +1492,9 @@ template <typename R>
 __global__ void __launch_bounds__(kBlockVerts) k_conres_part(ArenaPtrs<R> A) {
   __shared__ double s_red[kBlockVerts / 32], s_max[kBlockVerts / 32];
   __shared__ int s_arg[kBlockVerts / 32];
-  const int nwork = *A.nwork;
-  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+  int w0, nwork;
+  work_range(A, w0, nwork);
+  for (int w = w0 + blockIdx.x; w < nwork; w += gridDim.x) {
     const BlockInfo bi = A.blocks[A.work[w]];
     const MeshCtl &ctl = A.ctl[bi.mesh];
     double d2 = 0.0, dabs = 0.0;
@@ -1561,8 +1581,9 @@ __global__ void __launch_bounds__(256) k_routine_monitor(ArenaPtrs<R> A, int mes
 // all of its edges in edge order.
 template <typename R>
 __global__ void __launch_bounds__(kBlockVerts) k_limitgrad(ArenaPtrs<R> A) {
-  const int nwork = *A.nwork;
-  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+  int w0, nwork;
+  work_range(A, w0, nwork);
+  for (int w = w0 + blockIdx.x; w < nwork; w += gridDim.x) {
     const BlockInfo bi = A.blocks[A.work[w]];
     if (threadIdx.x >= bi.nv) continue;
     const MeshCtl &ctl = A.ctl[bi.mesh];

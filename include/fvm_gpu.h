@@ -284,7 +284,11 @@ typedef struct fvm_batch_caps {
                                    block's triangles and incidence staged by
                                    bulk copies (FP32 only); 0 (default): 3 in
                                    FP32, 1 in FP64                           */
-  int32_t reserved;
+  int32_t overlap;              /* 1: the meshes before and after the middle
+                                   of the work list run as two chains of
+                                   kernels on two streams, so one part's
+                                   gradient pass overlaps the other's flux
+                                   pass; 0 (default): one chain             */
 } fvm_batch_caps;
 
 int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *caps,
@@ -348,12 +352,14 @@ int64_t fvm_batch_launch_count(fvm_batch *b);
 /* Autotuner (no counterpart in the reference): runs `iters` timed
  * iterations of the resident solves under each form of the iteration (the
  * gradient pass staged by bulk copies, by per-thread loads or walked per
- * vertex; or the fused gradient+flux pass) and keeps the fastest.  Every
+ * vertex; or the fused gradient+flux pass; in one chain of kernels or
+ * two overlapped ones) and keeps the fastest.  Every
  * form gives the same bits, so the tuning iterations are ordinary
  * iterations of the solves (they count toward each solve's iterations).
  * ms_per_iter[i] (i < max) receives candidate i's device time per
  * iteration (0 for a candidate that does not fit), *choice the candidate
- * kept: 0 bulk, 1 loads, 2 per vertex, 3 fused. */
+ * kept: 0 bulk, 1 loads, 2 per vertex, 3 fused, 4 bulk (FP32) or loads
+ * (FP64) with the two overlapped chains, 5 fused with the two chains. */
 int32_t fvm_batch_tune(fvm_batch *b, int32_t iters, int32_t max, double *ms_per_iter,
                        int32_t *choice);
 
