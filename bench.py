@@ -204,7 +204,11 @@ def run_gpu(args):
     ms_local = e0.elapsed_time(e1)
     ms = replicas.max_over_ranks(ms_local)
     # per-kernel CUDA events over a second pass of the same steps (reading
-    # them needs a host sync after every iteration, kept out of `value`)
+    # them needs a host sync after every iteration, kept out of `value`);
+    # kernels one at a time (no overlapped chains), so each launch's time
+    # is its own
+    alone = {"split+overlap": "bulk", "fused+overlap": "fused"}.get(b.form, b.form)
+    b.set_form(alone)
     b.timing(True)
     b.step(1)
     b.sync()
@@ -213,6 +217,7 @@ def run_gpu(args):
     b.sync()
     kt = b.timing_read()
     b.timing(False)
+    b.set_form(tuned["choice"])
     units = replicas.sum_over_ranks(V * 3 * args.steps)
     value = units / (ms / 1e3)
     polls = [b.poll(s) for s in slots]
@@ -241,8 +246,9 @@ def run_gpu(args):
                 "traffic": (round(tr * V, 0) if tr is not None else None),
                 "algorithmic_bytes_per_launch": alg_flux,
                 "avg_launch_ms": round(flux_avg_s * 1e3, 4),
-                "events": f"CUDA events around every launch on its stream, over a second pass "
-                          f"of {args.steps} steps ({flux_n} launches)",
+                "events": f"CUDA events around every launch, over a second pass of "
+                          f"{args.steps} steps ({flux_n} launches) in form '{alone}' (one "
+                          "kernel at a time)",
                 "kernel_ms_share": {k: round(v[0] / max(sum(x[0] for x in kt.values()), 1e-9), 4)
                                     for k, v in kt.items() if v[1]}}
 
@@ -511,7 +517,8 @@ def run_serve(args):
     torch.cuda.init()
     reqs = serve.generate_requests(n=args.requests, rate=args.rate, seed=args.seed)
     srv = serve.Server(vertices=args.arena_vertices, meshes=512, chunk=args.chunk,
-                       workers=args.workers, max_iter=args.max_iter, minres=args.minres)
+                       workers=args.workers, max_iter=args.max_iter, minres=args.minres,
+                       tune_every=args.tune_every)
     res, stats = srv.run(reqs)
     srv.close()
     acc = fp64_accuracy(reqs, res)
@@ -525,7 +532,8 @@ def run_serve(args):
             "config": {"workload": f"{args.requests} NACA 4-digit requests, Poisson {args.rate}/s, "
                                    "5k-400k vertices log-uniform, 70% Euler / 30% laminar, "
                                    f"stop at drop {args.minres} or {args.max_iter} iterations",
-                       "arena_vertices": args.arena_vertices, "chunk": args.chunk},
+                       "arena_vertices": args.arena_vertices, "chunk": args.chunk,
+                       "tune_every_steps": args.tune_every},
             "latency_s": {"p50": stats["p50_latency_s"], "p99": stats["p99_latency_s"]},
             "stats": stats,
             "vs_fp64_gpu": {"solves_per_s": solves64, "ratio": stats["solves_per_s"] / solves64,
@@ -607,6 +615,8 @@ def main():
     ap.add_argument("--workers", type=int, default=8)
     ap.add_argument("--max-iter", type=int, default=5000)
     ap.add_argument("--minres", type=float, default=1e-6)
+    ap.add_argument("--tune-every", type=int, default=40,
+                    help="serving: re-run the autotuner every N steps (0: never)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

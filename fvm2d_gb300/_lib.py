@@ -119,6 +119,7 @@ SIGNATURES = {
                                           C.POINTER(C.c_int64), _pi]),
     "fvm_batch_launch_count": (C.c_int64, [C.c_void_p]),
     "fvm_batch_tune": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, _pd, _pi]),
+    "fvm_batch_set_form": (C.c_int32, [C.c_void_p, C.c_int32]),
     "fvm_layout_stats": (C.c_int32, [C.POINTER(FvmMesh), C.POINTER(C.c_int64)]),
     "fvm_gpu_conres_noalloc": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, _pd,
                                            _pd, _pd, _pi]),

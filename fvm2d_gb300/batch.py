@@ -67,6 +67,13 @@ class Batch:
         self.h = h
         self.precision = precision
         self._meshes = {}
+        gm = int(caps.get("grad_mode", 0)) or (3 if precision == L.FP32 else 1)
+        if int(caps.get("fused", 0)) > 0:
+            self.form = "fused+overlap" if int(caps.get("overlap", 0)) > 0 else "fused"
+        elif int(caps.get("overlap", 0)) > 0:
+            self.form = "split+overlap"
+        else:
+            self.form = {3: "bulk", 1: "loads", 2: "vertex"}[gm]
 
     def close(self):
         if getattr(self, "h", None) is not None and self.h.value:
@@ -180,6 +187,12 @@ class Batch:
 
     TUNE_CANDIDATES = ("bulk", "loads", "vertex", "fused", "split+overlap", "fused+overlap")
 
+    def set_form(self, name: str):
+        """Set the form of the iteration to one of TUNE_CANDIDATES."""
+        check(L.lib().fvm_batch_set_form(self.h, self.TUNE_CANDIDATES.index(name)),
+              "fvm_batch_set_form")
+        self.form = name
+
     def tune(self, iters: int = 10) -> dict:
         """Time each form of the iteration on the resident solves (ordinary
         iterations: every form gives the same bits) and keep the fastest.
@@ -188,6 +201,7 @@ class Batch:
         ms = (C.c_double * n)()
         ch = C.c_int32(-1)
         check(L.lib().fvm_batch_tune(self.h, int(iters), n, ms, C.byref(ch)), "fvm_batch_tune")
+        self.form = self.TUNE_CANDIDATES[ch.value]
         return {"choice": self.TUNE_CANDIDATES[ch.value],
                 "ms_per_iter": {k: (float(ms[i]) if ms[i] > 0 else None)
                                 for i, k in enumerate(self.TUNE_CANDIDATES)}}

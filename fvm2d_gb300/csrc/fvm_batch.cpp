@@ -1157,24 +1157,54 @@ extern "C" int32_t fvm_batch_step(fvm_batch *b, int32_t niter) {
   return FVM_OK;
 }
 
+// Forms of the iteration the tuner chooses from (fvm_batch_tune codes).
+struct Form {
+  bool fused;
+  int grad;
+  bool overlap;
+};
+constexpr int kForms = 6;
+
+static Form form_of(const fvm_batch *b, int i) {
+  const bool bulk = b->prec == FVM_PREC_FP32 &&
+                    grad_bulk_layout(b->caps.max_tri, b->caps.viscous != 0).total <= kMaxSmem;
+  const Form f[kForms] = {{false, 3, false}, {false, 1, false}, {false, 2, false},
+                          {true, 1, false},  {false, bulk ? 3 : 1, true}, {true, 1, true}};
+  return f[i];
+}
+
+static bool form_fits(const fvm_batch *b, const Form &f) {
+  const bool fp32 = b->prec == FVM_PREC_FP32;
+  if (f.grad == 3 && !(fp32 && grad_bulk_layout(b->caps.max_tri, b->caps.viscous != 0).total <= kMaxSmem))
+    return false;
+  if (f.fused) {
+    const size_t sm = fp32 ? smem_step(b->cfg, (float *)nullptr) : smem_step(b->cfg, (double *)nullptr);
+    if (sm > kMaxSmem || !b->fused_fits) return false;
+  }
+  return true;
+}
+
+static void apply_form(fvm_batch *b, const Form &f) {
+  b->fused = b->fused_wanted = f.fused;
+  b->cfg.grad_mode = f.grad;
+  b->overlap = f.overlap;
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+}
+
+extern "C" int32_t fvm_batch_set_form(fvm_batch *b, int32_t form) {
+  if (!b || form < 0 || form >= kForms) return FVM_ERR_ARG;
+  const Form f = form_of(b, form);
+  if (!form_fits(b, f)) return FVM_ERR_ARG;
+  apply_form(b, f);
+  return FVM_OK;
+}
+
 extern "C" int32_t fvm_batch_tune(fvm_batch *b, int32_t iters, int32_t max, double *ms_per_iter,
                                   int32_t *choice) {
   if (!b || iters < 1 || max < 0 || (max > 0 && !ms_per_iter)) return FVM_ERR_ARG;
-  struct Cand {
-    bool fused;
-    int grad;
-    bool overlap;
-  };
-  constexpr int kCands = 6;
-  const bool fp32_ = b->prec == FVM_PREC_FP32;
-  const bool bulk_ok_ = fp32_ && grad_bulk_layout(b->caps.max_tri, b->caps.viscous != 0).total <= kMaxSmem;
-  const Cand cands[kCands] = {{false, 3, false}, {false, 1, false}, {false, 2, false},
-                              {true, 1, false},  {false, bulk_ok_ ? 3 : 1, true},
-                              {true, 1, true}};
-  const bool fp32 = b->prec == FVM_PREC_FP32;
-  const bool bulk_ok = fp32 && grad_bulk_layout(b->caps.max_tri, b->caps.viscous != 0).total <= kMaxSmem;
-  const size_t step_smem = fp32 ? smem_step(b->cfg, (float *)nullptr) : smem_step(b->cfg, (double *)nullptr);
-  const bool fused_ok = step_smem <= kMaxSmem && b->fused_fits;
   for (int i = 0; i < max; i++) ms_per_iter[i] = 0.0;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   FVM_TRY(b, cudaEventCreate(&e0));
@@ -1186,15 +1216,10 @@ extern "C" int32_t fvm_batch_tune(fvm_batch *b, int32_t iters, int32_t max, doub
   int best = -1;
   double best_ms = 0.0;
   int32_t st = FVM_OK;
-  for (int i = 0; i < kCands && st == FVM_OK; i++) {
-    if ((cands[i].grad == 3 && !bulk_ok) || (cands[i].fused && !fused_ok)) continue;
-    b->fused = b->fused_wanted = cands[i].fused;
-    b->cfg.grad_mode = cands[i].grad;
-    b->overlap = cands[i].overlap;
-    if (b->graph) {
-      cudaGraphExecDestroy(b->graph);
-      b->graph = nullptr;
-    }
+  for (int i = 0; i < kForms && st == FVM_OK; i++) {
+    const Form f = form_of(b, i);
+    if (!form_fits(b, f)) continue;
+    apply_form(b, f);
     if ((st = fvm_batch_step(b, 1))) break;   // capture + one untimed iteration
     cudaError_t e = cudaEventRecord(e0, b->stream);
     if (e == cudaSuccess) st = fvm_batch_step(b, iters);
@@ -1213,14 +1238,8 @@ extern "C" int32_t fvm_batch_tune(fvm_batch *b, int32_t iters, int32_t max, doub
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  if (best < 0) best = bulk_ok ? 0 : 1;
-  b->fused = b->fused_wanted = cands[best].fused;
-  b->cfg.grad_mode = cands[best].grad;
-  b->overlap = cands[best].overlap;
-  if (b->graph) {
-    cudaGraphExecDestroy(b->graph);
-    b->graph = nullptr;
-  }
+  if (best < 0) best = form_fits(b, form_of(b, 0)) ? 0 : 1;
+  apply_form(b, form_of(b, best));
   if (choice) *choice = best;
   return st;
 }

@@ -122,10 +122,16 @@ def prepare(req: Request, precision: int) -> Prepared:
 
 class Server:
     def __init__(self, vertices: int = 6_000_000, meshes: int = 256, precision: int = L.FP32,
-                 chunk: int = 50, workers: int = 8, max_iter: int = 5000, minres: float = 1e-6):
-        self.batch = Batch(precision, vertices=vertices, meshes=meshes, viscous=True)
+                 chunk: int = 50, workers: int = 8, max_iter: int = 5000, minres: float = 1e-6,
+                 tune_every: int = 0, tune_iters: int = 2, **caps):
+        self.batch = Batch(precision, vertices=vertices, meshes=meshes, viscous=True, **caps)
         self.precision = precision
         self.chunk = chunk
+        # every tune_every steps the autotuner re-picks the form of the
+        # iteration for the current mix (its iterations are ordinary ones)
+        self.tune_every = tune_every
+        self.tune_iters = tune_iters
+        self.tunings = []
         self.workers = workers
         self.max_iter = max_iter
         self.minres = minres
@@ -182,6 +188,8 @@ class Server:
                 else:
                     time.sleep(0.001)
                 continue
+            if self.tune_every and steps % self.tune_every == 0:
+                self.tunings.append(b.tune(self.tune_iters)["choice"])
             b.step(self.chunk)                             # all resident solves at once
             steps += 1
             resident_vertices.append(sum(b._meshes[s].np for s in resident))
@@ -220,6 +228,7 @@ class Server:
                      p99_latency_s=float(np.percentile(lat, 99)),
                      vertex_stage_updates=float(sum(r.npts * 3 * r.niter for r in res)),
                      mean_resident_vertices=float(np.mean(resident_vertices)) if resident_vertices else 0.0,
-                     steps=steps, chunk=self.chunk)
+                     steps=steps, chunk=self.chunk,
+                     tuner_choices={k: self.tunings.count(k) for k in set(self.tunings)})
         stats["vertex_stage_updates_per_s"] = stats["vertex_stage_updates"] / makespan
         return res, stats

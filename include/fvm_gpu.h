@@ -362,6 +362,9 @@ int64_t fvm_batch_launch_count(fvm_batch *b);
  * (FP64) with the two overlapped chains, 5 fused with the two chains. */
 int32_t fvm_batch_tune(fvm_batch *b, int32_t iters, int32_t max, double *ms_per_iter,
                        int32_t *choice);
+/* Sets the form of the iteration to a candidate of fvm_batch_tune (the
+ * same codes); FVM_ERR_ARG for a form that does not fit this batch. */
+int32_t fvm_batch_set_form(fvm_batch *b, int32_t form);
 
 /* Layout statistics of a mesh after renumbering (no GPU needed):
  * out[0] blocks, [1] interior edge entries (cut edges counted in both
