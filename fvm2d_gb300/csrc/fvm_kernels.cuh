@@ -577,6 +577,115 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRADV_MINB32
 }
 
 // ---------------------------------------------------------------------------
+// conres.f:14-22 partials of one block: sum of gra^2 and max |gra| (first
+// driver index on ties), gra = rho_new - rho_old.  Called by every thread
+// of the CTA (contains barriers).  FP64 states: FP64 arithmetic as before.
+// FP32 states: gra is formed exactly as a pair of floats (TwoSum), its
+// square as a pair (FMA residual), and the warp sums are pair sums; each
+// warp's pair is converted to FP64 once and the warps are summed in FP64.
+// The FP64 pipe of this GPU is slow, and this keeps it out of the 256
+// per-thread reductions: the sum carries ~2^-47 relative error instead of
+// 2^-53; max |gra| is exact.
+// ---------------------------------------------------------------------------
+struct DFloat {
+  float hi, lo;
+};
+__device__ __forceinline__ DFloat two_sum(float a, float b) {   // a + b = hi + lo exactly
+  const float s = __fadd_rn(a, b);
+  const float z = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, z)), __fsub_rn(b, z));
+  return {s, e};
+}
+__device__ __forceinline__ DFloat df_add(DFloat x, DFloat y) {
+  const DFloat s = two_sum(x.hi, y.hi);
+  const float e = __fadd_rn(s.lo, __fadd_rn(x.lo, y.lo));
+  const float hi = __fadd_rn(s.hi, e);
+  return {hi, __fsub_rn(e, __fsub_rn(hi, s.hi))};
+}
+__device__ __forceinline__ bool df_greater(DFloat x, DFloat y) {   // normalized pairs
+  return x.hi > y.hi || (x.hi == y.hi && x.lo > y.lo);
+}
+
+template <typename R>
+__device__ __forceinline__ void block_conres_partial(bool have, R rho_new, R rho_old, int orig,
+                                                     double *s_red, double *s_max, int *s_arg,
+                                                     BlockPartial *out) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int darg = INT_MAX;
+  if constexpr (sizeof(R) == 8) {
+    double d2 = 0.0, dabs = 0.0;
+    if (have) {
+      const double gra = double(rho_new) - double(rho_old);
+      d2 = gra * gra;
+      dabs = fabs(gra);
+      if (dabs > 0.0) darg = orig;
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const double o2 = __shfl_down_sync(0xffffffffu, d2, off);
+      const double om = __shfl_down_sync(0xffffffffu, dabs, off);
+      const int oa = __shfl_down_sync(0xffffffffu, darg, off);
+      d2 += o2;
+      if (om > dabs || (om == dabs && oa < darg)) {
+        dabs = om;
+        darg = oa;
+      }
+    }
+    if (lane == 0) {
+      s_red[wid] = d2;
+      s_max[wid] = dabs;
+      s_arg[wid] = darg;
+    }
+  } else {
+    DFloat sq2 = {0.f, 0.f}, mx = {0.f, 0.f};
+    if (have) {
+      const DFloat g = two_sum(float(rho_new), -float(rho_old));
+      const float h2 = __fmul_rn(g.hi, g.hi);
+      const float l2 = __fadd_rn(__fmaf_rn(g.hi, g.hi, -h2), __fmul_rn(__fmul_rn(2.f, g.hi), g.lo));
+      sq2 = two_sum(h2, l2);
+      mx = g.hi >= 0.f ? g : DFloat{-g.hi, -g.lo};
+      if (mx.hi > 0.f) darg = orig;
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const DFloat o2 = {__shfl_down_sync(0xffffffffu, sq2.hi, off),
+                         __shfl_down_sync(0xffffffffu, sq2.lo, off)};
+      const DFloat om = {__shfl_down_sync(0xffffffffu, mx.hi, off),
+                         __shfl_down_sync(0xffffffffu, mx.lo, off)};
+      const int oa = __shfl_down_sync(0xffffffffu, darg, off);
+      sq2 = df_add(sq2, o2);
+      if (df_greater(om, mx) || (om.hi == mx.hi && om.lo == mx.lo && oa < darg)) {
+        mx = om;
+        darg = oa;
+      }
+    }
+    if (lane == 0) {
+      s_red[wid] = double(sq2.hi) + double(sq2.lo);
+      s_max[wid] = double(mx.hi) + double(mx.lo);   // exact
+      s_arg[wid] = darg;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sacc = 0.0, m = 0.0;
+    int a = INT_MAX;
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++) {
+      sacc += s_red[i];
+      if (s_max[i] > m || (s_max[i] == m && s_arg[i] < a)) {
+        m = s_max[i];
+        a = s_arg[i];
+      }
+    }
+    BlockPartial bp;
+    bp.sumsq = sacc;
+    bp.maxabs = m;
+    bp.argmax = a;
+    bp.pad = 0;
+    *out = bp;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Flux pass: residu.f:37-88 (recon + roe/kfvs/hllc over iedge, solid_flux,
 // farfield_flux) gathered per vertex in Fortran order, then either the
 // residual is written (MODE_RESIDUAL) or the RK stage of update.f:17-35 is
@@ -745,8 +854,9 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_FLUX_MINB32 
     if (err) atomicCAS(&ctl.err, 0, 4 /* FVM_ERR_ROE_SONIC */);
     __syncthreads();
     // phase 2: gather per vertex in Fortran order
-    double d2 = 0.0, dabs = 0.0;
-    int darg = INT_MAX;
+    bool have = false;
+    R rho_new = R(0), rho_old = R(0);
+    int org = 0;
     if (threadIdx.x < bi.nv) {
       const int v = bi.v0 + threadIdx.x;
       R acc[4];
@@ -793,52 +903,16 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_FLUX_MINB32 
         A.st[out_buf(p, stage)][v] = pn;
         if (stage == 3) {
           // conres.f:14-22 partials and check_positivity.f:13-14 (rho, p)
-          const double gra = double(pn.x) - double(po.x);
-          d2 = gra * gra;
-          dabs = fabs(gra);
-          if (dabs > 0.0) darg = A.orig[v];
-          if (pn.x <= R(0) || pn.w <= R(0)) atomicMin(&ctl.err_point, A.orig[v]);
+          have = true;
+          rho_new = pn.x;
+          rho_old = po.x;
+          org = A.orig[v];
+          if (pn.x <= R(0) || pn.w <= R(0)) atomicMin(&ctl.err_point, org);
         }
       }
     }
-    if (mode == MODE_UPDATE && stage == 3) {
-      // deterministic block reduction: warp shuffles then warp 0
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) {
-        const double o2 = __shfl_down_sync(0xffffffffu, d2, off);
-        const double om = __shfl_down_sync(0xffffffffu, dabs, off);
-        const int oa = __shfl_down_sync(0xffffffffu, darg, off);
-        d2 += o2;
-        if (om > dabs || (om == dabs && oa < darg)) {
-          dabs = om;
-          darg = oa;
-        }
-      }
-      const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-      if (lane == 0) {
-        s_red[wid] = d2;
-        s_max[wid] = dabs;
-        s_arg[wid] = darg;
-      }
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        double s = 0.0, m = 0.0;
-        int a = INT_MAX;
-        for (int i = 0; i < (int)(blockDim.x >> 5); i++) {
-          s += s_red[i];
-          if (s_max[i] > m || (s_max[i] == m && s_arg[i] < a)) {
-            m = s_max[i];
-            a = s_arg[i];
-          }
-        }
-        BlockPartial bp;
-        bp.sumsq = s;
-        bp.maxabs = m;
-        bp.argmax = a;
-        bp.pad = 0;
-        A.part[bi.part] = bp;
-      }
-    }
+    if (mode == MODE_UPDATE && stage == 3)
+      block_conres_partial<R>(have, rho_new, rho_old, org, s_red, s_max, s_arg, A.part + bi.part);
     __syncthreads();
   }
 }
@@ -1074,8 +1148,9 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_FLUX_MINB32 
     if (err) atomicCAS(&ctl.err, 0, 4 /* FVM_ERR_ROE_SONIC */);
     __syncthreads();
     // phase D: gather per own vertex in Fortran order, RK stage
-    double d2 = 0.0, dabs = 0.0;
-    int darg = INT_MAX;
+    bool have = false;
+    R rho_new = R(0), rho_old = R(0);
+    int org = 0;
     if (t < bi.nv) {
       const int v = bi.v0 + t;
       R acc[4];
@@ -1108,50 +1183,15 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_FLUX_MINB32 
       const R4<R> pn = rk_update<R>(mc, stage, po, pc, dtv, v_cvarea(A, v), acc, noslip);
       A.st[out_buf(p, stage)][v] = pn;
       if (stage == 3) {
-        const double gra = double(pn.x) - double(po.x);
-        d2 = gra * gra;
-        dabs = fabs(gra);
-        if (dabs > 0.0) darg = A.orig[v];
-        if (pn.x <= R(0) || pn.w <= R(0)) atomicMin(&ctl.err_point, A.orig[v]);
+        have = true;
+        rho_new = pn.x;
+        rho_old = po.x;
+        org = A.orig[v];
+        if (pn.x <= R(0) || pn.w <= R(0)) atomicMin(&ctl.err_point, org);
       }
     }
-    if (stage == 3) {
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) {
-        const double o2 = __shfl_down_sync(0xffffffffu, d2, off);
-        const double om = __shfl_down_sync(0xffffffffu, dabs, off);
-        const int oa = __shfl_down_sync(0xffffffffu, darg, off);
-        d2 += o2;
-        if (om > dabs || (om == dabs && oa < darg)) {
-          dabs = om;
-          darg = oa;
-        }
-      }
-      const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-      if (lane == 0) {
-        s_red[wid] = d2;
-        s_max[wid] = dabs;
-        s_arg[wid] = darg;
-      }
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        double sacc = 0.0, m = 0.0;
-        int a = INT_MAX;
-        for (int i = 0; i < (int)(blockDim.x >> 5); i++) {
-          sacc += s_red[i];
-          if (s_max[i] > m || (s_max[i] == m && s_arg[i] < a)) {
-            m = s_max[i];
-            a = s_arg[i];
-          }
-        }
-        BlockPartial bp;
-        bp.sumsq = sacc;
-        bp.maxabs = m;
-        bp.argmax = a;
-        bp.pad = 0;
-        A.part[bi.part] = bp;
-      }
-    }
+    if (stage == 3)
+      block_conres_partial<R>(have, rho_new, rho_old, org, s_red, s_max, s_arg, A.part + bi.part);
     __syncthreads();
   }
 }
