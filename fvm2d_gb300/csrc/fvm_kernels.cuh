@@ -126,6 +126,12 @@ __device__ __forceinline__ void fence_proxy_async_smem() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
+// Threads of the per-mesh monitor CTA (a power of two; the fixed-order
+// reduction trees depend on it).  Wider CTAs measured no faster.
+constexpr int kMonitorMaxThreads = 256;
+template <typename R>
+constexpr int monitor_threads() { return 256; }
+
 // Per-vertex geometry in the kernel's precision (FP32 copies for R = float).
 template <typename R>
 __device__ __forceinline__ R v_ais(const ArenaPtrs<R> &A, int v) {
@@ -1322,7 +1328,7 @@ __global__ void __launch_bounds__(kBlockVerts) k_sa(ArenaPtrs<R> A, int stage, i
 template <typename R>
 __device__ void clcd_block(const ArenaPtrs<R> &A, const MeshConst &mc, int mesh_phase,
                            int serial, double &cl, double &cd) {
-  __shared__ double s_x[256], s_y[256];
+  __shared__ double s_x[kMonitorMaxThreads], s_y[kMonitorMaxThreads];
   const R4<R> *P = A.st[mesh_phase];
   double xf = 0.0, yf = 0.0;
   if (serial) {
@@ -1349,6 +1355,38 @@ __device__ void clcd_block(const ArenaPtrs<R> &A, const MeshConst &mc, int mesh_
         yf = yf + pp * sy - txy * sx - tyy * sy;
       }
     }
+  } else if constexpr (sizeof(R) == 4) {
+    // FP32 states: each edge's force terms from the FP32 values (the edge
+    // vector an FP64 difference rounded once), accumulated in FP64
+    for (int i = threadIdx.x; i < mc.nsw; i += blockDim.x) {
+      const int2 nn = A.sw_nodes[mc.sw0 + i];
+      const double2 c1 = A.coord[nn.x], c2 = A.coord[nn.y];
+      const float sx = float(c2.y - c1.y), sy = -float(c2.x - c1.x);
+      const float mu1 = A.mu[nn.x], mu2 = A.mu[nn.y];
+      const Grad<R> g1 = A.grad[nn.x], g2 = A.grad[nn.y];
+      const float p1 = P[nn.x].w, p2 = P[nn.y].w;
+      const float n2b3 = 2.0f / 3.0f;
+      const float txx = 0.5f * (n2b3 * mu1 * (2.0f * g1.qx[1] - g1.qy[2]) +
+                                n2b3 * mu2 * (2.0f * g2.qx[1] - g2.qy[2]));
+      const float txy = 0.5f * (mu1 * (g1.qy[1] + g1.qx[2]) + mu2 * (g2.qy[1] + g2.qx[2]));
+      const float tyy = 0.5f * (n2b3 * mu1 * (2.0f * g1.qy[2] - g1.qx[1]) +
+                                n2b3 * mu2 * (2.0f * g2.qy[2] - g2.qx[1]));
+      const float pp = 0.5f * (p1 + p2);
+      xf += double(pp * sx - txx * sx - txy * sy);
+      yf += double(pp * sy - txy * sx - tyy * sy);
+    }
+    s_x[threadIdx.x] = xf;
+    s_y[threadIdx.x] = yf;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+      if (threadIdx.x < s) {
+        s_x[threadIdx.x] += s_x[threadIdx.x + s];
+        s_y[threadIdx.x] += s_y[threadIdx.x + s];
+      }
+      __syncthreads();
+    }
+    xf = s_x[0];
+    yf = s_y[0];
   } else {
     for (int i = threadIdx.x; i < mc.nsw; i += blockDim.x) {
       const int2 nn = A.sw_nodes[mc.sw0 + i];
@@ -1389,8 +1427,8 @@ __device__ void clcd_block(const ArenaPtrs<R> &A, const MeshConst &mc, int mesh_
 template <typename R>
 __device__ void conres_block(const ArenaPtrs<R> &A, const MeshConst &mc, double &sum,
                              double &mx, int &arg) {
-  __shared__ double s_s[256], s_m[256];
-  __shared__ int s_a[256];
+  __shared__ double s_s[kMonitorMaxThreads], s_m[kMonitorMaxThreads];
+  __shared__ int s_a[kMonitorMaxThreads];
   double s = 0.0, m = 0.0;
   int a = INT_MAX;
   for (int i = threadIdx.x; i < mc.nblk; i += blockDim.x) {
@@ -1424,7 +1462,7 @@ __device__ void conres_block(const ArenaPtrs<R> &A, const MeshConst &mc, double 
 
 // One CTA (256 threads) per mesh slot listed in mesh_list.
 template <typename R>
-__global__ void __launch_bounds__(256) k_monitor(ArenaPtrs<R> A, int serial_clcd) {
+__global__ void __launch_bounds__(kMonitorMaxThreads) k_monitor(ArenaPtrs<R> A, int serial_clcd) {
   const int m = blockIdx.x;
   MeshCtl &ctl = A.ctl[m];
   if (!ctl.active) return;

@@ -93,7 +93,7 @@ inline int fit_grid(const LaunchCfg &c, K kern, size_t smem) {
   }                                                                                        \
   cudaError_t launch_monitor(const ArenaPtrs<R> &A, const LaunchCfg &c, int serial_clcd) {  \
     if (A.nslots <= 0) return cudaSuccess;                                                 \
-    k_monitor<R><<<A.nslots, 256, 0, c.stream>>>(A, serial_clcd);                          \
+    k_monitor<R><<<A.nslots, monitor_threads<R>(), 0, c.stream>>>(A, serial_clcd);         \
     return cudaGetLastError();                                                             \
   }                                                                                        \
   cudaError_t launch_update(const ArenaPtrs<R> &A, const LaunchCfg &c, int irk) {           \
