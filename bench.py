@@ -184,7 +184,11 @@ def run_gpu(args):
         b.start(s, args.warmup + 2 * args.steps + 40)
     b.step(args.warmup)
     b.sync()
-    tuned = b.tune(iters=5)   # ordinary iterations of the solves; untimed
+    if args.form:             # a given form (profiling runs): no tuning
+        b.set_form(args.form)
+        tuned = {"choice": args.form, "ms_per_iter": None}
+    else:
+        tuned = b.tune(iters=5)   # ordinary iterations of the solves; untimed
     b.sync()
     b.step(1)           # instantiates the timed graph outside the timed region
     b.sync()
@@ -597,6 +601,96 @@ def fp64_accuracy(reqs, res, nmax=6, pmax=60000):
             "failed_requests_in_fp64": failed}
 
 
+ACCURACY_CASES = [
+    # (name, workload grid, flow, iterations)
+    ("config1 euler 160x48 roe", "euler_160x48", dict(mach=0.8, aoa_deg=1.25, cfl=1.0, iflux=1), 2000),
+    ("config2 euler 1024x384 roe", "euler_1024x384", dict(mach=0.8, aoa_deg=1.25, cfl=1.0, iflux=1), 2000),
+    ("config2 euler 1024x384 kfvs", "euler_1024x384", dict(mach=0.8, aoa_deg=1.25, cfl=1.0, iflux=2), 2000),
+    ("config2 euler 1024x384 hllc", "euler_1024x384", dict(mach=0.8, aoa_deg=1.25, cfl=1.0, iflux=3), 2000),
+    ("config3 laminar 512x192 roe", "laminar_512x192",
+     dict(iflow=2, mach=0.5, aoa_deg=0.0, rey=5000.0, cfl=0.8, iflux=1), 2000),
+    ("config4 rans-sa 768x256 hllc", "rans_768x256",
+     dict(iflow=3, mach=0.7, aoa_deg=2.0, rey=6.5e6, cfl=0.5, iflux=3, nut_ratio=3.0), 1000),
+]
+
+
+def run_accuracy(args):
+    """FP32 against FP64 (whose arithmetic equals the serial FP64 oracle's)
+    on the four single-mesh configurations: residual history, cl/cd (final
+    and mean of the last 256 iterations) and wall Cp after the same number
+    of iterations."""
+    import numpy as np
+
+    import fvm2d_gb300 as F
+    from fvm2d_gb300 import results
+    from fvm2d_gb300.batch import Batch
+    from fvm2d_gb300.ogrid import workload_grid
+    meshes, flows = [], []
+    for name, wl, flow, n in ACCURACY_CASES:
+        g = workload_grid(wl)
+        meshes.append(F.build_geometry(g.coord, g.elem, g.ptype,
+                                       wall_distance=flow.get("iflow", 1) == 3, bugcompat=0))
+        flows.append(flow)
+    out = {}
+    runs = {}
+    for prec in (F.FP64, F.FP32):
+        b = Batch(prec, vertices=sum(m.np for m in meshes), meshes=len(meshes), viscous=True)
+        pars = [F.make_params(precision=prec, bugcompat=0, **f) for f in flows]
+        slots = [b.add(p, m) for p, m in zip(pars, meshes)]
+        nmax = [c[3] for c in ACCURACY_CASES]
+        for s, n in zip(slots, nmax):
+            b.start(s, n)
+        hist = [dict(fres=[], cl=[], cd=[]) for _ in slots]
+        done = [0] * len(slots)
+        t0 = time.perf_counter()
+        while any(d < n for d, n in zip(done, nmax)):
+            b.step(500)
+            for j, s in enumerate(slots):
+                q = b.poll(s)
+                if q["niter"] > done[j]:
+                    h = b.history(s, done[j], q["niter"] - done[j])
+                    for k in ("fres", "cl", "cd"):
+                        hist[j][k].append(h[k])
+                    done[j] = q["niter"]
+                if not q["active"] and q["niter"] < nmax[j]:
+                    nmax[j] = q["niter"]          # stopped (status in poll)
+        wall = time.perf_counter() - t0
+        runs[prec] = []
+        for j, s in enumerate(slots):
+            q = b.poll(s)
+            st = b.get_state(s)
+            h = {k: np.concatenate(v) if v else np.zeros(0) for k, v in hist[j].items()}
+            runs[prec].append(dict(poll=q, hist=h, wall=results.wall_table(
+                meshes[j], st, pars[j], flows[j].get("iflow", 1))))
+        b.close()
+        out[f"wall_s_fp{64 if prec == F.FP64 else 32}"] = round(wall, 2)
+    cases = []
+    for j, (name, wl, flow, n) in enumerate(ACCURACY_CASES):
+        r64, r32 = runs[F.FP64][j], runs[F.FP32][j]
+        k = min(len(r64["hist"]["fres"]), len(r32["hist"]["fres"]))
+        f64, f32 = r64["hist"]["fres"][:k], r32["hist"]["fres"][:k]
+        tail = min(256, k)
+        cases.append({
+            "case": name, "vertices": meshes[j].np, "iterations": k,
+            "status": [r64["poll"]["status"], r32["poll"]["status"]],
+            "fres_final": [float(f64[-1]), float(f32[-1])] if k else None,
+            "fres_max_rel_err": float(np.max(np.abs(f32 - f64) / np.abs(f64))) if k else None,
+            "fres_log10_max_abs_diff": float(np.max(np.abs(np.log10(f32) - np.log10(f64)))) if k else None,
+            "cl": [r64["poll"]["cl"], r32["poll"]["cl"]], "cd": [r64["poll"]["cd"], r32["poll"]["cd"]],
+            "abs_err_cl": abs(r64["poll"]["cl"] - r32["poll"]["cl"]),
+            "abs_err_cd": abs(r64["poll"]["cd"] - r32["poll"]["cd"]),
+            "abs_err_cl_tail_mean": float(abs(np.mean(r64["hist"]["cl"][k - tail:k]) -
+                                              np.mean(r32["hist"]["cl"][k - tail:k]))) if k else None,
+            "abs_err_cd_tail_mean": float(abs(np.mean(r64["hist"]["cd"][k - tail:k]) -
+                                              np.mean(r32["hist"]["cd"][k - tail:k]))) if k else None,
+            "cp_max_abs_err": float(np.max(np.abs(r64["wall"]["cp"] - r32["wall"]["cp"]))),
+        })
+    out.update({"mode": "accuracy", "targets": {"cl": 1e-4, "cd": 2e-5},
+                "what": "FP32 batch vs FP64 batch (bitwise the serial FP64 oracle's arithmetic), "
+                        "same grids, same iteration counts", "cases": cases})
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -606,7 +700,10 @@ def main():
     ap.add_argument("--flux", choices=sorted(FLUX_CODES), default="roe")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--quick", action="store_true", help="skip the side measurements")
-    ap.add_argument("--mode", choices=["throughput", "serve"], default="throughput")
+    ap.add_argument("--form", default=None,
+                    choices=["bulk", "loads", "vertex", "fused", "split+overlap", "fused+overlap"],
+                    help="use this form of the iteration instead of the autotuner's choice")
+    ap.add_argument("--mode", choices=["throughput", "serve", "accuracy"], default="throughput")
     ap.add_argument("--requests", type=int, default=512)
     ap.add_argument("--rate", type=float, default=20.0)
     ap.add_argument("--seed", type=int, default=0)
@@ -626,6 +723,10 @@ def main():
         from fvm2d_gb300 import build
         build.build()
         run_serve(args)
+    elif args.mode == "accuracy":
+        from fvm2d_gb300 import build
+        build.build()
+        run_accuracy(args)
     else:
         from fvm2d_gb300 import build
         build.build()

@@ -587,11 +587,10 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRADV_MINB32
 // driver index on ties), gra = rho_new - rho_old.  Called by every thread
 // of the CTA (contains barriers).  FP64 states: FP64 arithmetic as before.
 // FP32 states: gra is formed exactly as a pair of floats (TwoSum), its
-// square as a pair (FMA residual), and the warp sums are pair sums; each
-// warp's pair is converted to FP64 once and the warps are summed in FP64.
-// The FP64 pipe of this GPU is slow, and this keeps it out of the 256
-// per-thread reductions: the sum carries ~2^-47 relative error instead of
-// 2^-53; max |gra| is exact.
+// square as a pair (FMA residual), and the warp and block sums are pair
+// sums, converted to FP64 once per block.  The FP64 pipe of this GPU is
+// slow, and this keeps it out of the reduction: the sum carries ~2^-47
+// relative error instead of 2^-53; max |gra| is exact.
 // ---------------------------------------------------------------------------
 struct DFloat {
   float hi, lo;
@@ -665,11 +664,32 @@ __device__ __forceinline__ void block_conres_partial(bool have, R rho_new, R rho
         darg = oa;
       }
     }
+    // warps' pairs summed by thread 0, still as pairs; one conversion to FP64
+    __shared__ DFloat s_sq[kBlockVerts / 32], s_mx[kBlockVerts / 32];
     if (lane == 0) {
-      s_red[wid] = double(sq2.hi) + double(sq2.lo);
-      s_max[wid] = double(mx.hi) + double(mx.lo);   // exact
+      s_sq[wid] = sq2;
+      s_mx[wid] = mx;
       s_arg[wid] = darg;
     }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      DFloat t = s_sq[0], m = s_mx[0];
+      int a = s_arg[0];
+      for (int i = 1; i < (int)(blockDim.x >> 5); i++) {
+        t = df_add(t, s_sq[i]);
+        if (df_greater(s_mx[i], m) || (s_mx[i].hi == m.hi && s_mx[i].lo == m.lo && s_arg[i] < a)) {
+          m = s_mx[i];
+          a = s_arg[i];
+        }
+      }
+      BlockPartial bp;
+      bp.sumsq = double(t.hi) + double(t.lo);
+      bp.maxabs = double(m.hi) + double(m.lo);   // exact
+      bp.argmax = a;
+      bp.pad = 0;
+      *out = bp;
+    }
+    return;
   }
   __syncthreads();
   if (threadIdx.x == 0) {

@@ -152,3 +152,34 @@ def test_amdba_roundtrip(tmp_path):
     np.testing.assert_array_equal(h.coord, g.coord)
     np.testing.assert_array_equal(h.elem, g.elem)
     np.testing.assert_array_equal(h.ptype, g.ptype)
+
+
+def test_wall_table_and_sol_roundtrip(fvm_lib, oracle_lib, tmp_path):
+    """WALL.DAT columns (result.f:92-118) and the SOL restart file
+    (finalize.f:14-24 / initialize.f:91-103) from an oracle state."""
+    from fvm2d_gb300 import results
+    g = naca_ogrid(48, 16)
+    o = oracle_lib.Oracle(g.coord, g.elem, g.ptype, iflow=L.LAMINAR, mach=0.5, rey=2000.0,
+                          cfl=0.5)
+    from fvm2d_gb300.solver import MeshArrays
+    m = MeshArrays(o.mesh_arrays())
+    m.wd = oracle_lib.wall_dist(m.coord, m.edge, m.ptype, bugcompat=0)
+    par = fvm_lib.make_params(iflow=L.LAMINAR, mach=0.5, rey=2000.0, cfl=0.5)
+
+    def state():
+        return {k: o.d(k).copy() for k in ("prim", "qx", "qy", "mu", "nut")}
+    st0 = state()
+    t0 = results.wall_table(m, st0, par, L.LAMINAR)
+    np.testing.assert_allclose(t0["cp"], 0.0, atol=1e-12)       # freestream start
+    o.iterate(5)
+    st = state()
+    t = results.wall_table(m, st, par, L.LAMINAR)
+    assert t["x"].shape == t["cp"].shape == t["cf"].shape == (m.nsp,)
+    assert np.all(np.isfinite(t["cf"])) and np.all(t["wd1"] > 0) and np.all(t["yplus"] >= 0)
+    p = tmp_path / "SOL"
+    results.write_sol(str(p), st["prim"], st["nut"], par.gamma1)
+    prim, nut = results.read_sol(str(p), par.gamma1)
+    np.testing.assert_allclose(prim, st["prim"], rtol=1e-13, atol=1e-15)
+    np.testing.assert_array_equal(nut, st["nut"])
+    results.write_wall(str(tmp_path / "WALL.DAT"), t)
+    assert np.loadtxt(str(tmp_path / "WALL.DAT")).shape == (m.nsp, 5)
