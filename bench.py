@@ -211,7 +211,8 @@ def run_gpu(args):
     # them needs a host sync after every iteration, kept out of `value`);
     # kernels one at a time (no overlapped chains), so each launch's time
     # is its own
-    alone = {"split+overlap": "bulk", "fused+overlap": "fused"}.get(b.form, b.form)
+    alone = {"split+overlap": "bulk", "split+overlap4": "bulk", "split+overlap8": "bulk",
+             "fused+overlap": "fused"}.get(b.form, b.form)
     b.set_form(alone)
     b.timing(True)
     b.step(1)
@@ -701,7 +702,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--quick", action="store_true", help="skip the side measurements")
     ap.add_argument("--form", default=None,
-                    choices=["bulk", "loads", "vertex", "fused", "split+overlap", "fused+overlap"],
+                    choices=["bulk", "loads", "vertex", "fused", "split+overlap", "fused+overlap",
+                             "split+overlap4", "split+overlap8"],
                     help="use this form of the iteration instead of the autotuner's choice")
     ap.add_argument("--mode", choices=["throughput", "serve", "accuracy"], default="throughput")
     ap.add_argument("--requests", type=int, default=512)

@@ -68,10 +68,12 @@ class Batch:
         self.precision = precision
         self._meshes = {}
         gm = int(caps.get("grad_mode", 0)) or (3 if precision == L.FP32 else 1)
+        ch = int(caps.get("overlap", 0))
         if int(caps.get("fused", 0)) > 0:
-            self.form = "fused+overlap" if int(caps.get("overlap", 0)) > 0 else "fused"
-        elif int(caps.get("overlap", 0)) > 0:
-            self.form = "split+overlap"
+            self.form = "fused+overlap" if ch > 1 else "fused"
+        elif ch > 1:
+            self.form = {2: "split+overlap", 4: "split+overlap4", 8: "split+overlap8"}.get(
+                ch, "split+overlap")
         else:
             self.form = {3: "bulk", 1: "loads", 2: "vertex"}[gm]
 
@@ -185,7 +187,8 @@ class Batch:
     def launch_count(self) -> int:
         return int(L.lib().fvm_batch_launch_count(self.h))
 
-    TUNE_CANDIDATES = ("bulk", "loads", "vertex", "fused", "split+overlap", "fused+overlap")
+    TUNE_CANDIDATES = ("bulk", "loads", "vertex", "fused", "split+overlap", "fused+overlap",
+                       "split+overlap4", "split+overlap8")
 
     def set_form(self, name: str):
         """Set the form of the iteration to one of TUNE_CANDIDATES."""

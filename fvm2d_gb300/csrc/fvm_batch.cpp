@@ -96,9 +96,10 @@ struct fvm_batch {
   RangeAlloc pool[P_COUNT];
   std::vector<Slot> slots;
   cudaStream_t stream = nullptr;
-  cudaStream_t stream2 = nullptr;          // second chain of the overlapped iteration
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-  bool overlap = false;                    // two chains over the halves of the meshes
+  // further chains of the overlapped iteration (chain 0 runs on `stream`)
+  cudaStream_t chain_stream[kMaxChains] = {};
+  cudaEvent_t ev_fork[kMaxChains] = {}, ev_join[kMaxChains] = {};
+  int chains = 1;                          // chains of kernels over parts of the meshes
   std::vector<void *> owned;
   // device arrays
   void *st[3] = {nullptr, nullptr, nullptr};
@@ -442,11 +443,23 @@ int32_t update_work(fvm_batch *b) {
     b->graph = nullptr;
   }
   const int n = (int)work.size();
-  // split of the work list at the mesh boundary nearest its middle
-  int split = 0;
-  for (int x : mesh_first)
-    if (std::abs(2 * x - n) < std::abs(2 * split - n)) split = x;
-  const int head[2] = {n, split};
+  // the work list in kMaxChains parts at mesh boundaries: part k ends at
+  // the boundary nearest (k+1)/chains of the list (the last parts are empty
+  // when fewer chains run)
+  int head[1 + kMaxChains];
+  head[0] = n;
+  int prev = 0;
+  for (int k = 1; k <= kMaxChains; k++) {
+    int end = n;
+    if (k < b->chains) {
+      const long target = (long)k * n / b->chains;
+      end = prev;
+      for (int x : mesh_first)
+        if (x >= prev && std::labs(x - target) < std::labs(end - target)) end = x;
+    }
+    head[k] = end;
+    prev = end;
+  }
   if (n) FVM_TRY(b, cudaMemcpyAsync(b->work, work.data(), n * sizeof(int), cudaMemcpyHostToDevice, b->stream));
   FVM_TRY(b, cudaMemcpyAsync(b->nwork, head, sizeof(head), cudaMemcpyHostToDevice, b->stream));
   FVM_TRY(b, cudaStreamSynchronize(b->stream));
@@ -478,7 +491,7 @@ int32_t enqueue_iteration(fvm_batch *b, bool with_events) {
   };
   // the three RK stages of the blocks of one part of the work list; with
   // fork set, an event after the first gradient pass lets the other part
-  // start then, so the two parts' passes overlap on the device
+  // start then, so the parts' passes overlap on the device
   auto stages = [&](const ArenaPtrs<R> &Ap, const LaunchCfg &cp, cudaEvent_t fork) -> int32_t {
     cudaStream_t st = cp.stream;
     for (int s = 1; s <= 3; s++) {
@@ -507,19 +520,22 @@ int32_t enqueue_iteration(fvm_batch *b, bool with_events) {
     }
     return FVM_OK;
   };
-  if (b->overlap) {
-    // two independent chains over the meshes before / from the split
-    ArenaPtrs<R> A1 = A, A2 = A;
-    A1.wpart = 1;
-    A2.wpart = 2;
-    LaunchCfg c2 = c;
-    c2.stream = b->stream2;
-    int32_t st = stages(A1, c, b->ev_fork);
-    if (st) return st;
-    FVM_TRY(b, cudaStreamWaitEvent(b->stream2, b->ev_fork, 0));
-    if ((st = stages(A2, c2, nullptr))) return st;
-    FVM_TRY(b, cudaEventRecord(b->ev_join, b->stream2));
-    FVM_TRY(b, cudaStreamWaitEvent(b->stream, b->ev_join, 0));
+  if (b->chains > 1) {
+    // independent chains over the parts of the work list; chain k starts
+    // after chain k-1's first pass, then all join the first stream
+    for (int k = 0; k < b->chains; k++) {
+      ArenaPtrs<R> Ak = A;
+      Ak.wpart = k + 1;
+      LaunchCfg ck = c;
+      ck.stream = k ? b->chain_stream[k] : b->stream;
+      if (k) FVM_TRY(b, cudaStreamWaitEvent(ck.stream, b->ev_fork[k - 1], 0));
+      const int32_t st = stages(Ak, ck, k + 1 < b->chains ? b->ev_fork[k] : nullptr);
+      if (st) return st;
+    }
+    for (int k = 1; k < b->chains; k++) {
+      FVM_TRY(b, cudaEventRecord(b->ev_join[k], b->chain_stream[k]));
+      FVM_TRY(b, cudaStreamWaitEvent(b->stream, b->ev_join[k], 0));
+    }
   } else {
     int32_t st = stages(A, c, nullptr);
     if (st) return st;
@@ -632,9 +648,11 @@ extern "C" int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *cap
     if (_e != cudaSuccess) return fail(cuda_status(b, _e));  \
   } while (0)
   TRYB(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
-  TRYB(cudaStreamCreateWithFlags(&b->stream2, cudaStreamNonBlocking));
-  TRYB(cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming));
-  TRYB(cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming));
+  for (int k = 0; k < kMaxChains; k++) {
+    if (k) TRYB(cudaStreamCreateWithFlags(&b->chain_stream[k], cudaStreamNonBlocking));
+    TRYB(cudaEventCreateWithFlags(&b->ev_fork[k], cudaEventDisableTiming));
+    TRYB(cudaEventCreateWithFlags(&b->ev_join[k], cudaEventDisableTiming));
+  }
   auto &O = b->owned;
   const size_t V = (size_t)b->cap[P_V] + kVertAlign, r = b->rsz;   // with slack
   for (int i = 0; i < 3; i++) TRYB(dalloc(O, (unsigned char **)&b->st[i], 4 * r * V));
@@ -662,7 +680,7 @@ extern "C" int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *cap
   TRYB(dalloc(O, &b->blocks, (size_t)c.blocks));
   TRYB(dalloc(O, &b->part, (size_t)c.blocks));
   TRYB(dalloc(O, &b->work, (size_t)c.blocks));
-  TRYB(dalloc(O, &b->nwork, 2));
+  TRYB(dalloc(O, &b->nwork, 1 + kMaxChains));
   TRYB(dalloc(O, &b->be_nodes, (size_t)c.edge_entries));
   TRYB(dalloc(O, &b->be_loc, (size_t)c.edge_entries));
   TRYB(dalloc(O, &b->halo_ids, (size_t)b->cap[P_HALO]));
@@ -690,7 +708,7 @@ extern "C" int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *cap
   TRYB(dalloc(O, &b->h_cd, H));
   TRYB(dalloc(O, &b->h_iresi, H));
   TRYB(cudaMemsetAsync(b->ctl, 0, sizeof(MeshCtl) * c.meshes, b->stream));
-  TRYB(cudaMemsetAsync(b->nwork, 0, 2 * sizeof(int), b->stream));
+  TRYB(cudaMemsetAsync(b->nwork, 0, (1 + kMaxChains) * sizeof(int), b->stream));
   TRYB(cudaMemsetAsync(b->grad, 0, 8 * r * V, b->stream));
   TRYB(cudaMemsetAsync(b->resv, 0, 4 * r * V, b->stream));
   TRYB(cudaStreamSynchronize(b->stream));
@@ -700,7 +718,7 @@ extern "C" int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *cap
   b->cfg.max_tri2 = c.max_tri2;
   b->cfg.max_loc = c.max_loc;
   b->fused = b->fused_wanted = c.fused > 0;
-  b->overlap = c.overlap > 0;
+  b->chains = std::min(std::max(c.overlap, 1), kMaxChains);
   // gradient pass: bulk-copy staging by default in FP32 (when its shared
   // memory fits), per-thread loads in FP64
   const bool bulk_fits = grad_bulk_layout(c.max_tri, c.viscous != 0).total <= kMaxSmem;
@@ -733,9 +751,11 @@ extern "C" int32_t fvm_batch_destroy(fvm_batch *b) {
   for (void *p : b->owned) cudaFree(p);
   if (b->pinned) cudaFreeHost(b->pinned);
   if (b->stream) cudaStreamDestroy(b->stream);
-  if (b->stream2) cudaStreamDestroy(b->stream2);
-  if (b->ev_fork) cudaEventDestroy(b->ev_fork);
-  if (b->ev_join) cudaEventDestroy(b->ev_join);
+  for (int k = 0; k < kMaxChains; k++) {
+    if (b->chain_stream[k]) cudaStreamDestroy(b->chain_stream[k]);
+    if (b->ev_fork[k]) cudaEventDestroy(b->ev_fork[k]);
+    if (b->ev_join[k]) cudaEventDestroy(b->ev_join[k]);
+  }
   delete b;
   return FVM_OK;
 }
@@ -1161,15 +1181,16 @@ extern "C" int32_t fvm_batch_step(fvm_batch *b, int32_t niter) {
 struct Form {
   bool fused;
   int grad;
-  bool overlap;
+  int chains;
 };
-constexpr int kForms = 6;
+constexpr int kForms = 8;
 
 static Form form_of(const fvm_batch *b, int i) {
   const bool bulk = b->prec == FVM_PREC_FP32 &&
                     grad_bulk_layout(b->caps.max_tri, b->caps.viscous != 0).total <= kMaxSmem;
-  const Form f[kForms] = {{false, 3, false}, {false, 1, false}, {false, 2, false},
-                          {true, 1, false},  {false, bulk ? 3 : 1, true}, {true, 1, true}};
+  const int g = bulk ? 3 : 1;
+  const Form f[kForms] = {{false, 3, 1}, {false, 1, 1}, {false, 2, 1}, {true, 1, 1},
+                          {false, g, 2}, {true, 1, 2},  {false, g, 4}, {false, g, 8}};
   return f[i];
 }
 
@@ -1184,22 +1205,23 @@ static bool form_fits(const fvm_batch *b, const Form &f) {
   return true;
 }
 
-static void apply_form(fvm_batch *b, const Form &f) {
+static int32_t apply_form(fvm_batch *b, const Form &f) {
   b->fused = b->fused_wanted = f.fused;
   b->cfg.grad_mode = f.grad;
-  b->overlap = f.overlap;
+  const bool rechain = f.chains != b->chains;
+  b->chains = f.chains;
   if (b->graph) {
     cudaGraphExecDestroy(b->graph);
     b->graph = nullptr;
   }
+  return rechain ? update_work(b) : FVM_OK;   // the parts of the work list
 }
 
 extern "C" int32_t fvm_batch_set_form(fvm_batch *b, int32_t form) {
   if (!b || form < 0 || form >= kForms) return FVM_ERR_ARG;
   const Form f = form_of(b, form);
   if (!form_fits(b, f)) return FVM_ERR_ARG;
-  apply_form(b, f);
-  return FVM_OK;
+  return apply_form(b, f);
 }
 
 extern "C" int32_t fvm_batch_tune(fvm_batch *b, int32_t iters, int32_t max, double *ms_per_iter,
@@ -1219,7 +1241,7 @@ extern "C" int32_t fvm_batch_tune(fvm_batch *b, int32_t iters, int32_t max, doub
   for (int i = 0; i < kForms && st == FVM_OK; i++) {
     const Form f = form_of(b, i);
     if (!form_fits(b, f)) continue;
-    apply_form(b, f);
+    if ((st = apply_form(b, f))) break;
     if ((st = fvm_batch_step(b, 1))) break;   // capture + one untimed iteration
     cudaError_t e = cudaEventRecord(e0, b->stream);
     if (e == cudaSuccess) st = fvm_batch_step(b, iters);
@@ -1239,9 +1261,9 @@ extern "C" int32_t fvm_batch_tune(fvm_batch *b, int32_t iters, int32_t max, doub
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (best < 0) best = form_fits(b, form_of(b, 0)) ? 0 : 1;
-  apply_form(b, form_of(b, best));
+  const int32_t st2 = apply_form(b, form_of(b, best));
   if (choice) *choice = best;
-  return st;
+  return st ? st : st2;
 }
 
 extern "C" int32_t fvm_batch_sync(fvm_batch *b) {
@@ -1313,7 +1335,7 @@ extern "C" int32_t fvm_batch_timing(fvm_batch *b, int32_t on) {
   if (want == b->timing) return FVM_OK;
   FVM_TRY(b, cudaStreamSynchronize(b->stream));
   if (want && b->ev.empty()) {
-    const int pairs = 32;
+    const int pairs = 128;
     b->ev.resize(2 * pairs);
     b->ev_kind.assign(pairs, 0);
     for (auto &e : b->ev) FVM_TRY(b, cudaEventCreate(&e));

@@ -60,6 +60,10 @@ struct BlockInfo {          // 16 ints, one per CTA
 // slack at its end for the rounded-up copies.
 constexpr int kVertAlign = 8;
 
+// Most chains of kernels an iteration runs side by side (parts of the
+// work list split at mesh boundaries).
+constexpr int kMaxChains = 8;
+
 #ifdef __CUDACC__
 #define FVM_HD __host__ __device__
 #else
@@ -231,8 +235,8 @@ struct ArenaPtrs {
   int *h_iresi;
   // block work list (indices into blocks[]) and its length
   const int *work;
-  const int *nwork;    // [0] blocks in the work list, [1] split (a mesh boundary)
-  int wpart;           // 0 whole list, 1 before the split, 2 from it
+  const int *nwork;    // [0] blocks in the work list, [k] end of part k (k = 1..kMaxChains)
+  int wpart;           // 0 the whole list, k part k
   int nslots;             // mesh slots (monitor grid)
 };
 

@@ -60,13 +60,18 @@ __device__ __forceinline__ void prefetch_l2(const void *p, size_t bytes) {
 }
 
 // The next block this CTA will process (persistent loop), for prefetching.
-// The blocks a launch covers: the whole work list (part 0), or the part of
-// it before (1) or from (2) the split, a mesh boundary.
+// The blocks a launch covers: the whole work list (part 0) or part k, which
+// ends at nwork[k] and starts where part k-1 ends (parts end at mesh
+// boundaries).
 template <typename R>
 __device__ __forceinline__ void work_range(const ArenaPtrs<R> &A, int &w0, int &w1) {
-  const int n = A.nwork[0], s = A.nwork[1];
-  w0 = A.wpart == 2 ? s : 0;
-  w1 = A.wpart == 1 ? s : n;
+  if (A.wpart == 0) {
+    w0 = 0;
+    w1 = A.nwork[0];
+  } else {
+    w0 = A.wpart == 1 ? 0 : A.nwork[A.wpart - 1];
+    w1 = A.nwork[A.wpart];
+  }
 }
 
 __device__ __forceinline__ const BlockInfo *next_block(const BlockInfo *blocks, const int *work,

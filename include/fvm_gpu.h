@@ -284,11 +284,12 @@ typedef struct fvm_batch_caps {
                                    block's triangles and incidence staged by
                                    bulk copies (FP32 only); 0 (default): 3 in
                                    FP32, 1 in FP64                           */
-  int32_t overlap;              /* 1: the meshes before and after the middle
-                                   of the work list run as two chains of
-                                   kernels on two streams, so one part's
-                                   gradient pass overlaps the other's flux
-                                   pass; 0 (default): one chain             */
+  int32_t overlap;              /* 2..8: the meshes run in that many chains
+                                   of kernels on their own streams (parts of
+                                   the work list split at mesh boundaries),
+                                   so one part's gradient pass overlaps
+                                   another's flux pass; 0 or 1 (default):
+                                   one chain                                */
 } fvm_batch_caps;
 
 int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *caps,
@@ -359,7 +360,8 @@ int64_t fvm_batch_launch_count(fvm_batch *b);
  * ms_per_iter[i] (i < max) receives candidate i's device time per
  * iteration (0 for a candidate that does not fit), *choice the candidate
  * kept: 0 bulk, 1 loads, 2 per vertex, 3 fused, 4 bulk (FP32) or loads
- * (FP64) with the two overlapped chains, 5 fused with the two chains. */
+ * (FP64) in two overlapped chains, 5 fused in two chains, 6 and 7 as 4 in
+ * four and eight chains. */
 int32_t fvm_batch_tune(fvm_batch *b, int32_t iters, int32_t max, double *ms_per_iter,
                        int32_t *choice);
 /* Sets the form of the iteration to a candidate of fvm_batch_tune (the
