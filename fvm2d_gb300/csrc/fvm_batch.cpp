@@ -495,7 +495,11 @@ int32_t enqueue_iteration(fvm_batch *b, bool with_events) {
   auto stages = [&](const ArenaPtrs<R> &Ap, const LaunchCfg &cp, cudaEvent_t fork) -> int32_t {
     cudaStream_t st = cp.stream;
     for (int s = 1; s <= 3; s++) {
-      if (visc) {
+      // viscosity (and at stage 1 the viscous time step); with separate
+      // passes, stages 2 and 3 take the viscosity the previous flux pass
+      // computed from its output (the fused pass reads halo viscosities
+      // while other CTAs update theirs, so it keeps the viscosity pass)
+      if (visc && (s == 1 || b->fused)) {
         FVM_TRY(b, mark(K_VISC, st));
         FVM_TRY(b, launch_visc(Ap, cp, s, s == 1, 0));
         FVM_TRY(b, done(st));

@@ -154,6 +154,16 @@ __device__ __forceinline__ R v_drmin(const ArenaPtrs<R> &A, int v) {
   else return A.drmin[v];
 }
 
+// viscosity.f for the state a stage has just produced, which the next stage
+// of the iteration starts from (what k_visc would compute at that stage)
+template <typename R>
+__device__ __forceinline__ void next_viscosity(const ArenaPtrs<R> &A, const MeshConst &mc,
+                                               const MeshCtl &ctl, int v, const R4<R> &pn) {
+  const R mul = sutherland_viscosity<R>(mc, pn.x, pn.w);
+  A.mul[v] = mul;
+  A.mu[v] = mc.iflow == 2 ? mul : mul + mu_turb<R>(mc, mul, pn.x, A.nut[ctl.nphase][v]);
+}
+
 template <typename R>
 __global__ void __launch_bounds__(kBlockVerts) k_visc(ArenaPtrs<R> A, int stage, int do_dt,
                                                       int routine) {
@@ -253,19 +263,24 @@ __device__ __forceinline__ TriVisc<R> tri_visc(const ArenaPtrs<R> &A, const Mesh
   const R eyt = en1 * dbyy[0] + en2 * dbyy[1] + en3 * dbyy[2];
   const R um = (p1.y + p2.y + p3.y) / R(3);
   const R vm = (p1.z + p2.z + p3.z) / R(3);
-  const R mut = (A.mu[t.x] + A.mu[t.y] + A.mu[t.z]) / R(3);
   const R mult = (A.mul[t.x] + A.mul[t.y] + A.mul[t.z]) / R(3);
-  const R prim5t = (A.nut[nbuf][t.x] + A.nut[nbuf][t.y] + A.nut[nbuf][t.z]) / R(3);
-  const R rhot = (p1.x + p2.x + p3.x) / R(3);
-  const R chi = prim5t * rhot / mult;
-  const R chi3 = cube(chi);
-  const R fv1 = chi3 / (chi3 + MCR(R, cv11));
+  // laminar meshes: mu = mul and nu~ = 0 exactly (viscosity.f, initialize.f),
+  // so the turbulent heat-flux term is exactly zero and mu, nu~ need no loads
+  R mut = mult, tterm = R(0);
+  if (mc.iflow == 3) {
+    mut = (A.mu[t.x] + A.mu[t.y] + A.mu[t.z]) / R(3);
+    const R prim5t = (A.nut[nbuf][t.x] + A.nut[nbuf][t.y] + A.nut[nbuf][t.z]) / R(3);
+    const R rhot = (p1.x + p2.x + p3.x) / R(3);
+    const R chi = prim5t * rhot / mult;
+    const R chi3 = cube(chi);
+    const R fv1 = chi3 / (chi3 + MCR(R, cv11));
+    tterm = rhot * prim5t * fv1 / MCR(R, prandtl_turb);
+  }
   TriVisc<R> o;
   o.txx = n2b3 * mut * (R(2) * ts.dxt[1] - ts.dyt[2]);
   o.txy = mut * (ts.dyt[1] + ts.dxt[2]);
   o.tyy = n2b3 * mut * (R(2) * ts.dyt[2] - ts.dxt[1]);
-  const R gpr = MCR(R, gamma) * (mult / MCR(R, prandtl) + rhot * prim5t * fv1 / MCR(R, prandtl_turb)) /
-                MCR(R, gamma1);
+  const R gpr = MCR(R, gamma) * (mult / MCR(R, prandtl) + tterm) / MCR(R, gamma1);
   o.efx = o.txx * um + o.txy * vm + gpr * ext;
   o.efy = o.txy * um + o.tyy * vm + gpr * eyt;
   o.areat = areat;
@@ -932,6 +947,8 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_FLUX_MINB32 
         const bool noslip = (mc.iflow != 1) && (A.vflag[v] & kVtxSolid);
         const R4<R> pn = rk_update<R>(mc, irk, po, pc, A.dt[v], v_cvarea(A, v), acc, noslip);
         A.st[out_buf(p, stage)][v] = pn;
+        // iterate mode: stages 2 and 3 start from the viscosity computed here
+        if (!routine && stage < 3 && mc.iflow != 1) next_viscosity<R>(A, mc, ctl, v, pn);
         if (stage == 3) {
           // conres.f:14-22 partials and check_positivity.f:13-14 (rho, p)
           have = true;
