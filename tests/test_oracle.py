@@ -141,3 +141,36 @@ def test_bugcompat_switches_change_results(oracle_lib, small_grid):
     a.iterate(3)
     b.iterate(3)
     assert not np.array_equal(a.d("nut"), b.d("nut"))
+
+
+GOLDEN = __import__("os").path.join(__import__("os").path.dirname(__file__), "golden")
+
+
+@pytest.mark.parametrize("name", ["euler_160x48_roe", "laminar_64x24_roe"])
+def test_oracle_reproduces_golden_history(oracle_lib, name):
+    """tests/golden/ fixtures (written by tests/golden/make_golden.py):
+    RES.DAT columns and final-state checksums.  Exact up to libm (the
+    laminar case calls pow)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", f"{GOLDEN}/make_golden.py")
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    ref = np.load(f"{GOLDEN}/{name}.npz")
+    got = mg.run_case(name)
+    tol = 0.0 if name.startswith("euler") else 1e-12
+    assert int(got["status"]) == int(ref["status"]) == 0
+    np.testing.assert_array_equal(got["iresi"], ref["iresi"])
+    for k in ("fres", "fresi", "cl", "cd", "prim_sum", "prim_sq", "prim_first"):
+        np.testing.assert_allclose(got[k], ref[k], rtol=tol, atol=0, err_msg=k)
+
+
+def test_oracle_reproduces_golden_fluxes(oracle_lib):
+    ref = np.load(f"{GOLDEN}/fluxes.npz")
+    g = naca_ogrid(20, 8)
+    for iflux, bugcompat, key, tol in ((1, 1, "roe", 0.0), (2, 1, "kfvs", 1e-13),
+                                       (3, 0, "hllc", 1e-13)):
+        o = oracle_lib.Oracle(g.coord, g.elem, g.ptype, iflux=iflux, bugcompat=bugcompat)
+        for k in range(len(ref["ds"])):
+            st, f = o.flux(iflux, ref["ds"][k], ref["priml"][k], ref["primr"][k])
+            assert st == ref[key + "_status"][k]
+            np.testing.assert_allclose(f, ref[key][k], rtol=tol, atol=1e-300, err_msg=key)
