@@ -29,6 +29,11 @@ __device__ __forceinline__ double mexp(double x) { return exp(x); }
 __device__ __forceinline__ float mpow(float x, float y) { return __powf(x, y); }
 __device__ __forceinline__ double mpow(double x, double y) { return pow(x, y); }
 __device__ __forceinline__ float mfabs(float x) { return fabsf(x); }
+// Division: IEEE in FP64; in FP32 the two-instruction approximation
+// (reciprocal and multiply; the divisors here are states, limiter sums and
+// sound speeds, far from the range where it loses accuracy)
+__device__ __forceinline__ float mdiv(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double mdiv(double a, double b) { return a / b; }
 __device__ __forceinline__ double mfabs(double x) { return fabs(x); }
 
 // Fortran dmin1/dmax1 on non-NaN operands
@@ -62,7 +67,7 @@ template <>
 __device__ __forceinline__ float limit_albada<float>(float ul, float ur, float eps) {
   const float top = (sq(ul) + eps) * ur + (sq(ur) + eps) * ul;
   const float bot = sq(ul) + sq(ur) + 2.0f * eps;
-  const float r = top / bot;
+  const float r = __fdividef(top, bot);
   return (ul * ur <= 0.0f) ? 0.0f : r;
 }
 
@@ -96,20 +101,20 @@ template <typename R>
 __device__ __forceinline__ bool roe_flux(R ct, R st, R length, const R pl4[4], const R pr4[4],
                                          R GAMMA, R GAMMA1, R flux[4]) {
   R rl = pl4[0], ul = pl4[1], vl = pl4[2], pl = pl4[3];
-  R al2 = GAMMA * pl / rl;
+  R al2 = mdiv(GAMMA * pl, rl);
   R ql2 = sq(ul) + sq(vl);
-  R hl = al2 / GAMMA1 + R(0.5) * ql2;
+  R hl = mdiv(al2, GAMMA1) + R(0.5) * ql2;
   R rr = pr4[0], ur = pr4[1], vr = pr4[2], pr = pr4[3];
-  R ar2 = GAMMA * pr / rr;
+  R ar2 = mdiv(GAMMA * pr, rr);
   R qr2 = sq(ur) + sq(vr);
-  R hr = ar2 / GAMMA1 + R(0.5) * qr2;
+  R hr = mdiv(ar2, GAMMA1) + R(0.5) * qr2;
   R unl = ul * ct + vl * st;
   R Fc0 = rl * unl;
   R Fc1 = pl * ct + rl * ul * unl;
   R Fc2 = pl * st + rl * vl * unl;
   R Fc3 = rl * hl * unl;
   R rl12 = msqrt(rl), rr12 = msqrt(rr);
-  R rd = R(1) / (rl12 + rr12);
+  R rd = mdiv(R(1), rl12 + rr12);
   R ua = (ul * rl12 + ur * rr12) * rd;
   R va = (vl * rl12 + vr * rr12) * rd;
   R ha = (hl * rl12 + hr * rr12) * rd;
@@ -126,13 +131,13 @@ __device__ __forceinline__ bool roe_flux(R ct, R st, R length, const R pl4[4], c
   R du1 = rr - rl;
   R du2 = rr * ur - rl * ul;
   R du3 = rr * vr - rl * vl;
-  R du4 = (pr - pl) / GAMMA1 + R(0.5) * (rr * qr2 - rl * ql2);
-  R m1 = (ct * du2 + st * du3 - una * du1) / aa;
-  R m2 = GAMMA1 * (du4 - ua * du2 - va * du3 + qa2 * du1) / sq(aa);
+  R du4 = mdiv(pr - pl, GAMMA1) + R(0.5) * (rr * qr2 - rl * ql2);
+  R m1 = mdiv(ct * du2 + st * du3 - una * du1, aa);
+  R m2 = mdiv(GAMMA1 * (du4 - ua * du2 - va * du3 + qa2 * du1), sq(aa));
   R a4 = R(0.5) * (m1 + m2);
   R a1 = R(0.5) * (m2 - m1);
   R a3 = du1 - a1 - a4;
-  R a2 = (st * du2 - ct * du3 + vna * du1) / aa;
+  R a2 = mdiv(st * du2 - ct * du3 + vna * du1, aa);
   R a1l1 = a1 * l1, a2l2 = a2 * l2, a3l3 = a3 * l3, a4l4 = a4 * l4;
   R aact = aa * ct, aast = aa * st;
   R Fd0 = a1l1 + a3l3 + a4l4;
