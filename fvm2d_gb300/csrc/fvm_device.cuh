@@ -157,26 +157,26 @@ __device__ __forceinline__ void kfvs_flux(R ct, R st, R length, const R pl4[4], 
                                           R GAMMA1, R PI, R flux[4]) {
   R rl = pl4[0], ul = pl4[1], vl = pl4[2], pl = pl4[3];
   R ql2 = sq(ul) + sq(vl);
-  R el = pl / GAMMA1 + R(0.5) * rl * ql2;
+  R el = mdiv(pl, GAMMA1) + R(0.5) * rl * ql2;
   R rr = pr4[0], ur = pr4[1], vr = pr4[2], pr = pr4[3];
   R qr2 = sq(ur) + sq(vr);
-  R er = pr / GAMMA1 + R(0.5) * rr * qr2;
+  R er = mdiv(pr, GAMMA1) + R(0.5) * rr * qr2;
   R unl = ul * ct + vl * st;
   R unr = ur * ct + vr * st;
   R vnl = -ul * st + vl * ct;
   R vnr = -ur * st + vr * ct;
-  R betal = R(0.5) * rl / pl;
+  R betal = mdiv(R(0.5) * rl, pl);
   R sl = unl * msqrt(betal);
   R Al = R(0.5) * (R(1) + merf(sl));
-  R Bl = R(0.5) * mexp(-sq(sl)) / msqrt(PI * betal);
+  R Bl = mdiv(R(0.5) * mexp(-sq(sl)), msqrt(PI * betal));
   R Fp0 = rl * (unl * Al + Bl);
   R Fp1 = (pl + rl * sq(unl)) * Al + rl * unl * Bl;
   R Fp2 = rl * (unl * Al + Bl) * vnl;
   R Fp3 = (el + pl) * unl * Al + (el + R(0.5) * pl) * Bl;
-  R betar = R(0.5) * rr / pr;
+  R betar = mdiv(R(0.5) * rr, pr);
   R sr = unr * msqrt(betar);
   R Ar = R(0.5) * (R(1) - merf(sr));
-  R Br = R(0.5) * mexp(-sq(sr)) / msqrt(PI * betar);
+  R Br = mdiv(R(0.5) * mexp(-sq(sr)), msqrt(PI * betar));
   R Fm0 = rr * (unr * Ar - Br);
   R Fm1 = (pr + rr * sq(unr)) * Ar - rr * unr * Br;
   R Fm2 = rr * (unr * Ar - Br) * vnr;
@@ -198,18 +198,18 @@ __device__ __forceinline__ void hllc_flux(R ct, R st, R length, const R pl4[4], 
   R ul = pl4[1] * ct + pl4[2] * st;
   R vl = -pl4[1] * st + pl4[2] * ct;
   R pl = pl4[3];
-  R al = msqrt(gamma * pl / rl);
-  R El = pl / GAMMA1 + R(0.5) * rl * (sq(ul) + sq(vl));
+  R al = msqrt(mdiv(gamma * pl, rl));
+  R El = mdiv(pl, GAMMA1) + R(0.5) * rl * (sq(ul) + sq(vl));
   R rr = pr4[0];
   R ur = pr4[1] * ct + pr4[2] * st;
   R vr = -pr4[1] * st + pr4[2] * ct;
   R pr = pr4[3];
-  R ar = msqrt(gamma * pr / rr);
-  R Er = pr / GAMMA1 + R(0.5) * rr * (sq(ur) + sq(vr));
+  R ar = msqrt(mdiv(gamma * pr, rr));
+  R Er = mdiv(pr, GAMMA1) + R(0.5) * rr * (sq(ur) + sq(vr));
   R rbar = R(0.5) * (rl + rr);
   R abar = R(0.5) * (al + ar);
   R Ppv = R(0.5) * (pl + pr - (ur - ul) * rbar * abar);
-  R Upv = R(0.5) * (ul + ur - (pr - pl) / (rbar * abar));
+  R Upv = R(0.5) * (ul + ur - mdiv(pr - pl, rbar * abar));
   R prmax, prmin;
   if (pl > pr) {
     prmax = pl;
@@ -218,7 +218,7 @@ __device__ __forceinline__ void hllc_flux(R ct, R st, R length, const R pl4[4], 
     prmax = pr;
     prmin = pl;
   }
-  R Q = prmax / prmin;
+  R Q = mdiv(prmax, prmin);
   R pstar, ustar;
   if (Q < R(2) && prmin < Ppv && Ppv < prmax) {
     pstar = Ppv;
@@ -245,8 +245,8 @@ __device__ __forceinline__ void hllc_flux(R ct, R st, R length, const R pl4[4], 
     pstar = a1 / a2;
     ustar = R(0.5) * (ul + ur + (pstar - pr) * gr - (pstar - pl) * gl);
   }
-  R ql = (pstar <= pl) ? R(1) : msqrt(R(1) + R(0.5) * (gamma + R(1)) * (pstar / pl - R(1)) / gamma);
-  R qr = (pstar <= pr) ? R(1) : msqrt(R(1) + R(0.5) * (gamma + R(1)) * (pstar / pr - R(1)) / gamma);
+  R ql = (pstar <= pl) ? R(1) : msqrt(R(1) + mdiv(R(0.5) * (gamma + R(1)) * (mdiv(pstar, pl) - R(1)), gamma));
+  R qr = (pstar <= pr) ? R(1) : msqrt(R(1) + mdiv(R(0.5) * (gamma + R(1)) * (mdiv(pstar, pr) - R(1)), gamma));
   R Sl = ul - al * ql;
   R Ss = ustar;
   R Sr = ur + ar * qr;
@@ -258,11 +258,11 @@ __device__ __forceinline__ void hllc_flux(R ct, R st, R length, const R pl4[4], 
     f3 = (El + pl) * ul;
   } else if (Sl <= R(0) && R(0) <= Ss) {
     R fl0 = rl * ul, fl1 = pl + rl * sq(ul), fl2 = rl * ul * vl, fl3 = (El + pl) * ul;
-    R fact = rl * (Sl - ul) / (Sl - Ss);
+    R fact = mdiv(rl * (Sl - ul), Sl - Ss);
     R du0 = fact - rl;
     R du1 = fact * Ss - rl * ul;
     R du2 = fact * vl - rl * vl;
-    R t1 = El / rl + (Ss - ul) * (Ss + pl / rl / (Sl - ul));
+    R t1 = mdiv(El, rl) + (Ss - ul) * (Ss + mdiv(mdiv(pl, rl), Sl - ul));
     R du3 = fact * t1 - El;
     f0 = fl0 + Sl * du0;
     f1 = fl1 + Sl * du1;
@@ -270,11 +270,11 @@ __device__ __forceinline__ void hllc_flux(R ct, R st, R length, const R pl4[4], 
     f3 = fl3 + Sl * du3;
   } else if (Ss <= R(0) && R(0) <= Sr) {
     R fr0 = rr * ur, fr1 = pr + rr * sq(ur), fr2 = rr * ur * vr, fr3 = (Er + pr) * ur;
-    R fact = rr * (Sr - ur) / (Sr - Ss);
+    R fact = mdiv(rr * (Sr - ur), Sr - Ss);
     R du0 = fact - rr;
     R du1 = fact * Ss - rr * ur;
     R du2 = fact * vr - rr * vr;
-    R t1 = Er / rr + (Ss - ur) * (Ss + pr / rr / (Sr - ur));
+    R t1 = mdiv(Er, rr) + (Ss - ur) * (Ss + mdiv(mdiv(pr, rr), Sr - ur));
     R du3 = fact * t1 - Er;
     f0 = fr0 + Sr * du0;
     f1 = fr1 + Sr * du1;
@@ -433,13 +433,13 @@ __device__ __forceinline__ R mu_turb(const MeshConst &mc, R mu_lam, R density, R
 template <typename R>
 __device__ __forceinline__ R time_step(const MeshConst &mc, const R4<R> &P, R mu, R drmin) {
   R q = msqrt(sq(P.y) + sq(P.z));
-  R a = msqrt(MCR(R, gamma) * P.w / P.x);
+  R a = msqrt(mdiv(MCR(R, gamma) * P.w, P.x));
   R dr = drmin;
   if (mc.iflow != 1) {
-    R dtv = R(2) * MCR(R, gamma) * mu / (P.x * MCR(R, prandtl));
-    return MCR(R, cfl) * sq(dr) / (dr * (q + a) + dtv);
+    R dtv = mdiv(R(2) * MCR(R, gamma) * mu, P.x * MCR(R, prandtl));
+    return mdiv(MCR(R, cfl) * sq(dr), dr * (q + a) + dtv);
   }
-  return MCR(R, cfl) * dr / (q + a);
+  return mdiv(MCR(R, cfl) * dr, q + a);
 }
 
 // ---------------------------------------------------- update.f, convert.f
@@ -448,7 +448,7 @@ __device__ __forceinline__ void prim2con(const R4<R> &P, R gamma1, R c[4]) {
   c[0] = P.x;
   c[1] = P.x * P.y;
   c[2] = P.x * P.z;
-  c[3] = P.w / gamma1 + R(0.5) * P.x * (sq(P.y) + sq(P.z));
+  c[3] = mdiv(P.w, gamma1) + R(0.5) * P.x * (sq(P.y) + sq(P.z));
 }
 
 template <typename R>
@@ -460,7 +460,7 @@ __device__ __forceinline__ R4<R> rk_update(const MeshConst &mc, int irk, const R
   R c0[4], c1[4], cn[4];
   prim2con(Po, gamma1, c0);
   prim2con(Pc, gamma1, c1);
-  R f = dt / cvarea;
+  R f = mdiv(dt, cvarea);
 #pragma unroll
   for (int j = 0; j < 4; j++) cn[j] = a * c0[j] + b * (c1[j] - f * res[j]);
   if (noslip) {
@@ -469,9 +469,9 @@ __device__ __forceinline__ R4<R> rk_update(const MeshConst &mc, int irk, const R
   }
   R4<R> out;
   out.x = cn[0];
-  out.y = cn[1] / cn[0];
-  out.z = cn[2] / cn[0];
-  out.w = gamma1 * (cn[3] - R(0.5) * (sq(cn[1]) + sq(cn[2])) / cn[0]);
+  out.y = mdiv(cn[1], cn[0]);
+  out.z = mdiv(cn[2], cn[0]);
+  out.w = gamma1 * (cn[3] - mdiv(R(0.5) * (sq(cn[1]) + sq(cn[2])), cn[0]));
   return out;
 }
 

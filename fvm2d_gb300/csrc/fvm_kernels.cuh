@@ -258,12 +258,12 @@ __device__ __forceinline__ TriVisc<R> tri_visc(const ArenaPtrs<R> &A, const Mesh
                                                const R4<R> &p3, const R dbxx[3],
                                                const R dbyy[3], const TriSmem<R> &ts) {
   const R n2b3 = R(2) / R(3);
-  const R en1 = p1.w / p1.x, en2 = p2.w / p2.x, en3 = p3.w / p3.x;
+  const R en1 = mdiv(p1.w, p1.x), en2 = mdiv(p2.w, p2.x), en3 = mdiv(p3.w, p3.x);
   const R ext = en1 * dbxx[0] + en2 * dbxx[1] + en3 * dbxx[2];
   const R eyt = en1 * dbyy[0] + en2 * dbyy[1] + en3 * dbyy[2];
-  const R um = (p1.y + p2.y + p3.y) / R(3);
-  const R vm = (p1.z + p2.z + p3.z) / R(3);
-  const R mult = (A.mul[t.x] + A.mul[t.y] + A.mul[t.z]) / R(3);
+  const R um = mdiv(p1.y + p2.y + p3.y, R(3));
+  const R vm = mdiv(p1.z + p2.z + p3.z, R(3));
+  const R mult = mdiv(A.mul[t.x] + A.mul[t.y] + A.mul[t.z], R(3));
   // laminar meshes: mu = mul and nu~ = 0 exactly (viscosity.f, initialize.f),
   // so the turbulent heat-flux term is exactly zero and mu, nu~ need no loads
   R mut = mult, tterm = R(0);
@@ -280,7 +280,7 @@ __device__ __forceinline__ TriVisc<R> tri_visc(const ArenaPtrs<R> &A, const Mesh
   o.txx = n2b3 * mut * (R(2) * ts.dxt[1] - ts.dyt[2]);
   o.txy = mut * (ts.dyt[1] + ts.dxt[2]);
   o.tyy = n2b3 * mut * (R(2) * ts.dyt[2] - ts.dxt[1]);
-  const R gpr = MCR(R, gamma) * (mult / MCR(R, prandtl) + tterm) / MCR(R, gamma1);
+  const R gpr = mdiv(MCR(R, gamma) * (mdiv(mult, MCR(R, prandtl)) + tterm), MCR(R, gamma1));
   o.efx = o.txx * um + o.txy * vm + gpr * ext;
   o.efy = o.txy * um + o.tyy * vm + gpr * eyt;
   o.areat = areat;
