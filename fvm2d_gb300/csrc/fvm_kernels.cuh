@@ -1473,12 +1473,23 @@ __device__ void conres_block(const ArenaPtrs<R> &A, const MeshConst &mc, double 
   __shared__ int s_a[kMonitorMaxThreads];
   double s = 0.0, m = 0.0;
   int a = INT_MAX;
-  for (int i = threadIdx.x; i < mc.nblk; i += blockDim.x) {
-    const BlockPartial bp = A.part[A.blocks[mc.blk0 + i].part];
-    s += bp.sumsq;
-    if (bp.maxabs > m || (bp.maxabs == m && bp.argmax < a)) {
-      m = bp.maxabs;
-      a = bp.argmax;
+  // the mesh's partials are contiguous (block k's record is blk0 + k);
+  // four loads in flight per thread, folded in index order
+  for (int i0 = threadIdx.x; i0 < mc.nblk; i0 += 4 * blockDim.x) {
+    BlockPartial bp[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const int i = i0 + u * (int)blockDim.x;
+      if (i < mc.nblk) bp[u] = A.part[mc.blk0 + i];
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      if (i0 + u * (int)blockDim.x >= mc.nblk) break;
+      s += bp[u].sumsq;
+      if (bp[u].maxabs > m || (bp[u].maxabs == m && bp[u].argmax < a)) {
+        m = bp[u].maxabs;
+        a = bp[u].argmax;
+      }
     }
   }
   s_s[threadIdx.x] = s;
