@@ -521,9 +521,10 @@ def run_serve(args):
     from fvm2d_gb300 import serve
     torch.cuda.init()
     reqs = serve.generate_requests(n=args.requests, rate=args.rate, seed=args.seed)
-    srv = serve.Server(vertices=args.arena_vertices, meshes=512, chunk=args.chunk,
-                       workers=args.workers, max_iter=args.max_iter, minres=args.minres,
-                       tune_every=args.tune_every)
+    cls = serve.NativeServer if args.service == "native" else serve.Server
+    srv = cls(vertices=args.arena_vertices, meshes=512, chunk=args.chunk,
+              workers=args.workers, max_iter=args.max_iter, minres=args.minres,
+              tune_every=args.tune_every)
     res, stats = srv.run(reqs)
     srv.close()
     acc = fp64_accuracy(reqs, res)
@@ -538,7 +539,7 @@ def run_serve(args):
                                    "5k-400k vertices log-uniform, 70% Euler / 30% laminar, "
                                    f"stop at drop {args.minres} or {args.max_iter} iterations",
                        "arena_vertices": args.arena_vertices, "chunk": args.chunk,
-                       "tune_every_steps": args.tune_every},
+                       "tune_every_steps": args.tune_every, "service": args.service},
             "latency_s": {"p50": stats["p50_latency_s"], "p99": stats["p99_latency_s"]},
             "stats": stats,
             "vs_fp64_gpu": {"solves_per_s": solves64, "ratio": stats["solves_per_s"] / solves64,
@@ -714,6 +715,8 @@ def main():
     ap.add_argument("--workers", type=int, default=8)
     ap.add_argument("--max-iter", type=int, default=5000)
     ap.add_argument("--minres", type=float, default=1e-6)
+    ap.add_argument("--service", choices=["python", "native"], default="python",
+                    help="serving loop: serve.Server (Python) or the C++ fvm_serve_* service")
     ap.add_argument("--tune-every", type=int, default=40,
                     help="serving: re-run the autotuner every N steps (0: never)")
     args = ap.parse_args()

@@ -120,6 +120,17 @@ SIGNATURES = {
     "fvm_batch_launch_count": (C.c_int64, [C.c_void_p]),
     "fvm_batch_tune": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, _pd, _pi]),
     "fvm_batch_set_form": (C.c_int32, [C.c_void_p, C.c_int32]),
+    "fvm_serve_create": (C.c_int32, [C.c_int32, C.c_void_p, C.c_int32, C.c_int32,
+                                     C.POINTER(C.c_void_p)]),
+    "fvm_serve_submit": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_double,
+                                     C.c_int32, C.POINTER(C.c_int64)]),
+    "fvm_serve_poll": (C.c_int32, [C.c_void_p, C.c_int64, _pi]),
+    "fvm_serve_wait": (C.c_int32, [C.c_void_p, C.c_int64, C.c_double, _pi]),
+    "fvm_serve_result": (C.c_int32, [C.c_void_p, C.c_int64, _pi, _pi, _pd, _pd, _pd, _pd]),
+    "fvm_serve_state": (C.c_int32, [C.c_void_p, C.c_int64, _pd, _pd]),
+    "fvm_serve_release": (C.c_int32, [C.c_void_p, C.c_int64]),
+    "fvm_serve_stats": (C.c_int32, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "fvm_serve_destroy": (C.c_int32, [C.c_void_p]),
     "fvm_layout_stats": (C.c_int32, [C.POINTER(FvmMesh), C.POINTER(C.c_int64)]),
     "fvm_gpu_conres_noalloc": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, _pd,
                                            _pd, _pd, _pi]),

@@ -44,6 +44,7 @@ UNITS = [
     ("fvm_setup.cu", "nvcc", ["--fmad=false"]),
     ("fvm_noalloc.cu", "nvcc", ["--fmad=false"]),
     ("fvm_batch.cpp", "cxx", []),
+    ("fvm_serve.cpp", "cxx", []),
     ("fvm_layout.cpp", "cxx", []),
     ("fvm_geometry.cpp", "cxx", []),
 ]

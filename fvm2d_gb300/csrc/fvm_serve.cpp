@@ -1,0 +1,338 @@
+// fvm_serve.cpp -- continuous-batching service of steady solves on one GPU,
+// in native code on top of the batch API (no counterpart in the reference,
+// whose driver runs one solve per process: main.f:42-76).
+//
+// Callers submit solves from any thread (the block layout is built on the
+// submitting thread, so several submitters prepare requests in parallel);
+// one service thread owns the batch arena and loops:
+//   admit   queued solves in arrival order while the arena has room (a solve
+//           that does not fit an empty arena is refused with
+//           FVM_ERR_CAPACITY);
+//   step    every resident solve `chunk` iterations (one CUDA graph launch
+//           per iteration, every mesh in each kernel);
+//   retire  solves that reached their residual drop or iteration cap
+//           (main.f:42) or stopped with a status: results (and the final
+//           state when asked) are kept for the caller, the arena ranges
+//           freed;
+// and, when asked, re-runs the autotuner every `tune_every` steps.
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <new>
+#include <thread>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/fvm_gpu.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Ticket {
+  int state = 0;                 // 0 queued, 1 running, 2 done
+  fvm_prepared *prep = nullptr;
+  int32_t np = 0, nmax = 0, slot = -1;
+  double minres = 0.0;
+  bool keep_state = false;
+  Clock::time_point t_submit, t_admit, t_done;
+  int32_t status = FVM_OK, niter = 0;
+  double fres = 0.0, cl = 0.0, cd = 0.0;
+  std::vector<double> prim, nut;
+};
+
+double seconds(Clock::time_point a, Clock::time_point b) {
+  return std::chrono::duration<double>(b - a).count();
+}
+
+}  // namespace
+
+struct fvm_server {
+  fvm_batch *b = nullptr;
+  int device = 0;
+  int32_t chunk = 50, tune_every = 0;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<int64_t> queue;            // prepared, waiting for admission
+  std::map<int64_t, Ticket> tickets;
+  std::map<int32_t, int64_t> resident;  // slot -> ticket (service thread only)
+  int64_t next_id = 1, submitted = 0, done = 0, steps = 0;
+  int32_t error = FVM_OK;               // a CUDA failure stops the service
+  bool stop = false;
+  std::thread worker;
+};
+
+namespace {
+
+void finish(fvm_server *s, int64_t id, Ticket &t, int32_t status) {
+  t.status = status;
+  t.state = 2;
+  t.t_done = Clock::now();
+  s->done++;
+  (void)id;
+}
+
+// Moves every resident solve that stopped to the done state.
+int32_t retire(fvm_server *s) {
+  std::vector<std::pair<int32_t, int64_t>> res(s->resident.begin(), s->resident.end());
+  for (const auto &r : res) {
+    int32_t active = 0, niter = 0, status = 0, bad = 0;
+    double fres = 0, cl = 0, cd = 0;
+    int32_t st = fvm_batch_poll(s->b, r.first, &active, &niter, &fres, &cl, &cd, &status, &bad);
+    if (st) return st;
+    if (active) continue;
+    std::vector<double> prim, nut;
+    bool keep;
+    int32_t np;
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      keep = s->tickets[r.second].keep_state;
+      np = s->tickets[r.second].np;
+    }
+    if (keep) {
+      prim.resize(4 * (size_t)np);
+      nut.resize(np);
+      std::vector<double> mul(np), mu(np), qx(4 * (size_t)np), qy(4 * (size_t)np);
+      st = fvm_batch_get_state(s->b, r.first, prim.data(), nut.data(), mul.data(), mu.data(),
+                               qx.data(), qy.data());
+      if (st) return st;
+    }
+    if ((st = fvm_batch_remove(s->b, r.first))) return st;
+    s->resident.erase(r.first);
+    std::lock_guard<std::mutex> lk(s->mu);
+    Ticket &t = s->tickets[r.second];
+    t.niter = niter;
+    t.fres = fres;
+    t.cl = cl;
+    t.cd = cd;
+    t.prim.swap(prim);
+    t.nut.swap(nut);
+    finish(s, r.second, t, status);
+  }
+  return FVM_OK;
+}
+
+// Admits queued solves in arrival order while they fit.
+int32_t admit(fvm_server *s) {
+  for (;;) {
+    int64_t id;
+    fvm_prepared *prep;
+    int32_t nmax;
+    double minres;
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      if (s->queue.empty()) return FVM_OK;
+      id = s->queue.front();
+      Ticket &t = s->tickets[id];
+      prep = t.prep;
+      nmax = t.nmax;
+      minres = t.minres;
+    }
+    int32_t slot = -1;
+    int32_t st = fvm_batch_add_prepared(s->b, prep, &slot);
+    std::lock_guard<std::mutex> lk(s->mu);
+    Ticket &t = s->tickets[id];
+    if (st == FVM_ERR_CAPACITY && !s->resident.empty()) return FVM_OK;   // waits for room
+    s->queue.pop_front();
+    if (st) {                  // too large for an empty arena, or bad input
+      fvm_prepared_free(prep);
+      t.prep = nullptr;
+      finish(s, id, t, st);
+      s->cv_done.notify_all();
+      if (st == FVM_ERR_CUDA) return st;
+      continue;
+    }
+    t.prep = nullptr;          // taken by the batch
+    t.slot = slot;
+    t.state = 1;
+    t.t_admit = Clock::now();
+    s->resident[slot] = id;
+    if ((st = fvm_batch_start(s->b, slot, nmax, minres))) return st;
+  }
+}
+
+void service(fvm_server *s) {
+  cudaSetDevice(s->device);
+  int32_t st = FVM_OK;
+  for (;;) {
+    {
+      std::unique_lock<std::mutex> lk(s->mu);
+      if (s->stop) break;
+      if (s->queue.empty() && s->resident.empty()) {
+        s->cv_work.wait_for(lk, std::chrono::milliseconds(20));
+        continue;
+      }
+    }
+    if ((st = admit(s))) break;
+    if (s->resident.empty()) continue;
+    if (s->tune_every > 0 && s->steps % s->tune_every == 0) {
+      int32_t choice = 0;
+      if ((st = fvm_batch_tune(s->b, 2, 0, nullptr, &choice))) break;
+    }
+    if ((st = fvm_batch_step(s->b, s->chunk))) break;
+    s->steps++;
+    if ((st = retire(s))) break;
+    s->cv_done.notify_all();
+  }
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (st) {                   // the service cannot continue: fail what is left
+    s->error = st;
+    for (auto &kv : s->tickets)
+      if (kv.second.state != 2) finish(s, kv.first, kv.second, st);
+  }
+  s->cv_done.notify_all();
+}
+
+}  // namespace
+
+extern "C" int32_t fvm_serve_create(int32_t precision, const fvm_batch_caps *caps,
+                                    int32_t chunk, int32_t tune_every, fvm_server **out) {
+  if (!caps || !out || chunk < 1 || tune_every < 0) return FVM_ERR_ARG;
+  *out = nullptr;
+  fvm_server *s = new (std::nothrow) fvm_server();
+  if (!s) return FVM_ERR_NOMEM;
+  int32_t st = fvm_batch_create(precision, caps, &s->b);
+  if (st) {
+    delete s;
+    return st;
+  }
+  cudaGetDevice(&s->device);
+  s->chunk = chunk;
+  s->tune_every = tune_every;
+  try {
+    s->worker = std::thread(service, s);
+  } catch (...) {
+    fvm_batch_destroy(s->b);
+    delete s;
+    return FVM_ERR_NOMEM;
+  }
+  *out = s;
+  return FVM_OK;
+}
+
+extern "C" int32_t fvm_serve_submit(fvm_server *s, const fvm_params *p, const fvm_mesh *m,
+                                    int32_t nmax, double minres, int32_t keep_state,
+                                    int64_t *ticket) {
+  if (!s || !p || !m || !ticket || nmax < 1) return FVM_ERR_ARG;
+  *ticket = 0;
+  fvm_prepared *prep = nullptr;
+  const int32_t st = fvm_batch_prepare(p, m, &prep);   // on the caller's thread
+  if (st) return st;
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (s->stop || s->error) {
+    fvm_prepared_free(prep);
+    return s->error ? s->error : FVM_ERR_STATE;
+  }
+  const int64_t id = s->next_id++;
+  Ticket &t = s->tickets[id];
+  t.prep = prep;
+  t.np = m->np;
+  t.nmax = nmax;
+  t.minres = minres;
+  t.keep_state = keep_state != 0;
+  t.t_submit = Clock::now();
+  s->queue.push_back(id);
+  s->submitted++;
+  s->cv_work.notify_one();
+  *ticket = id;
+  return FVM_OK;
+}
+
+extern "C" int32_t fvm_serve_poll(fvm_server *s, int64_t ticket, int32_t *state) {
+  if (!s || !state) return FVM_ERR_ARG;
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->tickets.find(ticket);
+  if (it == s->tickets.end()) return FVM_ERR_ARG;
+  *state = it->second.state;
+  return FVM_OK;
+}
+
+extern "C" int32_t fvm_serve_wait(fvm_server *s, int64_t ticket, double timeout_s,
+                                  int32_t *state) {
+  if (!s || !state) return FVM_ERR_ARG;
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto it = s->tickets.find(ticket);
+  if (it == s->tickets.end()) return FVM_ERR_ARG;
+  s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s < 0 ? 0 : timeout_s),
+                      [&] { return it->second.state == 2; });
+  *state = it->second.state;
+  return FVM_OK;
+}
+
+extern "C" int32_t fvm_serve_result(fvm_server *s, int64_t ticket, int32_t *status,
+                                    int32_t *niter, double *fres, double *cl, double *cd,
+                                    double *times) {
+  if (!s) return FVM_ERR_ARG;
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->tickets.find(ticket);
+  if (it == s->tickets.end() || it->second.state != 2) return FVM_ERR_ARG;
+  const Ticket &t = it->second;
+  if (status) *status = t.status;
+  if (niter) *niter = t.niter;
+  if (fres) *fres = t.fres;
+  if (cl) *cl = t.cl;
+  if (cd) *cd = t.cd;
+  if (times) {   // queued, resident, total (seconds)
+    const bool ran = t.slot >= 0;
+    times[0] = ran ? seconds(t.t_submit, t.t_admit) : seconds(t.t_submit, t.t_done);
+    times[1] = ran ? seconds(t.t_admit, t.t_done) : 0.0;
+    times[2] = seconds(t.t_submit, t.t_done);
+  }
+  return FVM_OK;
+}
+
+extern "C" int32_t fvm_serve_state(fvm_server *s, int64_t ticket, double *prim, double *nut) {
+  if (!s || !prim) return FVM_ERR_ARG;
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->tickets.find(ticket);
+  if (it == s->tickets.end() || it->second.state != 2 || it->second.prim.empty())
+    return FVM_ERR_ARG;
+  std::memcpy(prim, it->second.prim.data(), it->second.prim.size() * sizeof(double));
+  if (nut) std::memcpy(nut, it->second.nut.data(), it->second.nut.size() * sizeof(double));
+  return FVM_OK;
+}
+
+extern "C" int32_t fvm_serve_release(fvm_server *s, int64_t ticket) {
+  if (!s) return FVM_ERR_ARG;
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->tickets.find(ticket);
+  if (it == s->tickets.end() || it->second.state != 2) return FVM_ERR_ARG;
+  s->tickets.erase(it);
+  return FVM_OK;
+}
+
+extern "C" int32_t fvm_serve_stats(fvm_server *s, int64_t *out) {
+  if (!s || !out) return FVM_ERR_ARG;
+  std::lock_guard<std::mutex> lk(s->mu);
+  int64_t queued = 0, running = 0;
+  for (const auto &kv : s->tickets) {
+    queued += kv.second.state == 0;
+    running += kv.second.state == 1;
+  }
+  out[0] = s->submitted;
+  out[1] = s->done;
+  out[2] = queued;
+  out[3] = running;
+  out[4] = s->steps;
+  out[5] = s->error;
+  return FVM_OK;
+}
+
+extern "C" int32_t fvm_serve_destroy(fvm_server *s) {
+  if (!s) return FVM_OK;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop = true;
+  }
+  s->cv_work.notify_all();
+  if (s->worker.joinable()) s->worker.join();
+  for (auto &kv : s->tickets)
+    if (kv.second.prep) fvm_prepared_free(kv.second.prep);
+  const int32_t st = fvm_batch_destroy(s->b);
+  delete s;
+  return st;
+}

@@ -232,3 +232,125 @@ class Server:
                      tuner_choices={k: self.tunings.count(k) for k in set(self.tunings)})
         stats["vertex_stage_updates_per_s"] = stats["vertex_stage_updates"] / makespan
         return res, stats
+
+
+class NativeServer:
+    """The same service in native code (fvm_serve_* of the C ABI): a C++
+    service thread owns the arena, admits, steps and retires; this class
+    submits the arrivals (preparing them on a thread pool, since submit
+    builds the block layout on the calling thread) and collects results."""
+
+    def __init__(self, vertices: int = 6_000_000, meshes: int = 256, precision: int = L.FP32,
+                 chunk: int = 50, workers: int = 8, max_iter: int = 5000, minres: float = 1e-6,
+                 tune_every: int = 0, **caps):
+        import ctypes as C
+        c = L.FvmBatchCaps()
+        c.vertices, c.meshes, c.viscous = int(vertices), int(meshes), 1
+        for k, v in caps.items():
+            setattr(c, k, int(v))
+        h = C.c_void_p()
+        L.check(L.lib().fvm_serve_create(precision, C.byref(c), chunk, tune_every, C.byref(h)),
+                "fvm_serve_create")
+        self.h = h
+        self.precision = precision
+        self.workers = workers
+        self.max_iter = max_iter
+        self.minres = minres
+        self.chunk = chunk
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            L.lib().fvm_serve_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, params: L.FvmParams, mesh, keep_state: bool = False) -> int:
+        import ctypes as C
+        from .solver import MeshArrays
+        m = mesh if isinstance(mesh, MeshArrays) else MeshArrays(mesh)
+        ms = m.struct()
+        t = C.c_int64(0)
+        L.check(L.lib().fvm_serve_submit(self.h, C.byref(params), C.byref(ms), self.max_iter,
+                                         self.minres, 1 if keep_state else 0, C.byref(t)),
+                "fvm_serve_submit")
+        return t.value
+
+    def wait(self, ticket: int, timeout: float = 3600.0) -> bool:
+        import ctypes as C
+        st = C.c_int32(0)
+        L.check(L.lib().fvm_serve_wait(self.h, ticket, timeout, C.byref(st)), "fvm_serve_wait")
+        return st.value == 2
+
+    def result(self, ticket: int) -> dict:
+        import ctypes as C
+        st, n = C.c_int32(), C.c_int32()
+        f, cl, cd = C.c_double(), C.c_double(), C.c_double()
+        tm = (C.c_double * 3)()
+        L.check(L.lib().fvm_serve_result(self.h, ticket, C.byref(st), C.byref(n), C.byref(f),
+                                         C.byref(cl), C.byref(cd), tm), "fvm_serve_result")
+        return dict(status=st.value, niter=n.value, fres=f.value, cl=cl.value, cd=cd.value,
+                    queued_s=tm[0], resident_s=tm[1], total_s=tm[2])
+
+    def state(self, ticket: int, np_: int) -> dict:
+        prim, nut = np.zeros((np_, 4)), np.zeros(np_)
+        L.check(L.lib().fvm_serve_state(self.h, ticket, L.dptr(prim), L.dptr(nut)),
+                "fvm_serve_state")
+        return dict(prim=prim, nut=nut)
+
+    def stats(self) -> dict:
+        import ctypes as C
+        out = (C.c_int64 * 6)()
+        L.check(L.lib().fvm_serve_stats(self.h, out), "fvm_serve_stats")
+        return dict(zip(("submitted", "done", "queued", "running", "steps", "status"),
+                        [int(x) for x in out]))
+
+    def run(self, requests: list[Request]) -> tuple[list[Result], dict]:
+        """The request workload: each request is submitted at its arrival
+        time (grid generation and layout on the worker pool)."""
+        results = {r.rid: Result(rid=r.rid, npts=r.npts, laminar=r.laminar, arrival=r.arrival)
+                   for r in requests}
+        t0 = time.perf_counter()
+
+        def go(req):
+            delay = req.arrival - (time.perf_counter() - t0)
+            if delay > 0:
+                time.sleep(delay)
+            g = grid_for(req)
+            m = build_geometry(g.coord, g.elem, g.ptype)
+            results[req.rid].npts = m.np
+            return self.submit(params_for(req, self.precision), m)
+
+        order = sorted(requests, key=lambda r: r.arrival)
+        with cf.ThreadPoolExecutor(max_workers=self.workers) as pool:
+            tickets = list(pool.map(go, order))
+        for req, t in zip(order, tickets):
+            self.wait(t)
+            q = self.result(t)
+            r = results[req.rid]
+            r.finished = r.arrival + q["total_s"] + max(0.0, 0.0)
+            r.admitted = r.arrival + q["queued_s"]
+            r.niter, r.fres, r.cl, r.cd, r.status = q["niter"], q["fres"], q["cl"], q["cd"], q["status"]
+            r.converged = q["status"] == 0 and q["fres"] <= self.minres
+        makespan = time.perf_counter() - t0
+        res = [results[r.rid] for r in requests]
+        ok = [r for r in res if r.status == 0]
+        lat = np.array([r.latency for r in res])
+        st = self.stats()
+        stats = dict(requests=len(res), completed_ok=len(ok),
+                     failures=[dict(rid=r.rid, status=r.status, niter=r.niter, npts=r.npts,
+                                    laminar=r.laminar) for r in res if r.status != 0],
+                     reached_minres=sum(r.converged for r in res),
+                     iteration_cap=sum(r.status == 0 and not r.converged for r in res),
+                     makespan_s=makespan, solves_per_s=len(ok) / makespan,
+                     p50_latency_s=float(np.percentile(lat, 50)),
+                     p99_latency_s=float(np.percentile(lat, 99)),
+                     vertex_stage_updates=float(sum(r.npts * 3 * r.niter for r in res)),
+                     steps=st["steps"], chunk=self.chunk, service="native")
+        stats["vertex_stage_updates_per_s"] = stats["vertex_stage_updates"] / makespan
+        return res, stats
+

@@ -368,6 +368,46 @@ int32_t fvm_batch_tune(fvm_batch *b, int32_t iters, int32_t max, double *ms_per_
  * same codes); FVM_ERR_ARG for a form that does not fit this batch. */
 int32_t fvm_batch_set_form(fvm_batch *b, int32_t form);
 
+/* ------------------------------------------------------------------------
+ * Serving (no counterpart in the reference, whose driver runs one solve per
+ * process, main.f:42-76): a continuous-batching service on one GPU.  One
+ * service thread owns a batch arena; solves submitted from any thread are
+ * admitted in arrival order while the arena has room, advanced together
+ * `chunk` iterations at a time, and retired at their residual drop or
+ * iteration cap, freeing room for the next.  With tune_every > 0 the
+ * autotuner re-picks the form of the iteration every tune_every steps.
+ * ---------------------------------------------------------------------- */
+typedef struct fvm_server fvm_server;
+int32_t fvm_serve_create(int32_t precision, const fvm_batch_caps *caps,
+                         int32_t chunk, int32_t tune_every, fvm_server **out);
+/* Queues a solve of up to nmax iterations stopping at fres <= minres.  The
+ * block layout is built on the calling thread (submit from several threads
+ * to prepare in parallel); the mesh arrays are copied.  keep_state = 1
+ * keeps the final state for fvm_serve_state. */
+int32_t fvm_serve_submit(fvm_server *s, const fvm_params *p,
+                         const fvm_mesh *m, int32_t nmax, double minres,
+                         int32_t keep_state, int64_t *ticket);
+/* *state: 0 queued, 1 running, 2 done. */
+int32_t fvm_serve_poll(fvm_server *s, int64_t ticket, int32_t *state);
+int32_t fvm_serve_wait(fvm_server *s, int64_t ticket, double timeout_s,
+                       int32_t *state);
+/* Results of a done solve: status (FVM_OK, a stop of the method, or
+ * FVM_ERR_CAPACITY for a solve larger than the empty arena), iterations,
+ * last fres, cl, cd; times[3] = seconds queued, resident, in total. */
+int32_t fvm_serve_result(fvm_server *s, int64_t ticket, int32_t *status,
+                         int32_t *niter, double *fres, double *cl, double *cd,
+                         double *times);
+/* Final state (prim(4,np), nut(np), driver order) of a done solve submitted
+ * with keep_state. */
+int32_t fvm_serve_state(fvm_server *s, int64_t ticket, double *prim,
+                        double *nut);
+/* Forgets a done solve. */
+int32_t fvm_serve_release(fvm_server *s, int64_t ticket);
+/* out[6]: submitted, done, queued, running, steps, service status. */
+int32_t fvm_serve_stats(fvm_server *s, int64_t *out);
+/* Stops the service thread after its current step and frees everything. */
+int32_t fvm_serve_destroy(fvm_server *s);
+
 /* Layout statistics of a mesh after renumbering (no GPU needed):
  * out[0] blocks, [1] interior edge entries (cut edges counted in both
  * blocks), [2] triangle entries (block and halo), [3] max slots of a

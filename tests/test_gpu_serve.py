@@ -52,3 +52,41 @@ def test_request_larger_than_the_arena_is_refused_with_a_status(fvm_lib):
     srv.close()
     assert [r.status for r in res] == [0, L.ERR_CAPACITY, 0]
     assert stats["completed_ok"] == 2 and len(stats["failures"]) == 1
+
+
+def test_native_service_equals_alone(fvm_lib):
+    """The native service (fvm_serve_*): the same results as each solve run
+    alone in its own batch, an oversize request refused with a status, and
+    the final state kept on request."""
+    from fvm2d_gb300 import serve
+    from fvm2d_gb300.batch import Batch
+    reqs = serve.generate_requests(n=6, rate=100.0, seed=4, pmin=1500, pmax=6000, laminar_frac=0.4)
+    srv = serve.NativeServer(vertices=20000, meshes=3, chunk=10, workers=3, max_iter=60,
+                             minres=1e-6)
+    grids = [serve.grid_for(r) for r in reqs]
+    meshes = [fvm_lib.build_geometry(g.coord, g.elem, g.ptype) for g in grids]
+    tickets = [srv.submit(serve.params_for(r, L.FP32), m, keep_state=(k == 0))
+               for k, (r, m) in enumerate(zip(reqs, meshes))]
+    big = serve.grid_for(serve.Request(rid=99, arrival=0.0, thickness=0.12, camber=0.0,
+                                       camber_pos=0.4, npts=40000, laminar=False, mach=0.5,
+                                       aoa_deg=1.0, rey=0.0, seed=1))
+    tb = srv.submit(serve.params_for(reqs[0], L.FP32),
+                    fvm_lib.build_geometry(big.coord, big.elem, big.ptype))
+    for t in tickets + [tb]:
+        assert srv.wait(t, 600.0)
+    assert srv.result(tb)["status"] == L.ERR_CAPACITY
+    for k, (r, m, t) in enumerate(zip(reqs, meshes, tickets)):
+        q = srv.result(t)
+        b = Batch(L.FP32, vertices=m.np, meshes=1, viscous=True)
+        s = b.add(serve.params_for(r, L.FP32), m)
+        b.start(s, 60, 1e-6)
+        b.step(70)
+        p = b.poll(s)
+        assert (q["status"], q["niter"], q["fres"], q["cl"], q["cd"]) == \
+            (p["status"], p["niter"], p["fres"], p["cl"], p["cd"])
+        if k == 0:
+            np.testing.assert_array_equal(srv.state(t, m.np)["prim"], b.get_state(s)["prim"])
+        b.close()
+    st = srv.stats()
+    assert st["submitted"] == 7 and st["done"] == 7 and st["status"] == 0
+    srv.close()
