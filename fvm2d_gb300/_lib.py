@@ -126,7 +126,7 @@ SIGNATURES = {
                                      C.c_int32, C.POINTER(C.c_int64)]),
     "fvm_serve_poll": (C.c_int32, [C.c_void_p, C.c_int64, _pi]),
     "fvm_serve_wait": (C.c_int32, [C.c_void_p, C.c_int64, C.c_double, _pi]),
-    "fvm_serve_result": (C.c_int32, [C.c_void_p, C.c_int64, _pi, _pi, _pd, _pd, _pd, _pd]),
+    "fvm_serve_result": (C.c_int32, [C.c_void_p, C.c_int64, _pi, _pi, _pd, _pd, _pd, _pd, _pd]),
     "fvm_serve_state": (C.c_int32, [C.c_void_p, C.c_int64, _pd, _pd]),
     "fvm_serve_release": (C.c_int32, [C.c_void_p, C.c_int64]),
     "fvm_serve_stats": (C.c_int32, [C.c_void_p, C.POINTER(C.c_int64)]),

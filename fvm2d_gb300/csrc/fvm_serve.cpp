@@ -42,8 +42,11 @@ struct Ticket {
   Clock::time_point t_submit, t_admit, t_done;
   int32_t status = FVM_OK, niter = 0;
   double fres = 0.0, cl = 0.0, cd = 0.0;
+  double cl_tail = 0.0, cd_tail = 0.0;   // means over the last kTail iterations
   std::vector<double> prim, nut;
 };
+
+constexpr int kTail = 256;
 
 double seconds(Clock::time_point a, Clock::time_point b) {
   return std::chrono::duration<double>(b - a).count();
@@ -101,6 +104,22 @@ int32_t retire(fvm_server *s) {
                                qx.data(), qy.data());
       if (st) return st;
     }
+    // mean cl, cd over the last iterations (the history the device keeps)
+    double clt = 0.0, cdt = 0.0;
+    const int k = niter < kTail ? niter : kTail;
+    if (k > 0) {
+      std::vector<double> hf(k), hfi(k), hcl(k), hcd(k);
+      std::vector<int32_t> hi(k);
+      st = fvm_batch_history(s->b, r.first, niter - k, k, hf.data(), hi.data(), hfi.data(),
+                             hcl.data(), hcd.data());
+      if (st) return st;
+      for (int j = 0; j < k; j++) {
+        clt += hcl[j];
+        cdt += hcd[j];
+      }
+      clt /= k;
+      cdt /= k;
+    }
     if ((st = fvm_batch_remove(s->b, r.first))) return st;
     s->resident.erase(r.first);
     std::lock_guard<std::mutex> lk(s->mu);
@@ -109,6 +128,8 @@ int32_t retire(fvm_server *s) {
     t.fres = fres;
     t.cl = cl;
     t.cd = cd;
+    t.cl_tail = clt;
+    t.cd_tail = cdt;
     t.prim.swap(prim);
     t.nut.swap(nut);
     finish(s, r.second, t, status);
@@ -265,7 +286,7 @@ extern "C" int32_t fvm_serve_wait(fvm_server *s, int64_t ticket, double timeout_
 
 extern "C" int32_t fvm_serve_result(fvm_server *s, int64_t ticket, int32_t *status,
                                     int32_t *niter, double *fres, double *cl, double *cd,
-                                    double *times) {
+                                    double *tail, double *times) {
   if (!s) return FVM_ERR_ARG;
   std::lock_guard<std::mutex> lk(s->mu);
   auto it = s->tickets.find(ticket);
@@ -276,6 +297,10 @@ extern "C" int32_t fvm_serve_result(fvm_server *s, int64_t ticket, int32_t *stat
   if (fres) *fres = t.fres;
   if (cl) *cl = t.cl;
   if (cd) *cd = t.cd;
+  if (tail) {
+    tail[0] = t.cl_tail;
+    tail[1] = t.cd_tail;
+  }
   if (times) {   // queued, resident, total (seconds)
     const bool ran = t.slot >= 0;
     times[0] = ran ? seconds(t.t_submit, t.t_admit) : seconds(t.t_submit, t.t_done);

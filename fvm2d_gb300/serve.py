@@ -291,9 +291,11 @@ class NativeServer:
         st, n = C.c_int32(), C.c_int32()
         f, cl, cd = C.c_double(), C.c_double(), C.c_double()
         tm = (C.c_double * 3)()
+        tail = (C.c_double * 2)()
         L.check(L.lib().fvm_serve_result(self.h, ticket, C.byref(st), C.byref(n), C.byref(f),
-                                         C.byref(cl), C.byref(cd), tm), "fvm_serve_result")
+                                         C.byref(cl), C.byref(cd), tail, tm), "fvm_serve_result")
         return dict(status=st.value, niter=n.value, fres=f.value, cl=cl.value, cd=cd.value,
+                    cl_tail=tail[0], cd_tail=tail[1],
                     queued_s=tm[0], resident_s=tm[1], total_s=tm[2])
 
     def state(self, ticket: int, np_: int) -> dict:
@@ -332,9 +334,10 @@ class NativeServer:
             self.wait(t)
             q = self.result(t)
             r = results[req.rid]
-            r.finished = r.arrival + q["total_s"] + max(0.0, 0.0)
+            r.finished = r.arrival + q["total_s"]
             r.admitted = r.arrival + q["queued_s"]
             r.niter, r.fres, r.cl, r.cd, r.status = q["niter"], q["fres"], q["cl"], q["cd"], q["status"]
+            r.cl_tail, r.cd_tail = q["cl_tail"], q["cd_tail"]
             r.converged = q["status"] == 0 and q["fres"] <= self.minres
         makespan = time.perf_counter() - t0
         res = [results[r.rid] for r in requests]

@@ -393,10 +393,11 @@ int32_t fvm_serve_wait(fvm_server *s, int64_t ticket, double timeout_s,
                        int32_t *state);
 /* Results of a done solve: status (FVM_OK, a stop of the method, or
  * FVM_ERR_CAPACITY for a solve larger than the empty arena), iterations,
- * last fres, cl, cd; times[3] = seconds queued, resident, in total. */
+ * last fres, cl, cd; tail[2] = mean cl, cd over the last 256 iterations;
+ * times[3] = seconds queued, resident, in total. */
 int32_t fvm_serve_result(fvm_server *s, int64_t ticket, int32_t *status,
                          int32_t *niter, double *fres, double *cl, double *cd,
-                         double *times);
+                         double *tail, double *times);
 /* Final state (prim(4,np), nut(np), driver order) of a done solve submitted
  * with keep_state. */
 int32_t fvm_serve_state(fvm_server *s, int64_t ticket, double *prim,
