@@ -715,7 +715,7 @@ def main():
     ap.add_argument("--workers", type=int, default=8)
     ap.add_argument("--max-iter", type=int, default=5000)
     ap.add_argument("--minres", type=float, default=1e-6)
-    ap.add_argument("--service", choices=["python", "native"], default="python",
+    ap.add_argument("--service", choices=["python", "native"], default="native",
                     help="serving loop: serve.Server (Python) or the C++ fvm_serve_* service")
     ap.add_argument("--tune-every", type=int, default=40,
                     help="serving: re-run the autotuner every N steps (0: never)")
