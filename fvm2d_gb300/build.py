@@ -4,8 +4,9 @@ Every translation unit is compiled in parallel:
   * CUDA kernels for sm_103a only (``-gencode arch=compute_103a,code=sm_103a``);
     the FP64 kernels and the set-up kernels with ``--fmad=false`` so their
     arithmetic is rounded exactly as written; the FP32 kernels with
-    contraction allowed and approximate division and square root (a few
-    ulp; the FP32 path is judged against the FP64 oracle by tolerance);
+    contraction allowed, approximate division and square root (a few ulp)
+    and subnormals flushed to zero (the FP32 path is judged against the
+    FP64 oracle by tolerance);
   * host C++ with ``-ffp-contract=off`` (the driver-side geometry must equal
     the serial FP64 arithmetic on x86 and on Arm alike).
 No CPU fallback is built: without this library the package refuses to run.
@@ -40,7 +41,7 @@ CXX_COMMON = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wext
 UNITS = [
     ("fvm_kernels_fp64.cu", "nvcc", ["--fmad=false"]),
     ("fvm_kernels_fp32.cu", "nvcc", os.environ.get(
-        "FVM_FP32_FLAGS", "-prec-div=false -prec-sqrt=false").split()),
+        "FVM_FP32_FLAGS", "-prec-div=false -prec-sqrt=false -ftz=true").split()),
     ("fvm_setup.cu", "nvcc", ["--fmad=false"]),
     ("fvm_noalloc.cu", "nvcc", ["--fmad=false"]),
     ("fvm_batch.cpp", "cxx", []),
