@@ -107,7 +107,7 @@ struct fvm_batch {
   void *dt = nullptr, *mu = nullptr, *mul = nullptr, *nut[2] = {nullptr, nullptr};
   double2 *coord = nullptr;
   double *ais = nullptr, *cvarea = nullptr, *drmin = nullptr, *wd = nullptr;
-  float *ais32 = nullptr, *cvarea32 = nullptr, *drmin32 = nullptr;   // FP32 batches
+  float *ais32 = nullptr, *cvarea32 = nullptr, *drmin32 = nullptr, *wd32 = nullptr;   // FP32
   int *orig = nullptr;
   uint8_t *vflag = nullptr;
   int2 *ve_rng = nullptr, *vt_rng = nullptr, *va_rng = nullptr;
@@ -197,6 +197,7 @@ ArenaPtrs<R> ptrs(const fvm_batch *b) {
   A.ais32 = b->ais32;
   A.cvarea32 = b->cvarea32;
   A.drmin32 = b->drmin32;
+  A.wd32 = b->wd32;
   A.wd = b->wd;
   A.orig = b->orig;
   A.vflag = b->vflag;
@@ -700,6 +701,7 @@ extern "C" int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *cap
     TRYB(dalloc(O, &b->ais32, V));
     TRYB(dalloc(O, &b->cvarea32, V));
     TRYB(dalloc(O, &b->drmin32, V));
+    TRYB(dalloc(O, &b->wd32, V));
     TRYB(dalloc(O, &b->tri_g32, (size_t)c.tri_entries));
   }
   TRYB(dalloc(O, &b->sw_nodes, (size_t)c.solid_edges));
@@ -1001,6 +1003,8 @@ extern "C" int32_t fvm_batch_add_prepared(fvm_batch *b, fvm_prepared *prep, int3
     PUT(put_range(b, b->cvarea32, v0, f));
     for (size_t i = 0; i < f.size(); i++) f[i] = (float)prep->drmin[i];
     PUT(put_range(b, b->drmin32, v0, f));
+    for (size_t i = 0; i < f.size(); i++) f[i] = (float)prep->wd[i];
+    PUT(put_range(b, b->wd32, v0, f));
   }
   PUT(put_range(b, b->wd, v0, prep->wd));
   PUT(put_range(b, b->orig, v0, prep->orig));

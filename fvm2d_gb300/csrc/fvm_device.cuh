@@ -415,17 +415,17 @@ __device__ __forceinline__ void farfield_flux(const MeshConst &mc, double cl, do
 // ------------------------------------------------------------ viscosity.f
 template <typename R>
 __device__ __forceinline__ R sutherland_viscosity(const MeshConst &mc, R density, R pressure) {
-  R temp = pressure / density / MCR(R, gas_const);
+  R temp = mdiv(mdiv(pressure, density), MCR(R, gas_const));
   R num = MCR(R, t_inf) + MCR(R, sconst);
   R den = temp + MCR(R, sconst);
-  return mpow(temp / MCR(R, t_inf), R(1.5)) * (num / den) / MCR(R, rey);
+  return mdiv(mpow(mdiv(temp, MCR(R, t_inf)), R(1.5)) * mdiv(num, den), MCR(R, rey));
 }
 
 template <typename R>
 __device__ __forceinline__ R mu_turb(const MeshConst &mc, R mu_lam, R density, R nu_tilde) {
-  R chi = nu_tilde * density / mu_lam;
+  R chi = mdiv(nu_tilde * density, mu_lam);
   R chi3 = cube(chi);
-  R fv1 = chi3 / (chi3 + MCR(R, cv11));
+  R fv1 = mdiv(chi3, chi3 + MCR(R, cv11));
   return density * nu_tilde * fv1;
 }
 
@@ -477,23 +477,22 @@ __device__ __forceinline__ R4<R> rk_update(const MeshConst &mc, int irk, const R
 
 // --------------------------------------------------------- sa_model.f
 template <typename R>
-__device__ __forceinline__ R update_sa(const MeshConst &mc, R nut, R rho, R mul, double wd_,
-                                       R dt, double cvarea, R divf, R omega) {
-  R wd = R(wd_);
-  R chi = nut * rho / mul;
+__device__ __forceinline__ R update_sa(const MeshConst &mc, R nut, R rho, R mul, R wd,
+                                       R dt, R cvarea, R divf, R omega) {
+  R chi = mdiv(nut * rho, mul);
   R chi3 = cube(chi);
-  R fv1 = chi3 / (chi3 + MCR(R, cv11));
-  R fv2 = R(1) / cube(R(1) + chi / MCR(R, cv2));
-  R r = nut / wd / (wd * MCR(R, kolm2));
-  R fv3 = (R(1) + chi * fv1) * (R(1) - fv2) / dmax1(chi, R(0.001));
+  R fv1 = mdiv(chi3, chi3 + MCR(R, cv11));
+  R fv2 = mdiv(R(1), cube(R(1) + mdiv(chi, MCR(R, cv2))));
+  R r = mdiv(mdiv(nut, wd), wd * MCR(R, kolm2));
+  R fv3 = mdiv((R(1) + chi * fv1) * (R(1) - fv2), dmax1(chi, R(0.001)));
   R S = fv3 * mfabs(omega) + r * fv2;
-  r = r / S;
+  r = mdiv(r, S);
   r = dmin1(r, R(2));
   R g = r + MCR(R, cw2) * (pow6(r) - r);
-  R fw = g * mpow(MCR(R, cw31) / (pow6(g) + MCR(R, cw32)), R(1) / R(6));
+  R fw = g * mpow(mdiv(MCR(R, cw31), pow6(g) + MCR(R, cw32)), mdiv(R(1), R(6)));
   R source = MCR(R, cb1) * S * nut;
-  R fact = R(1) + MCR(R, cw1) * fw * (nut / wd) * (dt / wd);
-  return (nut - (dt / R(cvarea)) * divf + dt * source) / fact;
+  R fact = R(1) + MCR(R, cw1) * fw * mdiv(nut, wd) * mdiv(dt, wd);
+  return mdiv(nut - mdiv(dt, cvarea) * divf + dt * source, fact);
 }
 
 }  // namespace fvm

@@ -213,7 +213,7 @@ struct ArenaPtrs {
   const int4 *bt_nodes;   // triangle entries (n1, n2, n3, arena triangle)
   const double *elarea;   // per arena triangle
   const EdgeGeo32 *be_g32; // FP32 path: ends, geometry and local slots of each edge entry
-  const float *ais32, *cvarea32, *drmin32;   // FP32 path: per-vertex copies
+  const float *ais32, *cvarea32, *drmin32, *wd32;   // FP32 path: per-vertex copies
   const TriGeo32 *tri_g32; // FP32 path: per triangle entry of the blocks (bt_* order)
   // solid edges per mesh for clcd (n1, n2) in beindx order
   const int2 *sw_nodes;

@@ -149,6 +149,11 @@ __device__ __forceinline__ R v_cvarea(const ArenaPtrs<R> &A, int v) {
   else return A.cvarea[v];
 }
 template <typename R>
+__device__ __forceinline__ R v_wd(const ArenaPtrs<R> &A, int v) {
+  if constexpr (sizeof(R) == 4) return A.wd32[v];
+  else return A.wd[v];
+}
+template <typename R>
 __device__ __forceinline__ R v_drmin(const ArenaPtrs<R> &A, int v) {
   if constexpr (sizeof(R) == 4) return A.drmin32[v];
   else return A.drmin[v];
@@ -1271,10 +1276,24 @@ __global__ void __launch_bounds__(kBlockVerts) k_sa(ArenaPtrs<R> A, int stage, i
     R *nut_new = A.nut[1 - ctl.nphase];
     for (int k = threadIdx.x; k < bi.nt; k += blockDim.x) {
       const int4 t = A.bt_nodes[bi.t0 + k];
-      const double2 c1 = A.coord[t.x], c2 = A.coord[t.y], c3 = A.coord[t.z];
-      const R areat = R(0.25 / A.elarea[t.w]);
-      const R dbxx[3] = {R(c2.y - c3.y), R(c3.y - c1.y), R(c1.y - c2.y)};
-      const R dbyy[3] = {R(c3.x - c2.x), R(c1.x - c3.x), R(c2.x - c1.x)};
+      R areat, dbxx[3], dbyy[3];
+      if constexpr (sizeof(R) == 4) {   // FP32 copies rounded once
+        const TriGeo32 tg = A.tri_g32[bi.t0 + k];
+        areat = tg.areat;
+        for (int j = 0; j < 3; j++) {
+          dbxx[j] = tg.dbxx[j];
+          dbyy[j] = tg.dbyy[j];
+        }
+      } else {
+        const double2 c1 = A.coord[t.x], c2 = A.coord[t.y], c3 = A.coord[t.z];
+        areat = R(0.25 / A.elarea[t.w]);
+        dbxx[0] = R(c2.y - c3.y);
+        dbxx[1] = R(c3.y - c1.y);
+        dbxx[2] = R(c1.y - c2.y);
+        dbyy[0] = R(c3.x - c2.x);
+        dbyy[1] = R(c1.x - c3.x);
+        dbyy[2] = R(c2.x - c1.x);
+      }
       int a1 = t.x, a2 = t.y, a3 = t.z;
       if (mc.bugcompat) {
         a1 = mc.orig123[0];
@@ -1286,21 +1305,31 @@ __global__ void __launch_bounds__(kBlockVerts) k_sa(ArenaPtrs<R> A, int stage, i
       const R mul1 = A.mul[t.x], mul2 = A.mul[t.y], mul3 = A.mul[t.z];
       const R n1 = nut[t.x], n2 = nut[t.y], n3 = nut[t.z];
       const R r1 = P[t.x].x, r2 = P[t.y].x, r3 = P[t.z].x;
-      const R mult = (mul1 + mul2 + mul3) / R(3);
-      const R prim5t = (n1 + n2 + n3) / R(3);
-      const R rhot = (r1 + r2 + r3) / R(3);
-      const R mutb = mult / rhot + prim5t;
+      const R mult = mdiv(mul1 + mul2 + mul3, R(3));
+      const R prim5t = mdiv(n1 + n2 + n3, R(3));
+      const R rhot = mdiv(r1 + r2 + r3, R(3));
+      const R mutb = mdiv(mult, rhot) + prim5t;
       const R cs1 = MCR(R, cb2sig1), cs2 = MCR(R, cb2sig2);
-      s_t[3 * k + 0] = (cs1 * mutb - cs2 * (mul1 / r1 + n1)) * (nux * dbxx[0] + nuy * dbyy[0]) * areat;
-      s_t[3 * k + 1] = (cs1 * mutb - cs2 * (mul2 / r2 + n2)) * (nux * dbxx[1] + nuy * dbyy[1]) * areat;
-      s_t[3 * k + 2] = (cs1 * mutb - cs2 * (mul3 / r3 + n3)) * (nux * dbxx[2] + nuy * dbyy[2]) * areat;
+      s_t[3 * k + 0] = (cs1 * mutb - cs2 * (mdiv(mul1, r1) + n1)) * (nux * dbxx[0] + nuy * dbyy[0]) * areat;
+      s_t[3 * k + 1] = (cs1 * mutb - cs2 * (mdiv(mul2, r2) + n2)) * (nux * dbxx[1] + nuy * dbyy[1]) * areat;
+      s_t[3 * k + 2] = (cs1 * mutb - cs2 * (mdiv(mul3, r3) + n3)) * (nux * dbxx[2] + nuy * dbyy[2]) * areat;
     }
     for (int k = threadIdx.x; k < bi.ne; k += blockDim.x) {
       const int e = bi.e0 + k;
-      const int2 nn = A.be_nodes[e];
-      const double2 ds = A.be_ds[e];
+      int2 nn;
+      R d1, d2;
+      if constexpr (sizeof(R) == 4) {   // ds = (cos, sin) |ds| from the FP32 record
+        const EdgeGeo32 g = A.be_g32[e];
+        nn = make_int2(g.n1, g.n2);
+        d1 = g.ct * g.len;
+        d2 = g.st * g.len;
+      } else {
+        nn = A.be_nodes[e];
+        const double2 ds = A.be_ds[e];
+        d1 = R(ds.x);
+        d2 = R(ds.y);
+      }
       const R4<R> p1 = P[nn.x], p2 = P[nn.y];
-      const R d1 = R(ds.x), d2 = R(ds.y);
       const R unl = p1.y * d1 + p1.z * d2;
       const R unr = p2.y * d1 + p2.z * d2;
       const R una = R(0.5) * (unl + unr);
@@ -1352,7 +1381,8 @@ __global__ void __launch_bounds__(kBlockVerts) k_sa(ArenaPtrs<R> A, int stage, i
       } else {
         const Grad<R> g = A.grad[v];
         const R omega = g.qy[1] - g.qx[2];
-        nn = update_sa<R>(mc, nut[v], P[v].x, A.mul[v], A.wd[v], A.dt[v], A.cvarea[v], divf, omega);
+        nn = update_sa<R>(mc, nut[v], P[v].x, A.mul[v], v_wd(A, v), A.dt[v], v_cvarea(A, v), divf,
+                          omega);
       }
       nut_new[v] = nn;
       if (nn < R(0)) atomicMin(&ctl.err_point, A.orig[v]);
