@@ -120,6 +120,7 @@ SIGNATURES = {
     "fvm_batch_launch_count": (C.c_int64, [C.c_void_p]),
     "fvm_batch_tune": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, _pd, _pi]),
     "fvm_batch_set_form": (C.c_int32, [C.c_void_p, C.c_int32]),
+    "fvm_abi_sizes": (None, [C.POINTER(C.c_int64)]),
     "fvm_serve_create": (C.c_int32, [C.c_int32, C.c_void_p, C.c_int32, C.c_int32,
                                      C.POINTER(C.c_void_p)]),
     "fvm_serve_submit": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_double,

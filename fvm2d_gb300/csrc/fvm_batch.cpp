@@ -1417,6 +1417,13 @@ int32_t residu_impl(fvm_handle *h) {
 
 }  // namespace
 
+extern "C" void fvm_abi_sizes(int64_t out[4]) {
+  out[0] = (int64_t)sizeof(fvm_params);
+  out[1] = (int64_t)sizeof(fvm_mesh);
+  out[2] = (int64_t)sizeof(fvm_geom);
+  out[3] = (int64_t)sizeof(fvm_batch_caps);
+}
+
 extern "C" const char *fvm_gpu_strerror(int32_t s) {
   switch (s) {
     case FVM_OK: return "ok";

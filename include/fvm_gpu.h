@@ -153,6 +153,9 @@ int32_t fvm_gpu_create(const fvm_params *params, const fvm_mesh *mesh,
                        fvm_handle **out);
 int32_t fvm_gpu_destroy(fvm_handle *h);
 const char *fvm_gpu_strerror(int32_t status);
+/* sizeof of the ABI structs, for bindings to check their mirrors:
+ * out[0] fvm_params, [1] fvm_mesh, [2] fvm_geom, [3] fvm_batch_caps. */
+void fvm_abi_sizes(int64_t out[4]);
 
 /* State transfer in the driver's vertex order (initialize.f / finalize.f
  * arrays).  iterlast is the iteration counter of the first iteration to run

@@ -183,3 +183,15 @@ def test_wall_table_and_sol_roundtrip(fvm_lib, oracle_lib, tmp_path):
     np.testing.assert_array_equal(nut, st["nut"])
     results.write_wall(str(tmp_path / "WALL.DAT"), t)
     assert np.loadtxt(str(tmp_path / "WALL.DAT")).shape == (m.nsp, 5)
+
+
+def test_ctypes_mirrors_match_the_abi_structs(fvm_lib):
+    """The Python mirrors of fvm_params, fvm_mesh, fvm_geom and
+    fvm_batch_caps have the C structs' sizes (a drifted field would shift
+    every later one)."""
+    import ctypes as C
+    out = (C.c_int64 * 4)()
+    L.lib().fvm_abi_sizes(out)
+    assert list(out) == [C.sizeof(L.FvmParams), C.sizeof(L.FvmMesh), C.sizeof(L.FvmGeom),
+                         C.sizeof(L.FvmBatchCaps)]
+
