@@ -181,7 +181,7 @@ def run_gpu(args):
     b, slots = make_batch(FLUX_CODES[args.flux], F.FP32, meshes)
     ext = torch.cuda.ExternalStream(b.stream())
     for s in slots:
-        b.start(s, args.warmup + 2 * args.steps + 40)
+        b.start(s, args.warmup + 2 * args.steps + 200)   # + the tuner's iterations
     b.step(args.warmup)
     b.sync()
     if args.form:             # a given form (profiling runs): no tuning

@@ -29,6 +29,7 @@ using namespace fvm;
 namespace {
 
 constexpr int kHistRows = 512;    // history ring per slot (RES.DAT rows)
+constexpr int kGraphIters = 10;   // iterations per graph launch (untimed steps)
 
 // first-fit allocator of index ranges [0, cap)
 class RangeAlloc {
@@ -134,9 +135,12 @@ struct fvm_batch {
   double *h_fres = nullptr, *h_fresi = nullptr, *h_cl = nullptr, *h_cd = nullptr;
   int *h_iresi = nullptr;
   int *work = nullptr, *nwork = nullptr;
+  int *mesh_part = nullptr;                // per slot: the part (chain) holding its blocks
+  std::vector<int> mesh_part_h;
   LaunchCfg cfg{};
   bool any_turbulent_ok = true;
-  cudaGraphExec_t graph = nullptr;
+  cudaGraphExec_t graph = nullptr;         // one iteration
+  cudaGraphExec_t graph_multi = nullptr;   // kGraphIters iterations
   // timing
   bool timing = false;
   std::vector<cudaEvent_t> ev;    // pairs around each kernel of an iteration
@@ -231,6 +235,7 @@ ArenaPtrs<R> ptrs(const fvm_batch *b) {
   A.h_iresi = b->h_iresi;
   A.work = b->work;
   A.nwork = b->nwork;
+  A.mesh_part = b->mesh_part;
   A.wpart = 0;
   A.nslots = (int)b->slots.size();
   return A;
@@ -394,6 +399,8 @@ cudaError_t put_range(fvm_batch *b, T *base, int64_t off, const std::vector<T> &
   return cudaMemcpyAsync(base + off, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, b->stream);
 }
 
+void drop_graphs(fvm_batch *b);
+
 int32_t update_work(fvm_batch *b) {
   std::vector<int> work, mesh_first;
   int flux = -1;
@@ -439,10 +446,7 @@ int32_t update_work(fvm_batch *b) {
   const bool use_fused = b->fused_wanted && b->fused_fits;
   changed |= use_fused != b->fused;
   b->fused = use_fused;
-  if (changed && b->graph) {            // different kernels or tiles: re-capture
-    cudaGraphExecDestroy(b->graph);
-    b->graph = nullptr;
-  }
+  if (changed) drop_graphs(b);          // different kernels or tiles: re-capture
   const int n = (int)work.size();
   // the work list in kMaxChains parts at mesh boundaries: part k ends at
   // the boundary nearest (k+1)/chains of the list (the last parts are empty
@@ -461,15 +465,31 @@ int32_t update_work(fvm_batch *b) {
     head[k] = end;
     prev = end;
   }
+  // the part (chain) of every resident mesh, for the per-chain monitors
+  std::vector<int> part(b->slots.size(), 0);
+  {
+    size_t m = 0;
+    for (size_t i = 0; i < b->slots.size(); i++)
+      if (b->slots[i].used) {
+        const int first = mesh_first[m++];
+        int k = 1;
+        while (k < kMaxChains && first >= head[k]) k++;
+        part[i] = k;
+      }
+  }
+  b->mesh_part_h = part;
   if (n) FVM_TRY(b, cudaMemcpyAsync(b->work, work.data(), n * sizeof(int), cudaMemcpyHostToDevice, b->stream));
   FVM_TRY(b, cudaMemcpyAsync(b->nwork, head, sizeof(head), cudaMemcpyHostToDevice, b->stream));
+  FVM_TRY(b, cudaMemcpyAsync(b->mesh_part, b->mesh_part_h.data(), part.size() * sizeof(int),
+                             cudaMemcpyHostToDevice, b->stream));
   FVM_TRY(b, cudaStreamSynchronize(b->stream));
   return FVM_OK;
 }
 
-// kernels of one iteration, in order; optional timing events around each
+// kernels of `iters` iterations, in order; optional timing events around
+// each (one iteration only)
 template <typename R>
-int32_t enqueue_iteration(fvm_batch *b, bool with_events) {
+int32_t enqueue_iteration(fvm_batch *b, bool with_events, int iters) {
   const ArenaPtrs<R> A = ptrs<R>(b);
   const LaunchCfg &c = b->cfg;
   const bool visc = c.viscous;   // a viscous mesh is resident
@@ -525,54 +545,78 @@ int32_t enqueue_iteration(fvm_batch *b, bool with_events) {
     }
     return FVM_OK;
   };
+  // the end of an iteration for the meshes of one part: SA step, then the
+  // monitor of those meshes (conres, clcd, stop test)
+  auto finish_iteration = [&](const ArenaPtrs<R> &Ap, const LaunchCfg &cp) -> int32_t {
+    cudaStream_t st = cp.stream;
+    if (b->run_sa) {
+      FVM_TRY(b, mark(K_SA, st));
+      FVM_TRY(b, launch_sa(Ap, cp, 3, 0));
+      FVM_TRY(b, done(st));
+    }
+    FVM_TRY(b, mark(K_MON, st));
+    FVM_TRY(b, launch_monitor(Ap, cp, b->prec == FVM_PREC_FP64 ? 1 : 0));
+    FVM_TRY(b, done(st));
+    return FVM_OK;
+  };
   if (b->chains > 1) {
-    // independent chains over the parts of the work list; chain k starts
-    // after chain k-1's first pass, then all join the first stream
+    // independent chains over the parts of the work list, each running
+    // `iters` whole iterations of its meshes; chain k starts after chain
+    // k-1's first pass, then all join the first stream
     for (int k = 0; k < b->chains; k++) {
       ArenaPtrs<R> Ak = A;
       Ak.wpart = k + 1;
       LaunchCfg ck = c;
       ck.stream = k ? b->chain_stream[k] : b->stream;
       if (k) FVM_TRY(b, cudaStreamWaitEvent(ck.stream, b->ev_fork[k - 1], 0));
-      const int32_t st = stages(Ak, ck, k + 1 < b->chains ? b->ev_fork[k] : nullptr);
-      if (st) return st;
+      for (int it = 0; it < iters; it++) {
+        int32_t st = stages(Ak, ck, (it == 0 && k + 1 < b->chains) ? b->ev_fork[k] : nullptr);
+        if (!st) st = finish_iteration(Ak, ck);
+        if (st) return st;
+      }
     }
     for (int k = 1; k < b->chains; k++) {
       FVM_TRY(b, cudaEventRecord(b->ev_join[k], b->chain_stream[k]));
       FVM_TRY(b, cudaStreamWaitEvent(b->stream, b->ev_join[k], 0));
     }
   } else {
-    int32_t st = stages(A, c, nullptr);
-    if (st) return st;
+    for (int it = 0; it < iters; it++) {
+      int32_t st = stages(A, c, nullptr);
+      if (!st) st = finish_iteration(A, c);
+      if (st) return st;
+    }
   }
-  if (b->run_sa) {
-    FVM_TRY(b, mark(K_SA, b->stream));
-    FVM_TRY(b, launch_sa(A, c, 3, 0));
-    FVM_TRY(b, done(b->stream));
-  }
-  FVM_TRY(b, mark(K_MON, b->stream));
-  FVM_TRY(b, launch_monitor(A, c, b->prec == FVM_PREC_FP64 ? 1 : 0));
-  FVM_TRY(b, done(b->stream));
-  b->kernels_per_iter = k;
+  b->kernels_per_iter = k / iters;
   return FVM_OK;
 }
 
-int32_t build_graph(fvm_batch *b) {
-  if (b->graph) return FVM_OK;
+// The graph of one iteration (iters = 1, per-kernel events when timing) or
+// of kGraphIters iterations (fewer launches, and with several chains each
+// chain runs on into its next iteration without waiting for the others).
+int32_t build_graph(fvm_batch *b, int iters) {
+  cudaGraphExec_t &out = iters > 1 ? b->graph_multi : b->graph;
+  if (out) return FVM_OK;
   cudaGraph_t g = nullptr;
   FVM_TRY(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-  int32_t st = b->prec == FVM_PREC_FP64 ? enqueue_iteration<double>(b, b->timing)
-                                        : enqueue_iteration<float>(b, b->timing);
+  const bool ev = b->timing && iters == 1;
+  int32_t st = b->prec == FVM_PREC_FP64 ? enqueue_iteration<double>(b, ev, iters)
+                                        : enqueue_iteration<float>(b, ev, iters);
   cudaError_t e = cudaStreamEndCapture(b->stream, &g);
   if (st != FVM_OK) {
     if (g) cudaGraphDestroy(g);
     return st;
   }
   FVM_TRY(b, e);
-  e = cudaGraphInstantiate(&b->graph, g, 0);
+  e = cudaGraphInstantiate(&out, g, 0);
   cudaGraphDestroy(g);
   FVM_TRY(b, e);
   return FVM_OK;
+}
+
+void drop_graphs(fvm_batch *b) {
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  if (b->graph_multi) cudaGraphExecDestroy(b->graph_multi);
+  b->graph = b->graph_multi = nullptr;
 }
 
 Slot *slot_of(fvm_batch *b, int32_t slot) {
@@ -686,6 +730,7 @@ extern "C" int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *cap
   TRYB(dalloc(O, &b->part, (size_t)c.blocks));
   TRYB(dalloc(O, &b->work, (size_t)c.blocks));
   TRYB(dalloc(O, &b->nwork, 1 + kMaxChains));
+  TRYB(dalloc(O, &b->mesh_part, (size_t)c.meshes));
   TRYB(dalloc(O, &b->be_nodes, (size_t)c.edge_entries));
   TRYB(dalloc(O, &b->be_loc, (size_t)c.edge_entries));
   TRYB(dalloc(O, &b->halo_ids, (size_t)b->cap[P_HALO]));
@@ -752,7 +797,7 @@ extern "C" int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *cap
 extern "C" int32_t fvm_batch_destroy(fvm_batch *b) {
   if (!b) return FVM_OK;
   if (b->stream) cudaStreamSynchronize(b->stream);
-  if (b->graph) cudaGraphExecDestroy(b->graph);
+  drop_graphs(b);
   for (cudaEvent_t e : b->ev) cudaEventDestroy(e);
   for (void *p : b->owned) cudaFree(p);
   if (b->pinned) cudaFreeHost(b->pinned);
@@ -1167,8 +1212,16 @@ extern "C" int32_t fvm_batch_start(fvm_batch *b, int32_t slot, int32_t nmax, dou
 
 extern "C" int32_t fvm_batch_step(fvm_batch *b, int32_t niter) {
   if (!b || niter < 0) return FVM_ERR_ARG;
-  int32_t st = build_graph(b);
-  if (st) return st;
+  int32_t st;
+  if (!b->timing && niter >= kGraphIters) {
+    if ((st = build_graph(b, kGraphIters))) return st;
+    for (; niter >= kGraphIters; niter -= kGraphIters) {
+      FVM_TRY(b, cudaGraphLaunch(b->graph_multi, b->stream));
+      b->launches += (int64_t)b->kernels_per_iter * kGraphIters;
+    }
+  }
+  if (niter == 0) return FVM_OK;
+  if ((st = build_graph(b, 1))) return st;
   for (int i = 0; i < niter; i++) {
     FVM_TRY(b, cudaGraphLaunch(b->graph, b->stream));
     b->launches += b->kernels_per_iter;
@@ -1218,10 +1271,7 @@ static int32_t apply_form(fvm_batch *b, const Form &f) {
   b->cfg.grad_mode = f.grad;
   const bool rechain = f.chains != b->chains;
   b->chains = f.chains;
-  if (b->graph) {
-    cudaGraphExecDestroy(b->graph);
-    b->graph = nullptr;
-  }
+  drop_graphs(b);
   return rechain ? update_work(b) : FVM_OK;   // the parts of the work list
 }
 
@@ -1235,6 +1285,8 @@ extern "C" int32_t fvm_batch_set_form(fvm_batch *b, int32_t form) {
 extern "C" int32_t fvm_batch_tune(fvm_batch *b, int32_t iters, int32_t max, double *ms_per_iter,
                                   int32_t *choice) {
   if (!b || iters < 1 || max < 0 || (max > 0 && !ms_per_iter)) return FVM_ERR_ARG;
+  // whole multi-iteration graphs when the steps are untimed
+  const int timed = b->timing ? iters : (iters + kGraphIters - 1) / kGraphIters * kGraphIters;
   for (int i = 0; i < max; i++) ms_per_iter[i] = 0.0;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   FVM_TRY(b, cudaEventCreate(&e0));
@@ -1250,16 +1302,19 @@ extern "C" int32_t fvm_batch_tune(fvm_batch *b, int32_t iters, int32_t max, doub
     const Form f = form_of(b, i);
     if (!form_fits(b, f)) continue;
     if ((st = apply_form(b, f))) break;
-    if ((st = fvm_batch_step(b, 1))) break;   // capture + one untimed iteration
+    // timed as the steps will run: whole multi-iteration graphs (captured
+    // before the timing), so each form is timed over at least one
+    if (!b->timing && (st = build_graph(b, kGraphIters))) break;
+    if ((st = fvm_batch_step(b, 1))) break;   // one untimed iteration
     cudaError_t e = cudaEventRecord(e0, b->stream);
-    if (e == cudaSuccess) st = fvm_batch_step(b, iters);
+    if (e == cudaSuccess) st = fvm_batch_step(b, timed);
     if (e == cudaSuccess && st == FVM_OK) e = cudaEventRecord(e1, b->stream);
     if (e == cudaSuccess && st == FVM_OK) e = cudaEventSynchronize(e1);
     float ms = 0.f;
     if (e == cudaSuccess && st == FVM_OK) e = cudaEventElapsedTime(&ms, e0, e1);
     if (e != cudaSuccess) st = cuda_status(b, e);
     if (st) break;
-    const double per = (double)ms / iters;
+    const double per = (double)ms / timed;
     if (i < max) ms_per_iter[i] = per;
     if (best < 0 || per < best_ms) {
       best = i;
@@ -1349,10 +1404,7 @@ extern "C" int32_t fvm_batch_timing(fvm_batch *b, int32_t on) {
     for (auto &e : b->ev) FVM_TRY(b, cudaEventCreate(&e));
   }
   b->timing = want;
-  if (b->graph) {
-    cudaGraphExecDestroy(b->graph);
-    b->graph = nullptr;
-  }
+  drop_graphs(b);
   return FVM_OK;
 }
 

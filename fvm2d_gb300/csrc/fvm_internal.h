@@ -237,6 +237,7 @@ struct ArenaPtrs {
   const int *work;
   const int *nwork;    // [0] blocks in the work list, [k] end of part k (k = 1..kMaxChains)
   int wpart;           // 0 the whole list, k part k
+  const int *mesh_part;  // per slot: the part holding the mesh's blocks
   int nslots;             // mesh slots (monitor grid)
 };
 

@@ -1549,6 +1549,7 @@ __global__ void __launch_bounds__(kMonitorMaxThreads) k_monitor(ArenaPtrs<R> A, 
   const int m = blockIdx.x;
   MeshCtl &ctl = A.ctl[m];
   if (!ctl.active) return;
+  if (A.wpart > 0 && A.mesh_part[m] != A.wpart) return;   // another chain's mesh
   const MeshConst &mc = A.mc[m];
   double sum, mx;
   int arg;

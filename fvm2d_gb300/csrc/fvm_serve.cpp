@@ -192,7 +192,7 @@ void service(fvm_server *s) {
     if (s->resident.empty()) continue;
     if (s->tune_every > 0 && s->steps % s->tune_every == 0) {
       int32_t choice = 0;
-      if ((st = fvm_batch_tune(s->b, 2, 0, nullptr, &choice))) break;
+      if ((st = fvm_batch_tune(s->b, 10, 0, nullptr, &choice))) break;
     }
     if ((st = fvm_batch_step(s->b, s->chunk))) break;
     s->steps++;

@@ -123,7 +123,7 @@ def prepare(req: Request, precision: int) -> Prepared:
 class Server:
     def __init__(self, vertices: int = 6_000_000, meshes: int = 256, precision: int = L.FP32,
                  chunk: int = 50, workers: int = 8, max_iter: int = 5000, minres: float = 1e-6,
-                 tune_every: int = 0, tune_iters: int = 2, **caps):
+                 tune_every: int = 0, tune_iters: int = 10, **caps):
         self.batch = Batch(precision, vertices=vertices, meshes=meshes, viscous=True, **caps)
         self.precision = precision
         self.chunk = chunk

@@ -354,7 +354,9 @@ int32_t fvm_batch_timing_read(fvm_batch *b, int32_t max, char *names,
 int64_t fvm_batch_launch_count(fvm_batch *b);
 
 /* Autotuner (no counterpart in the reference): runs `iters` timed
- * iterations of the resident solves under each form of the iteration (the
+ * iterations (rounded up to whole graphs of 10 iterations, which is how
+ * untimed steps run) of the resident solves under each form of the
+ * iteration (the
  * gradient pass staged by bulk copies, by per-thread loads or walked per
  * vertex; or the fused gradient+flux pass; in one chain of kernels or
  * two overlapped ones) and keeps the fastest.  Every
