@@ -24,7 +24,8 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 INC = os.path.join(os.path.dirname(HERE), "include")
-# FVM_BUILD_TAG / FVM_FP32_FLAGS select an alternative build (own directory)
+# FVM_BUILD_TAG / FVM_FP32_FLAGS / FVM_CXX_FLAGS select an alternative build
+# (own directory)
 TAG = os.environ.get("FVM_BUILD_TAG", "")
 OUT = os.path.join(HERE, "_build", platform.machine() + (("-" + TAG) if TAG else ""))
 LIB = os.path.join(OUT, "libfvm2d_gb300.so")
@@ -72,7 +73,8 @@ def _compile(unit, kind, extra, digest, verbose):
     if kind == "nvcc":
         cmd = [NVCC] + NVCC_COMMON + extra + ["-c", src, "-o", obj]
     else:
-        cmd = [os.environ.get("CXX", "g++")] + CXX_COMMON + extra + ["-c", src, "-o", obj]
+        cmd = ([os.environ.get("CXX", "g++")] + CXX_COMMON + extra +
+               os.environ.get("FVM_CXX_FLAGS", "").split() + ["-c", src, "-o", obj])
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

@@ -29,7 +29,10 @@ using namespace fvm;
 namespace {
 
 constexpr int kHistRows = 512;    // history ring per slot (RES.DAT rows)
-constexpr int kGraphIters = 10;   // iterations per graph launch (untimed steps)
+#ifndef FVM_GRAPH_ITERS
+#define FVM_GRAPH_ITERS 10
+#endif
+constexpr int kGraphIters = FVM_GRAPH_ITERS;   // iterations per graph launch (untimed steps)
 
 // first-fit allocator of index ranges [0, cap)
 class RangeAlloc {
