@@ -286,6 +286,17 @@ int32_t build_layout(const fvm_mesh &m, int bv, MeshLayout &L) {
     bi.nt = (int)btris[b].size();
     if (bi.nt > 0x3fff) return FVM_ERR_CAPACITY;
     L.max_tri = std::max(L.max_tri, bi.nt);
+    // the block's interior triangles (all three vertices its own) first,
+    // then those touching the halo, each group ascending: the gradient
+    // passes' first trips over the entries then read only the block's own
+    // (staged) states.  Sums follow the per-vertex lists, which are put
+    // back in ascending triangle order below, so the order here changes
+    // no result.
+    std::stable_partition(btris[b].begin(), btris[b].end(), [&](int t) {
+      for (int q = 0; q < 3; q++)
+        if (!inblk(L.iperm[m.elem[3 * t + q] - 1])) return false;
+      return true;
+    });
     for (int k = 0; k < bi.nt; k++) {
       const int t = btris[b][k];
       int n[3];
@@ -294,6 +305,10 @@ int32_t build_layout(const fvm_mesh &m, int bv, MeshLayout &L) {
       for (int q = 0; q < 3; q++)
         if (inblk(n[q])) vtri[n[q]].push_back((uint16_t)(k | (q << kTriPosShift)));
     }
+    for (int v = v0; v < v1; v++)   // green_gauss.f visits triangles ascending
+      std::sort(vtri[v].begin(), vtri[v].end(), [&](uint16_t x, uint16_t y) {
+        return btris[b][x & 0x3fff] < btris[b][y & 0x3fff];
+      });
     // the halo's other triangles follow, then each halo vertex lists its
     // triangles (ascending triangle number: the order green_gauss.f visits)
     const std::vector<int> &extra = btris_extra[b];

@@ -1,0 +1,139 @@
+"""The single-mesh workloads at their full sizes, against the CPU oracle.
+
+Sizes: 1024 x 384 Euler (393,216 vertices, jittered), 512 x 192 laminar
+(98,304) and 768 x 256 RANS-SA (196,608) NACA 0012 O-grids.
+
+- FP64 Roe uses only + - * / and sqrt, so the state after whole iterations
+  must equal the oracle's bit for bit (and the residual's location and
+  maximum); the norm and the forces are sums in another order.
+- The transcendental paths (KFVS erf/exp, HLLC's two-rarefaction pow,
+  Sutherland's pow, the SA model) differ from glibc by a few ulp per call;
+  the state carries 1e-9 relative (as the small-grid KFVS/HLLC histories
+  do), the residual history 1e-10.
+- FP32 (the batched path's arithmetic) against the FP64 oracle: the state
+  after a few iterations, and converged lift and drag on the 160 x 48 case
+  within |dcl| <= 1e-4 and |dcd| <= 2e-5.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+from fvm2d_gb300 import _lib as L  # noqa: E402
+from fvm2d_gb300.batch import Batch  # noqa: E402
+from fvm2d_gb300.ogrid import workload_grid  # noqa: E402
+
+EULER = dict(mach=0.8, aoa_deg=1.25, cfl=1.0)
+LAMINAR = dict(iflow=L.LAMINAR, mach=0.5, aoa_deg=0.0, rey=5000.0, cfl=0.8, iflux=L.ROE)
+RANS = dict(iflow=L.TURBULENT, mach=0.7, aoa_deg=2.0, rey=6.5e6, cfl=0.5, iflux=L.HLLC,
+            nut_ratio=3.0, bugcompat=0)
+
+REDUCTION_RTOL = 1e-12        # FP64 sums over all vertices / wall edges, other order
+HISTORY_RTOL = 1e-10          # residual history, transcendental paths
+STATE_RTOL = 1e-9             # state after a few iterations, transcendental paths (the
+                              # few-ulp libm differences grow through the limiter)
+FP32_STATE_RTOL = 1e-5        # FP32 state vs FP64 after a few iterations
+FP32_FRES_RTOL = 1e-3         # FP32 residual history vs FP64
+FP32_CL_ABS, FP32_CD_ABS = 1e-4, 2e-5
+
+
+def rel_err(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def euler_grid():
+    return workload_grid("euler_1024x384")
+
+
+def pair(oracle_lib, fvm_lib, grid, **kw):
+    o = oracle_lib.Oracle(grid.coord, grid.elem, grid.ptype, **kw)
+    s = fvm_lib.Solver(fvm_lib.make_params(precision=L.FP64, **kw), o.mesh_arrays())
+    s.set_state(o.d("prim"), o.d("nut"), o.d("mul"), o.d("mu"), iterlast=0)
+    return o, s
+
+
+def test_euler_1024x384_roe_bitwise(oracle_lib, fvm_lib, euler_grid):
+    o, s = pair(oracle_lib, fvm_lib, euler_grid, iflux=L.ROE, **EULER)
+    st, h = s.iterate(3)
+    ost, oh = o.iterate(3)
+    assert st == ost == 0
+    np.testing.assert_array_equal(s.get_state()["prim"], o.d("prim"))
+    np.testing.assert_array_equal(h["iresi"], oh["iresi"])
+    np.testing.assert_array_equal(h["fresi"], oh["fresi"])
+    # the norm's sum of squares and the force sums are reductions over
+    # blocks on the GPU, serial chains in the oracle: a few ulp apart
+    assert rel_err(h["fres"], oh["fres"]) <= REDUCTION_RTOL
+    assert rel_err(h["cl"], oh["cl"]) <= REDUCTION_RTOL
+    assert rel_err(h["cd"], oh["cd"]) <= REDUCTION_RTOL
+
+
+@pytest.mark.parametrize("iflux", [L.KFVS, L.HLLC])
+def test_euler_1024x384_kfvs_hllc(oracle_lib, fvm_lib, euler_grid, iflux):
+    o, s = pair(oracle_lib, fvm_lib, euler_grid, iflux=iflux, bugcompat=0, **EULER)
+    st, h = s.iterate(3)
+    ost, oh = o.iterate(3)
+    assert st == ost == 0
+    assert rel_err(h["fres"], oh["fres"]) <= HISTORY_RTOL
+    assert rel_err(s.get_state()["prim"], o.d("prim")) <= STATE_RTOL
+
+
+def test_laminar_512x192(oracle_lib, fvm_lib):
+    o, s = pair(oracle_lib, fvm_lib, workload_grid("laminar_512x192"), **LAMINAR)
+    st, h = s.iterate(3)
+    ost, oh = o.iterate(3)
+    assert st == ost == 0
+    assert rel_err(h["fres"], oh["fres"]) <= HISTORY_RTOL
+    assert abs(h["cd"][-1] - oh["cd"][-1]) <= 1e-8
+    assert rel_err(s.get_state()["prim"], o.d("prim")) <= STATE_RTOL
+
+
+def test_rans_sa_768x256(oracle_lib, fvm_lib):
+    o, s = pair(oracle_lib, fvm_lib, workload_grid("rans_768x256"), **RANS)
+    st, h = s.iterate(2)
+    ost, oh = o.iterate(2)
+    assert st == ost == 0
+    assert rel_err(h["fres"], oh["fres"]) <= HISTORY_RTOL
+    got = s.get_state()
+    assert rel_err(got["prim"], o.d("prim")) <= STATE_RTOL
+    assert rel_err(got["nut"], o.d("nut")) <= STATE_RTOL
+
+
+def test_fp32_batch_1024x384_tracks_fp64(oracle_lib, fvm_lib, euler_grid):
+    """FP32 state and fluxes, FP64 geometry and norms: the state after five
+    iterations against the oracle's FP64 state."""
+    o = oracle_lib.Oracle(euler_grid.coord, euler_grid.elem, euler_grid.ptype,
+                          iflux=L.ROE, **EULER)
+    m = o.mesh_arrays()
+    b = Batch(L.FP32, vertices=euler_grid.coord.shape[0], meshes=1)
+    slot = b.add(fvm_lib.make_params(precision=L.FP32, iflux=L.ROE, **EULER), m)
+    b.start(slot, 5)
+    b.step(5)
+    b.sync()
+    q = b.poll(slot)
+    assert q["status"] == 0 and q["niter"] == 5
+    h = b.history(slot, 0, 5)
+    ost, oh = o.iterate(5)
+    assert ost == 0
+    assert rel_err(b.get_state(slot)["prim"], o.d("prim")) <= FP32_STATE_RTOL
+    assert rel_err(h["fres"], oh["fres"]) <= FP32_FRES_RTOL
+
+
+def test_fp32_converged_lift_drag_160x48(oracle_lib, fvm_lib):
+    """2000 iterations of the 160 x 48 Euler case (Roe + limiter): FP32 lift
+    and drag against the FP64 oracle's."""
+    g = workload_grid("euler_160x48")
+    o = oracle_lib.Oracle(g.coord, g.elem, g.ptype, iflux=L.ROE, **EULER)
+    b = Batch(L.FP32, vertices=g.coord.shape[0], meshes=1)
+    slot = b.add(fvm_lib.make_params(precision=L.FP32, iflux=L.ROE, **EULER), o.mesh_arrays())
+    b.start(slot, 2000)
+    b.step(2000)
+    b.sync()
+    q = b.poll(slot)
+    assert q["status"] == 0 and q["niter"] == 2000
+    ost, oh = o.iterate(2000)
+    assert ost == 0
+    assert abs(q["cl"] - oh["cl"][-1]) <= FP32_CL_ABS
+    assert abs(q["cd"] - oh["cd"][-1]) <= FP32_CD_ABS
