@@ -1397,6 +1397,39 @@ __global__ void __launch_bounds__(kBlockVerts) k_sa(ArenaPtrs<R> A, int stage, i
 // stop test of main.f:42.  FP64 arithmetic; the clcd sum is the serial
 // Fortran chain when serial_clcd is set.
 // ---------------------------------------------------------------------------
+// One solid edge's pressure and viscous force (clcd.f:20-40), added to
+// (xf, yf).  FP32 states: the terms from the FP32 values (the edge vector
+// an FP64 difference rounded once), accumulated in FP64.
+template <typename R>
+__device__ __forceinline__ void wall_force(double2 c1, double2 c2, R mu1, R mu2, const Grad<R> &g1,
+                                           const Grad<R> &g2, R p1, R p2, double &xf,
+                                           double &yf) {
+  if constexpr (sizeof(R) == 4) {
+    const float sx = float(c2.y - c1.y), sy = -float(c2.x - c1.x);
+    const float n2b3 = 2.0f / 3.0f;
+    const float txx = 0.5f * (n2b3 * mu1 * (2.0f * g1.qx[1] - g1.qy[2]) +
+                              n2b3 * mu2 * (2.0f * g2.qx[1] - g2.qy[2]));
+    const float txy = 0.5f * (mu1 * (g1.qy[1] + g1.qx[2]) + mu2 * (g2.qy[1] + g2.qx[2]));
+    const float tyy = 0.5f * (n2b3 * mu1 * (2.0f * g1.qy[2] - g1.qx[1]) +
+                              n2b3 * mu2 * (2.0f * g2.qy[2] - g2.qx[1]));
+    const float pp = 0.5f * (p1 + p2);
+    xf += double(pp * sx - txx * sx - txy * sy);
+    yf += double(pp * sy - txy * sx - tyy * sy);
+  } else {
+    const double dx = c2.x - c1.x, dy = c2.y - c1.y;
+    const double sx = dy, sy = -dx;
+    const double txx = 0.5 * (2.0 / 3.0 * mu1 * (2.0 * double(g1.qx[1]) - double(g1.qy[2])) +
+                              2.0 / 3.0 * mu2 * (2.0 * double(g2.qx[1]) - double(g2.qy[2])));
+    const double txy = 0.5 * (mu1 * (double(g1.qy[1]) + double(g1.qx[2])) +
+                              mu2 * (double(g2.qy[1]) + double(g2.qx[2])));
+    const double tyy = 0.5 * (2.0 / 3.0 * mu1 * (2.0 * double(g1.qy[2]) - double(g1.qx[1])) +
+                              2.0 / 3.0 * mu2 * (2.0 * double(g2.qy[2]) - double(g2.qx[1])));
+    const double pp = 0.5 * (double(p1) + double(p2));
+    xf += pp * sx - txx * sx - txy * sy;
+    yf += pp * sy - txy * sx - tyy * sy;
+  }
+}
+
 template <typename R>
 __device__ void clcd_block(const ArenaPtrs<R> &A, const MeshConst &mc, int mesh_phase,
                            int serial, double &cl, double &cd) {
@@ -1427,56 +1460,35 @@ __device__ void clcd_block(const ArenaPtrs<R> &A, const MeshConst &mc, int mesh_
         yf = yf + pp * sy - txy * sx - tyy * sy;
       }
     }
-  } else if constexpr (sizeof(R) == 4) {
-    // FP32 states: each edge's force terms from the FP32 values (the edge
-    // vector an FP64 difference rounded once), accumulated in FP64
-    for (int i = threadIdx.x; i < mc.nsw; i += blockDim.x) {
-      const int2 nn = A.sw_nodes[mc.sw0 + i];
-      const double2 c1 = A.coord[nn.x], c2 = A.coord[nn.y];
-      const float sx = float(c2.y - c1.y), sy = -float(c2.x - c1.x);
-      const float mu1 = A.mu[nn.x], mu2 = A.mu[nn.y];
-      const Grad<R> g1 = A.grad[nn.x], g2 = A.grad[nn.y];
-      const float p1 = P[nn.x].w, p2 = P[nn.y].w;
-      const float n2b3 = 2.0f / 3.0f;
-      const float txx = 0.5f * (n2b3 * mu1 * (2.0f * g1.qx[1] - g1.qy[2]) +
-                                n2b3 * mu2 * (2.0f * g2.qx[1] - g2.qy[2]));
-      const float txy = 0.5f * (mu1 * (g1.qy[1] + g1.qx[2]) + mu2 * (g2.qy[1] + g2.qx[2]));
-      const float tyy = 0.5f * (n2b3 * mu1 * (2.0f * g1.qy[2] - g1.qx[1]) +
-                                n2b3 * mu2 * (2.0f * g2.qy[2] - g2.qx[1]));
-      const float pp = 0.5f * (p1 + p2);
-      xf += double(pp * sx - txx * sx - txy * sy);
-      yf += double(pp * sy - txy * sx - tyy * sy);
-    }
-    s_x[threadIdx.x] = xf;
-    s_y[threadIdx.x] = yf;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-      if (threadIdx.x < s) {
-        s_x[threadIdx.x] += s_x[threadIdx.x + s];
-        s_y[threadIdx.x] += s_y[threadIdx.x + s];
-      }
-      __syncthreads();
-    }
-    xf = s_x[0];
-    yf = s_y[0];
   } else {
-    for (int i = threadIdx.x; i < mc.nsw; i += blockDim.x) {
-      const int2 nn = A.sw_nodes[mc.sw0 + i];
-      const double2 c1 = A.coord[nn.x], c2 = A.coord[nn.y];
-      const double dx = c2.x - c1.x, dy = c2.y - c1.y;
-      const double sx = dy, sy = -dx;
-      const double mu1 = double(A.mu[nn.x]), mu2 = double(A.mu[nn.y]);
-      const Grad<R> g1 = A.grad[nn.x], g2 = A.grad[nn.y];
-      const double p1 = double(P[nn.x].w), p2 = double(P[nn.y].w);
-      const double txx = 0.5 * (2.0 / 3.0 * mu1 * (2.0 * double(g1.qx[1]) - double(g1.qy[2])) +
-                                2.0 / 3.0 * mu2 * (2.0 * double(g2.qx[1]) - double(g2.qy[2])));
-      const double txy = 0.5 * (mu1 * (double(g1.qy[1]) + double(g1.qx[2])) +
-                                mu2 * (double(g2.qy[1]) + double(g2.qx[2])));
-      const double tyy = 0.5 * (2.0 / 3.0 * mu1 * (2.0 * double(g1.qy[2]) - double(g1.qx[1])) +
-                                2.0 / 3.0 * mu2 * (2.0 * double(g2.qy[2]) - double(g2.qx[1])));
-      const double pp = 0.5 * (p1 + p2);
-      xf += pp * sx - txx * sx - txy * sy;
-      yf += pp * sy - txy * sx - tyy * sy;
+    // each thread's edges i, i + blockDim, ... summed in that order, with
+    // the loads of four edges issued together per trip
+    constexpr int kU = 4;
+    const int nt = (int)blockDim.x;
+    for (int i0 = threadIdx.x; i0 < mc.nsw; i0 += kU * nt) {
+      int2 nn[kU];
+#pragma unroll
+      for (int u = 0; u < kU; u++)
+        nn[u] = (i0 + u * nt < mc.nsw) ? A.sw_nodes[mc.sw0 + i0 + u * nt] : make_int2(0, 0);
+      double2 c1[kU], c2[kU];
+      R mu1[kU], mu2[kU], p1[kU], p2[kU];
+      Grad<R> g1[kU], g2[kU];
+#pragma unroll
+      for (int u = 0; u < kU; u++) {
+        c1[u] = A.coord[nn[u].x];
+        c2[u] = A.coord[nn[u].y];
+        mu1[u] = A.mu[nn[u].x];
+        mu2[u] = A.mu[nn[u].y];
+        g1[u] = A.grad[nn[u].x];
+        g2[u] = A.grad[nn[u].y];
+        p1[u] = P[nn[u].x].w;
+        p2[u] = P[nn[u].y].w;
+      }
+#pragma unroll
+      for (int u = 0; u < kU; u++) {
+        if (i0 + u * nt >= mc.nsw) break;
+        wall_force<R>(c1[u], c2[u], mu1[u], mu2[u], g1[u], g2[u], p1[u], p2[u], xf, yf);
+      }
     }
     s_x[threadIdx.x] = xf;
     s_y[threadIdx.x] = yf;
@@ -1504,16 +1516,18 @@ __device__ void conres_block(const ArenaPtrs<R> &A, const MeshConst &mc, double 
   double s = 0.0, m = 0.0;
   int a = INT_MAX;
   // the mesh's partials are contiguous (block k's record is blk0 + k);
-  // four loads in flight per thread, folded in index order
-  for (int i0 = threadIdx.x; i0 < mc.nblk; i0 += 4 * blockDim.x) {
-    BlockPartial bp[4];
+  // eight loads in flight per thread (a 2048-block mesh in one trip),
+  // folded in index order
+  constexpr int kU = 8;
+  for (int i0 = threadIdx.x; i0 < mc.nblk; i0 += kU * blockDim.x) {
+    BlockPartial bp[kU];
 #pragma unroll
-    for (int u = 0; u < 4; u++) {
+    for (int u = 0; u < kU; u++) {
       const int i = i0 + u * (int)blockDim.x;
       if (i < mc.nblk) bp[u] = A.part[mc.blk0 + i];
     }
 #pragma unroll
-    for (int u = 0; u < 4; u++) {
+    for (int u = 0; u < kU; u++) {
       if (i0 + u * (int)blockDim.x >= mc.nblk) break;
       s += bp[u].sumsq;
       if (bp[u].maxabs > m || (bp[u].maxabs == m && bp[u].argmax < a)) {
