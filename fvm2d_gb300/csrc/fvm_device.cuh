@@ -250,41 +250,29 @@ __device__ __forceinline__ void hllc_flux(R ct, R st, R length, const R pl4[4], 
   R Sl = ul - al * ql;
   R Ss = ustar;
   R Sr = ur + ar * qr;
-  R f0, f1, f2, f3;
-  if (R(0) <= Sl) {
-    f0 = rl * ul;
-    f1 = pl + rl * sq(ul);
-    f2 = rl * ul * vl;
-    f3 = (El + pl) * ul;
-  } else if (Sl <= R(0) && R(0) <= Ss) {
-    R fl0 = rl * ul, fl1 = pl + rl * sq(ul), fl2 = rl * ul * vl, fl3 = (El + pl) * ul;
-    R fact = mdiv(rl * (Sl - ul), Sl - Ss);
-    R du0 = fact - rl;
-    R du1 = fact * Ss - rl * ul;
-    R du2 = fact * vl - rl * vl;
-    R t1 = mdiv(El, rl) + (Ss - ul) * (Ss + mdiv(mdiv(pl, rl), Sl - ul));
-    R du3 = fact * t1 - El;
-    f0 = fl0 + Sl * du0;
-    f1 = fl1 + Sl * du1;
-    f2 = fl2 + Sl * du2;
-    f3 = fl3 + Sl * du3;
-  } else if (Ss <= R(0) && R(0) <= Sr) {
-    R fr0 = rr * ur, fr1 = pr + rr * sq(ur), fr2 = rr * ur * vr, fr3 = (Er + pr) * ur;
-    R fact = mdiv(rr * (Sr - ur), Sr - Ss);
-    R du0 = fact - rr;
-    R du1 = fact * Ss - rr * ur;
-    R du2 = fact * vr - rr * vr;
-    R t1 = mdiv(Er, rr) + (Ss - ur) * (Ss + mdiv(mdiv(pr, rr), Sr - ur));
-    R du3 = fact * t1 - Er;
-    f0 = fr0 + Sr * du0;
-    f1 = fr1 + Sr * du1;
-    f2 = fr2 + Sr * du2;
-    f3 = fr3 + Sr * du3;
-  } else {
-    f0 = rr * ur;
-    f1 = pr + rr * sq(ur);
-    f2 = rr * ur * vr;
-    f3 = (Er + pr) * ur;
+  // hllc_flux.f:105-147: F(U_L) if 0 <= Sl; F_L + Sl (U*_L - U_L) if
+  // Sl <= 0 <= Ss; F_R + Sr (U*_R - U_R) if Ss <= 0 <= Sr; else F(U_R).
+  // The side is chosen first and its terms computed once, with the same
+  // operations as the branch it stands for, so a warp whose edges fall in
+  // different cases does not run both sides.
+  const bool c1 = R(0) <= Sl;
+  const bool c2 = !c1 && Sl <= R(0) && R(0) <= Ss;
+  const bool c3 = !c1 && !c2 && Ss <= R(0) && R(0) <= Sr;
+  const bool left = c1 || c2, star = c2 || c3;
+  const R rk = left ? rl : rr, uk = left ? ul : ur, vk = left ? vl : vr;
+  const R pk = left ? pl : pr, Ek = left ? El : Er, Sk = left ? Sl : Sr;
+  R f0 = rk * uk, f1 = pk + rk * sq(uk), f2 = rk * uk * vk, f3 = (Ek + pk) * uk;
+  if (star) {
+    R fact = mdiv(rk * (Sk - uk), Sk - Ss);
+    R du0 = fact - rk;
+    R du1 = fact * Ss - rk * uk;
+    R du2 = fact * vk - rk * vk;
+    R t1 = mdiv(Ek, rk) + (Ss - uk) * (Ss + mdiv(mdiv(pk, rk), Sk - uk));
+    R du3 = fact * t1 - Ek;
+    f0 = f0 + Sk * du0;
+    f1 = f1 + Sk * du1;
+    f2 = f2 + Sk * du2;
+    f3 = f3 + Sk * du3;
   }
   if (rotate_back) {
     R fn = f1, ft = f2;
