@@ -833,24 +833,23 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_FLUX_MINB32 
     const MeshConst &mc = A.mc[bi.mesh];
     const int p = ctl.phase;
     const R4<R> *P = A.st[cur_buf(p, stage)];
-    if (threadIdx.x == 0) {
+    // FP64: the next block's inputs into L2.  Not in FP32, where the same
+    // prefetches made the pass slower (0.206 -> 0.216 ms on 8 meshes of
+    // 1024 x 384 timed alone; whole iterations 1.025 -> 1.040 ms).
+    if (sizeof(R) == 8 && threadIdx.x == 0) {
       const BlockInfo *nb = next_block(A.blocks, A.work, w, nwork);
       if (nb) {
         const BlockInfo n = *nb;
-        if (sizeof(R) == 8) {
-          prefetch_l2(A.be_nodes + n.e0, sizeof(int2) * n.ne);
-          prefetch_l2(A.be_csl + n.e0, sizeof(D4) * n.ne);
-        } else {
-          prefetch_l2(A.be_g32 + n.e0, sizeof(EdgeGeo32) * n.ne);
-        }
+        prefetch_l2(A.be_nodes + n.e0, sizeof(int2) * n.ne);
+        prefetch_l2(A.be_csl + n.e0, sizeof(D4) * n.ne);
         prefetch_l2(P + n.v0, sizeof(R4<R>) * n.nv);
         prefetch_l2(A.grad + n.v0, sizeof(Grad<R>) * n.nv);
-        if (sizeof(R) == 8) prefetch_l2(A.coord + n.v0, sizeof(double2) * n.nv);
+        prefetch_l2(A.coord + n.v0, sizeof(double2) * n.nv);
         prefetch_l2(A.ve_rng + n.v0, sizeof(int2) * n.nv);
         if (mode == MODE_UPDATE) {
           prefetch_l2(A.st[old_buf(p, stage)] + n.v0, sizeof(R4<R>) * n.nv);
           prefetch_l2(A.dt + n.v0, sizeof(R) * n.nv);
-          prefetch_l2(sizeof(R) == 4 ? (const void *)(A.cvarea32 + n.v0) : (const void *)(A.cvarea + n.v0), sizeof(R) * n.nv);
+          prefetch_l2(A.cvarea + n.v0, sizeof(R) * n.nv);
         }
       }
     }
