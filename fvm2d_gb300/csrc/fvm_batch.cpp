@@ -418,7 +418,8 @@ int32_t update_work(fvm_batch *b) {
   // small changes of the mix keep the graph), never above the arena's
   // capacities: smaller tiles let more CTAs share an SM.
   int tile[4] = {0, 0, 0, 0};
-  bool any_visc = false, any_turb = false;
+  int max_halo = 0;
+  bool any_visc = false, any_turb = false, tri_loc = true;
   for (const Slot &s : b->slots)
     if (s.used) {
       any_visc |= s.par.iflow != FVM_INVISCID;
@@ -427,10 +428,19 @@ int32_t update_work(fvm_batch *b) {
       tile[1] = std::max(tile[1], s.L.max_slots);
       tile[2] = std::max(tile[2], s.L.max_tri2);
       tile[3] = std::max(tile[3], s.L.max_loc);
+      max_halo = std::max(max_halo, s.L.max_halo);
+      tri_loc &= s.L.max_loc <= kTriLocMax;
     }
+  // the bulk gradient pass's halo ids (rounded up to 8 like the tiles; a
+  // block of more than kTriLocMax own + halo vertices sends the pass to its
+  // per-thread form while its mesh is resident)
+  max_halo = std::min((max_halo + 7) & ~7, kTriLocMax);
+  bool changed_halo = max_halo != b->cfg.max_halo || tri_loc != b->cfg.tri_loc;
+  b->cfg.max_halo = max_halo;
+  b->cfg.tri_loc = tri_loc;
   const int cap[4] = {b->caps.max_tri, b->caps.max_slots, b->caps.max_tri2, b->caps.max_loc};
   int *cur[4] = {&b->cfg.max_tri, &b->cfg.max_slots, &b->cfg.max_tri2, &b->cfg.max_loc};
-  bool changed = flux != b->cfg.flux;
+  bool changed = flux != b->cfg.flux || changed_halo;
   b->cfg.flux = flux;
   for (int i = 0; i < 4; i++) {
     if (!tile[i]) continue;             // empty batch: keep the current tiles
@@ -771,11 +781,13 @@ extern "C" int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *cap
   b->cfg.max_tri = c.max_tri;
   b->cfg.max_tri2 = c.max_tri2;
   b->cfg.max_loc = c.max_loc;
+  b->cfg.max_halo = 0;
+  b->cfg.tri_loc = true;
   b->fused = b->fused_wanted = c.fused > 0;
   b->chains = std::min(std::max(c.overlap, 1), kMaxChains);
   // gradient pass: bulk-copy staging by default in FP32 (when its shared
   // memory fits), per-thread loads in FP64
-  const bool bulk_fits = grad_bulk_layout(c.max_tri, c.viscous != 0).total <= kMaxSmem;
+  const bool bulk_fits = grad_bulk_layout(c.max_tri, kTriLocMax, c.viscous != 0).total <= kMaxSmem;
   b->cfg.grad_mode = c.grad_mode > 0 ? c.grad_mode
                                       : (precision == FVM_PREC_FP32 && bulk_fits ? 3 : 1);
   if (b->cfg.grad_mode < 1 || b->cfg.grad_mode > 3 ||
@@ -898,7 +910,7 @@ extern "C" int32_t fvm_batch_prepare(const fvm_params *par, const fvm_mesh *m, f
     g.dbyy[1] = (float)(x1 - x3);
     g.dbyy[2] = (float)(x2 - x1);
     g.areat = (float)(0.25 / m->elarea[t]);
-    g.pad = 0.f;
+    g.loc = L.bt_loc[k];
     P->tri_g32[k] = g;
   }
   *out = P;
@@ -1251,7 +1263,7 @@ constexpr int kForms = 8;
 
 static Form form_of(const fvm_batch *b, int i) {
   const bool bulk = b->prec == FVM_PREC_FP32 &&
-                    grad_bulk_layout(b->caps.max_tri, b->caps.viscous != 0).total <= kMaxSmem;
+                    grad_bulk_layout(b->caps.max_tri, kTriLocMax, b->caps.viscous != 0).total <= kMaxSmem;
   const int g = bulk ? 3 : 1;
   const Form f[kForms] = {{false, 3, 1}, {false, 1, 1}, {false, 2, 1}, {true, 1, 1},
                           {false, g, 2}, {true, 1, 2},  {false, g, 4}, {false, g, 8}};
@@ -1260,7 +1272,7 @@ static Form form_of(const fvm_batch *b, int i) {
 
 static bool form_fits(const fvm_batch *b, const Form &f) {
   const bool fp32 = b->prec == FVM_PREC_FP32;
-  if (f.grad == 3 && !(fp32 && grad_bulk_layout(b->caps.max_tri, b->caps.viscous != 0).total <= kMaxSmem))
+  if (f.grad == 3 && !(fp32 && grad_bulk_layout(b->caps.max_tri, kTriLocMax, b->caps.viscous != 0).total <= kMaxSmem))
     return false;
   if (f.fused) {
     const size_t sm = fp32 ? smem_step(b->cfg, (float *)nullptr) : smem_step(b->cfg, (double *)nullptr);

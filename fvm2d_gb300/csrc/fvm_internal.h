@@ -71,24 +71,24 @@ constexpr int kMaxChains = 8;
 #endif
 
 // Shared memory of the bulk-copy gradient pass (FP32): the block's triangle
-// entries (16 B), their geometry (32 B, overwritten in place by the
-// triangle sums), the viscous terms (9 values), the vertices' incidence
-// ranges and the incidence list (both copied in 16-byte units), and the
-// states of the block's own vertices.
+// records (geometry and the ends' local slots, 32 B, overwritten in place
+// by the triangle sums), the viscous terms (9 values), the vertices'
+// incidence ranges and the incidence list (both copied in 16-byte units),
+// the states of the block's own vertices and the ids of its halo vertices.
 struct GradBulkLayout {
-  uint32_t bt, geo, vis, vtr, vtl, pv, total;
+  uint32_t geo, vis, vtr, vtl, pv, halo, total;
 };
 FVM_HD inline uint32_t fvm_up16(uint32_t x) { return (x + 15u) & ~15u; }
-FVM_HD inline GradBulkLayout grad_bulk_layout(int max_tri, bool viscous) {
+FVM_HD inline GradBulkLayout grad_bulk_layout(int max_tri, int max_halo, bool viscous) {
   GradBulkLayout l;
   const uint32_t mt = (uint32_t)max_tri;
-  l.bt = 0;
-  l.geo = fvm_up16(mt * 16u);
-  l.vis = l.geo + fvm_up16(mt * 32u);
+  l.geo = 0;
+  l.vis = fvm_up16(mt * 32u);
   l.vtr = l.vis + (viscous ? fvm_up16(mt * 36u) : 0u);
   l.vtl = l.vtr + fvm_up16((uint32_t)(kBlockVerts + kVertAlign) * 8u);
   l.pv = l.vtl + fvm_up16((3u * mt + 16u) * 2u);
-  l.total = l.pv + (uint32_t)kBlockVerts * 16u;
+  l.halo = l.pv + (uint32_t)kBlockVerts * 16u;
+  l.total = l.halo + fvm_up16((uint32_t)max_halo * 4u);
   return l;
 }
 
@@ -170,8 +170,14 @@ struct alignas(32) D4 {
 struct alignas(16) TriGeo32 {
   float dbxx[3], dbyy[3];   // green_gauss.f:108-113: y2-y3, y3-y1, y1-y2 / x3-x2, x1-x3, x2-x1
   float areat;              // 0.25/elarea (green_gauss.f:180)
-  float pad;
+  uint32_t loc;             // the three ends' block-local slots (kTriLocBits each), or kTriNoLoc
 };
+// Block-local slot of a vertex: own vertices 0..nv-1, then the block's halo
+// vertices (halo_ids order).  Three slots of kTriLocBits bits fit one word
+// when the block has at most kTriLocMax own + halo vertices.
+constexpr int kTriLocBits = 10;
+constexpr int kTriLocMax = 1 << kTriLocBits;
+constexpr uint32_t kTriNoLoc = 0xffffffffu;
 
 // One interior edge entry of a block for the FP32 kernels: its ends, the
 // FP64 edge vector and dual-face normal rounded once to FP32 (flux.f:10-13

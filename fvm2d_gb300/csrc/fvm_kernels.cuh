@@ -399,12 +399,13 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRAD_MINB32 
 // returns.
 template <typename R>
 __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRAD_MINB32 : 1)
-    k_grad_bulk(ArenaPtrs<R> A, int stage, int do_dt, int routine, int max_tri, int viscous) {
+    k_grad_bulk(ArenaPtrs<R> A, int stage, int do_dt, int routine, int max_tri, int max_halo,
+                int viscous) {
   if constexpr (sizeof(R) == 4) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bar;
-    const GradBulkLayout lay = grad_bulk_layout(max_tri, viscous != 0);
-    int4 *s_bt = reinterpret_cast<int4 *>(smem_raw + lay.bt);
+    const GradBulkLayout lay = grad_bulk_layout(max_tri, max_halo, viscous != 0);
+    int *s_halo = reinterpret_cast<int *>(smem_raw + lay.halo);
     const TriGeo32 *s_geo = reinterpret_cast<const TriGeo32 *>(smem_raw + lay.geo);
     TriSmem<R> *s_tri = reinterpret_cast<TriSmem<R> *>(smem_raw + lay.geo);   // in place
     R *s_vis = reinterpret_cast<R *>(smem_raw + lay.vis);
@@ -425,12 +426,14 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRAD_MINB32 
       const R4<R> *P = A.st[cur_buf(ctl.phase, stage)];
       const int vt_a = bi.vt0 & ~7;                       // 16-byte units of uint16
       const int vt_b = (bi.vt0 + bi.nvt + 7) & ~7;
+      // the halo vertices' ids, for the records' local slots (plain loads,
+      // in flight during the copies)
+      for (int h = threadIdx.x; h < bi.nh; h += blockDim.x) s_halo[h] = A.halo_ids[bi.h0 + h];
       if (threadIdx.x == 0) {
-        const uint32_t nbt = 16u * bi.nt, ngeo = 32u * bi.nt;
+        const uint32_t ngeo = 32u * bi.nt;
         const uint32_t nvtr = 8u * ((bi.nv + 1) & ~1), nvtl = 2u * (vt_b - vt_a);
         const uint32_t npv = 16u * bi.nv;
-        mbar_expect_tx(&bar, nbt + ngeo + nvtr + nvtl + npv);
-        if (nbt) bulk_g2s(s_bt, A.bt_nodes + bi.t0, nbt, &bar);
+        mbar_expect_tx(&bar, ngeo + nvtr + nvtl + npv);
         if (ngeo) bulk_g2s((void *)s_geo, A.tri_g32 + bi.t0, ngeo, &bar);
         bulk_g2s(s_vtr, A.vt_rng + bi.v0, nvtr, &bar);
         if (nvtl) bulk_g2s(s_vtl, A.vt_list + vt_a, nvtl, &bar);
@@ -438,12 +441,12 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRAD_MINB32 
         const BlockInfo *nb = next_block(A.blocks, A.work, w, nwork);
         if (nb) {
           const BlockInfo n = *nb;
-          prefetch_l2(A.bt_nodes + n.t0, sizeof(int4) * n.nt);
           prefetch_l2(A.tri_g32 + n.t0, sizeof(TriGeo32) * n.nt);
           prefetch_l2(P + n.v0, sizeof(R4<R>) * n.nv);
           prefetch_l2(A.vt_rng + n.v0, sizeof(int2) * n.nv);
           prefetch_l2(A.vt_list + n.vt0, sizeof(uint16_t) * n.nvt);
           prefetch_l2(A.ais32 + n.v0, sizeof(float) * n.nv);
+          prefetch_l2(A.halo_ids + n.h0, sizeof(int) * n.nh);
         }
       }
       const bool late = !mbar_wait_bounded(&bar, parity);
@@ -452,15 +455,21 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRAD_MINB32 
         if (threadIdx.x == 0) atomicCAS(&A.ctl[bi.mesh].err, 0, 6 /* FVM_ERR_TIMEOUT */);
         return;
       }
-      // phase 1: one thread per triangle touching the block
-      auto state = [&](int v) {   // own vertices from shared memory
-        const unsigned l = (unsigned)(v - bi.v0);
-        return l < (unsigned)bi.nv ? s_pv[l] : P[v];
+      // phase 1: one thread per triangle touching the block; its ends by
+      // local slot: own vertices' states from shared memory, the halo's
+      // from global memory
+      auto state = [&](uint32_t l) {
+        return l < (uint32_t)bi.nv ? s_pv[l] : P[s_halo[l - bi.nv]];
+      };
+      auto vertex = [&](uint32_t l) {
+        return l < (uint32_t)bi.nv ? bi.v0 + (int)l : s_halo[l - bi.nv];
       };
       for (int k = threadIdx.x; k < bi.nt; k += blockDim.x) {
-        const int4 t = s_bt[k];
-        const R4<R> p1 = state(t.x), p2 = state(t.y), p3 = state(t.z);
         const TriGeo32 tg = s_geo[k];
+        constexpr uint32_t lm = (uint32_t)(kTriLocMax - 1);
+        const uint32_t l1 = tg.loc & lm, l2 = (tg.loc >> kTriLocBits) & lm,
+                       l3 = (tg.loc >> (2 * kTriLocBits)) & lm;
+        const R4<R> p1 = state(l1), p2 = state(l2), p3 = state(l3);
         R dbxx[3], dbyy[3];
 #pragma unroll
         for (int j = 0; j < 3; j++) {
@@ -470,6 +479,7 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRAD_MINB32 
         TriSmem<R> ts;
         tri_sums<R>(p1, p2, p3, dbxx, dbyy, ts);
         if (visc) {
+          const int4 t = make_int4(vertex(l1), vertex(l2), vertex(l3), 0);
           const TriVisc<R> tv = tri_visc<R>(A, mc, ctl.nphase, t, tg.areat, p1, p2, p3, dbxx, dbyy, ts);
           R *sv = s_vis + 9 * k;
 #pragma unroll

@@ -43,12 +43,12 @@ inline int fit_grid(const LaunchCfg &c, K kern, size_t smem) {
       k_grad_v<R><<<fit_grid(c, k_grad_v<R>, 0), kBlockVerts, 0, c.stream>>>(A, stage, do_dt, routine); \
       return cudaGetLastError();                                                           \
     }                                                                                      \
-    if (c.grad_mode == 3) {                                                                \
+    if (c.grad_mode == 3 && c.tri_loc) {  /* else the per-thread form, same sums */      \
       if (sizeof(R) != 4) return cudaErrorNotSupported;                                    \
-      const size_t sb = grad_bulk_layout(c.max_tri, c.viscous).total;                      \
+      const size_t sb = grad_bulk_layout(c.max_tri, c.max_halo, c.viscous).total;          \
       if (sb > kMaxSmem) return cudaErrorInvalidConfiguration;                            \
       k_grad_bulk<R><<<fit_grid(c, k_grad_bulk<R>, sb), kBlockVerts, sb, c.stream>>>(       \
-          A, stage, do_dt, routine, c.max_tri, c.viscous ? 1 : 0);                         \
+          A, stage, do_dt, routine, c.max_tri, c.max_halo, c.viscous ? 1 : 0);             \
       return cudaGetLastError();                                                           \
     }                                                                                      \
     k_grad<R><<<fit_grid(c, k_grad<R>, sm), kBlockVerts, sm, c.stream>>>(A, stage, do_dt, routine, c.max_tri);  \
@@ -147,7 +147,7 @@ inline int fit_grid(const LaunchCfg &c, K kern, size_t smem) {
       e = cudaFuncSetAttribute(k_flux<R, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f); \
     if (e == cudaSuccess)                                                                  \
       e = cudaFuncSetAttribute(k_sa<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s); \
-    const size_t gb = grad_bulk_layout(c.max_tri, c.viscous).total;                        \
+    const size_t gb = grad_bulk_layout(c.max_tri, kTriLocMax, c.viscous).total;            \
     if (e == cudaSuccess && sizeof(R) == 4 && gb <= kMaxSmem)                              \
       e = cudaFuncSetAttribute(k_grad_bulk<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gb); \
     return e;                                                                              \

@@ -22,6 +22,8 @@ struct LaunchCfg {
   bool fit;          // grid = CTAs resident at once (occupancy x sms), capped by grid
   int grad_mode;     // gradient pass: 1 loads per thread (k_grad), 2 per vertex
                      // (k_grad_v), 3 bulk copies to shared memory (k_grad_bulk, FP32)
+  int max_halo;      // max halo vertices of a block (k_grad_bulk's halo ids)
+  bool tri_loc;      // every resident block's triangle records carry local slots
   cudaStream_t stream;
 };
 

@@ -231,6 +231,7 @@ int32_t build_layout(const fvm_mesh &m, int bv, MeshLayout &L) {
     BlockInfo &bi = L.blocks[b];
     bi.h0 = (int)L.halo_ids.size();
     bi.nh = (int)halo.size();
+    L.max_halo = std::max(L.max_halo, bi.nh);
     L.halo_ids.insert(L.halo_ids.end(), halo.begin(), halo.end());
     const int nloc = bi.nv + bi.nh;
     if (nloc > 0xffff) return FVM_ERR_CAPACITY;
@@ -302,6 +303,14 @@ int32_t build_layout(const fvm_mesh &m, int bv, MeshLayout &L) {
       int n[3];
       for (int q = 0; q < 3; q++) n[q] = L.iperm[m.elem[3 * t + q] - 1];
       L.bt_nodes.push_back(make_int4(n[0], n[1], n[2], t));
+      uint32_t lc = 0;
+      bool packs = true;
+      for (int q = 0; q < 3; q++) {
+        const uint32_t l = local(n[q]);
+        packs &= l < (uint32_t)kTriLocMax;
+        lc |= (l & (uint32_t)(kTriLocMax - 1)) << (kTriLocBits * q);
+      }
+      L.bt_loc.push_back(packs ? lc : kTriNoLoc);
       for (int q = 0; q < 3; q++)
         if (inblk(n[q])) vtri[n[q]].push_back((uint16_t)(k | (q << kTriPosShift)));
     }
@@ -319,6 +328,7 @@ int32_t build_layout(const fvm_mesh &m, int bv, MeshLayout &L) {
       int n[3];
       for (int q = 0; q < 3; q++) n[q] = L.iperm[m.elem[3 * t + q] - 1];
       L.bt_nodes.push_back(make_int4(n[0], n[1], n[2], t));
+      L.bt_loc.push_back(kTriNoLoc);   // halo-only triangle: no slots of its own block
     }
     {
       std::unordered_map<int, int> slot_of;
@@ -386,6 +396,20 @@ int64_t verify_layout(const MeshLayout &L) {
     auto vert_of = [&](uint32_t l) {
       return (int)l < bi.nv ? bi.v0 + (int)l : L.halo_ids[bi.h0 + (int)l - bi.nv];
     };
+    if (bi.nh > L.max_halo || L.bt_loc.size() != L.bt_nodes.size()) bad++;
+    // triangle records: the packed local slots name the entry's ends
+    for (int k = 0; k < bi.nt2 && L.bt_loc.size() == L.bt_nodes.size(); k++) {
+      const uint32_t lc = L.bt_loc[bi.t0 + k];
+      if (lc == kTriNoLoc) {
+        if (k < bi.nt && nloc <= kTriLocMax) bad++;
+        continue;
+      }
+      const int4 &t = L.bt_nodes[bi.t0 + k];
+      for (int q = 0; q < 3; q++) {
+        const uint32_t l = (lc >> (kTriLocBits * q)) & (uint32_t)(kTriLocMax - 1);
+        if ((int)l >= nloc || !has(t, vert_of(l), q)) bad++;
+      }
+    }
     for (int k = 0; k < bi.ne; k++) {
       const uint32_t ll = L.be_loc[bi.e0 + k];
       const int2 nn = L.be_nodes[bi.e0 + k];

@@ -23,6 +23,7 @@ struct MeshLayout {
   std::vector<int> be_edge;       // driver edge index (0-based) of each entry
   std::vector<int4> bb_nodes;     // boundary entries (n1, n2, 1 solid | 2 farfield, -)
   std::vector<int4> bt_nodes;     // triangle entries (n1, n2, n3, driver triangle)
+  std::vector<uint32_t> bt_loc;   // per triangle entry: the ends' local slots (kTriLoc*)
   std::vector<int> ve_ptr;        // [np+1]
   std::vector<uint16_t> ve_list;
   std::vector<int> vt_ptr;        // [np+1]
@@ -37,6 +38,7 @@ struct MeshLayout {
   std::vector<int> hl_ptr;        // per block: nh+1 offsets (relative) into hl_list
   std::vector<uint16_t> hl_list;  // halo vertex triangles: slot | pos << 14
   int max_tri = 0, max_slots = 0, max_tri2 = 0, max_loc = 0;
+  int max_halo = 0;               // max halo vertices of a block
 };
 
 // Builds the layout; returns FVM_OK or FVM_ERR_ARG (bad connectivity) /
