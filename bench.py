@@ -424,8 +424,11 @@ def run_reference(args):
     from oracle import oracle
     oracle.build()
     cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
-    # each step: one iteration per core on a mesh sized so the run stays short
-    ni, nr = (256, 96) if args.steps + args.warmup > 40 else (512, 192)
+    # each step: one iteration per core, on the workload's 1024 x 384 mesh
+    # when the run stays within a few minutes (about 0.45 s per iteration on
+    # one core), else on a smaller mesh of the same family as the sample
+    n_it = args.steps + args.warmup
+    ni, nr = (NI, NR) if n_it <= 300 else ((512, 192) if n_it <= 1600 else (256, 96))
     seeds = list(range(2, 2 + cores))
     from fvm2d_gb300.ogrid import naca_ogrid
     grids = [naca_ogrid(ni, nr, radius=20.0, first_spacing=5e-4, jitter=0.1, seed=s)
@@ -452,8 +455,10 @@ def run_reference(args):
             "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "impl": "reference",
-            "config": {"workload": f"naca0012 O-grid jittered, Euler M0.8 AoA1.25, {args.flux} "
-                                   "+ limiter, RK3, CFL 1", "vertices_per_mesh": grids[0].np,
+            "config": {"workload": f"naca0012 O-grid {NI}x{NR} jittered +-10%, Euler "
+                                   f"M0.8 AoA1.25, {args.flux} + limiter, RK3, CFL 1",
+                       "sample": f"{ni}x{nr} meshes of the same family, one per core",
+                       "vertices_per_mesh": grids[0].np,
                        "parallelism": f"{cores} host threads"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": sample},
