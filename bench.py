@@ -295,18 +295,20 @@ def run_gpu(args):
             if n > 0:
                 rows += len(b.history(s, drained[j], n)["fres"])
                 drained[j] = st["niter"]
-    for s, out in zip(slots, finals):
-        out[:] = b.get_state(s)["prim"]
+    for s, out in zip(slots, finals):     # the solution (prim) of each solve
+        out[:] = b.get_state(s, fields=("prim",))["prim"]
     b.sync()
     e2e_s = replicas.max_over_ranks(time.perf_counter() - t0)
     e2e_value = replicas.sum_over_ranks(V * 3 * args.steps) / e2e_s
-    h2d = V * 16 + len(slots) * 96 * 2
-    d2h = V * 16 * 3 + rows * 36 + len(slots) * 96 * 3
+    # FP64 driver-order arrays cross the link (permuted and converted on the
+    # device): prim in, prim out; RES.DAT rows; the per-mesh control records
+    h2d = V * 8 * 4 + len(slots) * 96 * 2
+    d2h = V * 8 * 4 + rows * 36 + len(slots) * 96 * 3
     e2e = {"value": e2e_value, "unit": UNIT,
            "h2d_bytes_per_step": round(h2d / args.steps, 1),
            "d2h_bytes_per_step": round(d2h / args.steps, 1),
-           "what": "fvm_batch_set_state (host FP64 prim -> pinned -> device) + start + "
-                   "steps + RES.DAT rows + fvm_batch_get_state, wall clock"}
+           "what": "fvm_batch_set_state (host FP64 prim -> device, permuted and converted "
+                   "there) + start + steps + RES.DAT rows + fvm_batch_get_state, wall clock"}
     b.close()
 
     extra = {}

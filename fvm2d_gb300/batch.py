@@ -129,14 +129,19 @@ class Batch:
         check(L.lib().fvm_batch_set_state(self.h, slot, dptr(prim), *[dptr(a) for a in conv],
                                           iterlast), "fvm_batch_set_state")
 
-    def get_state(self, slot) -> dict:
+    STATE_FIELDS = ("prim", "nut", "mul", "mu", "qx", "qy")
+
+    def get_state(self, slot, fields=STATE_FIELDS) -> dict:
+        """The slot's state in driver order (FP64); `fields` limits the
+        arrays read back (the others are passed to the C ABI as NULL)."""
         n = self._meshes[slot].np
-        out = {k: np.zeros((n, 4)) for k in ("prim", "qx", "qy")}
-        for k in ("nut", "mul", "mu"):
-            out[k] = np.zeros(n)
-        check(L.lib().fvm_batch_get_state(self.h, slot, dptr(out["prim"]), dptr(out["nut"]),
-                                          dptr(out["mul"]), dptr(out["mu"]), dptr(out["qx"]),
-                                          dptr(out["qy"])), "fvm_batch_get_state")
+        bad = set(fields) - set(self.STATE_FIELDS)
+        if bad:
+            raise ValueError(f"unknown state fields {sorted(bad)}")
+        out = {k: np.zeros((n, 4)) if k in ("prim", "qx", "qy") else np.zeros(n)
+               for k in fields}
+        ptr = [dptr(out[k]) if k in out else None for k in self.STATE_FIELDS]
+        check(L.lib().fvm_batch_get_state(self.h, slot, *ptr), "fvm_batch_get_state")
         return out
 
     def start(self, slot, nmax: int, minres: float = 0.0):

@@ -152,8 +152,8 @@ struct fvm_batch {
   int64_t t_launch[K_COUNT] = {0};
   int64_t launches = 0;           // kernels launched since creation
   int kernels_per_iter = 0;
-  unsigned char *pinned = nullptr;   // page-locked staging for state transfers
-  size_t pinned_size = 0;
+  double *dstage = nullptr;           // device staging of driver-order state transfers
+  size_t dstage_size = 0;
   std::string last_error;
 };
 
@@ -317,20 +317,20 @@ MeshConst make_const(const fvm_params &p) {
   return c;
 }
 
-// page-locked staging buffer of at least n bytes
-unsigned char *staging(fvm_batch *b, size_t n, cudaError_t &e) {
+// device staging buffer of at least n bytes
+double *dstaging(fvm_batch *b, size_t n, cudaError_t &e) {
   e = cudaSuccess;
-  if (b->pinned_size < n) {
-    if (b->pinned) cudaFreeHost(b->pinned);
-    b->pinned = nullptr;
-    b->pinned_size = 0;
+  if (b->dstage_size < n) {
+    if (b->dstage) cudaFree(b->dstage);
+    b->dstage = nullptr;
+    b->dstage_size = 0;
     void *p = nullptr;
-    e = cudaMallocHost(&p, n);
+    e = cudaMalloc(&p, n);
     if (e != cudaSuccess) return nullptr;
-    b->pinned = static_cast<unsigned char *>(p);
-    b->pinned_size = n;
+    b->dstage = static_cast<double *>(p);
+    b->dstage_size = n;
   }
-  return b->pinned;
+  return b->dstage;
 }
 
 int32_t get_ctl(fvm_batch *b, int slot, MeshCtl &c) {
@@ -345,54 +345,36 @@ int32_t put_ctl(fvm_batch *b, int slot, const MeshCtl &c) {
   return FVM_OK;
 }
 
-// host double [np][k] (driver order) -> device [np][k] of the slot
+// host double [np][k] (driver order) -> device [np][k] of the slot: the
+// array goes to the device as it is; a kernel permutes it into arena order
+// and converts it to the batch precision
 int32_t put_vertex(fvm_batch *b, const Slot &s, void *dst_base, const double *src, int k,
                    size_t stride) {
   const int np = s.L.np;
+  const size_t n = (size_t)np * k * sizeof(double);
   cudaError_t e;
-  unsigned char *buf = staging(b, (size_t)np * stride, e);
+  double *stage = dstaging(b, n, e);
   FVM_TRY(b, e);
-  std::memset(buf, 0, (size_t)np * stride);
-  for (int v = 0; v < np; v++) {
-    const double *q = src + (size_t)s.L.perm[v] * k;
-    unsigned char *d = buf + (size_t)v * stride;
-    for (int c = 0; c < k; c++) {
-      if (b->rsz == 8) {
-        std::memcpy(d + 8 * c, &q[c], 8);
-      } else {
-        const float x = (float)q[c];
-        std::memcpy(d + 4 * c, &x, 4);
-      }
-    }
-  }
   unsigned char *dst = static_cast<unsigned char *>(dst_base) + (size_t)s.off[P_V] * stride;
-  FVM_TRY(b, cudaMemcpyAsync(dst, buf, (size_t)np * stride, cudaMemcpyHostToDevice, b->stream));
+  FVM_TRY(b, cudaMemcpyAsync(stage, src, n, cudaMemcpyHostToDevice, b->stream));
+  FVM_TRY(b, launch_put_vertex(b->rsz, dst, stride, stage, b->orig + s.off[P_V], np, k, b->stream));
   FVM_TRY(b, cudaStreamSynchronize(b->stream));
   return FVM_OK;
 }
 
+// device [np][stride] of the slot, values c0..c0+k-1 -> host double [np][k]
+// in driver order (permuted and widened on the device)
 int32_t get_vertex(fvm_batch *b, const Slot &s, double *dst, const void *src_base, int k,
                    size_t stride, int c0 = 0) {
   const int np = s.L.np;
+  const size_t n = (size_t)np * k * sizeof(double);
   cudaError_t e;
-  unsigned char *buf = staging(b, (size_t)np * stride, e);
+  double *stage = dstaging(b, n, e);
   FVM_TRY(b, e);
   const unsigned char *src = static_cast<const unsigned char *>(src_base) + (size_t)s.off[P_V] * stride;
-  FVM_TRY(b, cudaMemcpyAsync(buf, src, (size_t)np * stride, cudaMemcpyDeviceToHost, b->stream));
+  FVM_TRY(b, launch_get_vertex(b->rsz, stage, src, stride, b->orig + s.off[P_V], np, k, c0, b->stream));
+  FVM_TRY(b, cudaMemcpyAsync(dst, stage, n, cudaMemcpyDeviceToHost, b->stream));
   FVM_TRY(b, cudaStreamSynchronize(b->stream));
-  for (int v = 0; v < np; v++) {
-    double *d = dst + (size_t)s.L.perm[v] * k;
-    const unsigned char *q = buf + (size_t)v * stride;
-    for (int c = 0; c < k; c++) {
-      if (b->rsz == 8) {
-        std::memcpy(&d[c], q + 8 * (c0 + c), 8);
-      } else {
-        float x;
-        std::memcpy(&x, q + 4 * (c0 + c), 4);
-        d[c] = x;
-      }
-    }
-  }
   return FVM_OK;
 }
 
@@ -815,7 +797,7 @@ extern "C" int32_t fvm_batch_destroy(fvm_batch *b) {
   drop_graphs(b);
   for (cudaEvent_t e : b->ev) cudaEventDestroy(e);
   for (void *p : b->owned) cudaFree(p);
-  if (b->pinned) cudaFreeHost(b->pinned);
+  if (b->dstage) cudaFree(b->dstage);
   if (b->stream) cudaStreamDestroy(b->stream);
   for (int k = 0; k < kMaxChains; k++) {
     if (b->chain_stream[k]) cudaStreamDestroy(b->chain_stream[k]);

@@ -114,4 +114,47 @@ cudaError_t launch_wall_dist(int np, int nsedge, const double2 *coord, const int
   return cudaGetLastError();
 }
 
+// Driver-order FP64 arrays (k values per vertex) to and from a mesh's
+// per-vertex arrays in arena order (rows of `stride` bytes, values of type R
+// from column c0): orig holds each arena vertex's driver index (1-based).
+// Conversions round to nearest, as the host's would (this unit does not
+// flush subnormals).
+template <typename R>
+__global__ void k_put_vertex(unsigned char *dst, size_t stride, const double *__restrict__ src,
+                             const int *__restrict__ orig, int np, int k) {
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < np; v += gridDim.x * blockDim.x) {
+    const double *q = src + (size_t)(orig[v] - 1) * k;
+    R *d = reinterpret_cast<R *>(dst + (size_t)v * stride);
+    for (int c = 0; c < k; c++) d[c] = (R)q[c];
+  }
+}
+
+template <typename R>
+__global__ void k_get_vertex(double *dst, const unsigned char *src, size_t stride,
+                             const int *__restrict__ orig, int np, int k, int c0) {
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < np; v += gridDim.x * blockDim.x) {
+    const R *q = reinterpret_cast<const R *>(src + (size_t)v * stride) + c0;
+    double *d = dst + (size_t)(orig[v] - 1) * k;
+    for (int c = 0; c < k; c++) d[c] = (double)q[c];
+  }
+}
+
+cudaError_t launch_put_vertex(int rsz, unsigned char *dst, size_t stride, const double *src,
+                              const int *orig, int np, int k, cudaStream_t s) {
+  if (np <= 0) return cudaSuccess;
+  const int g = (np + 255) / 256;
+  if (rsz == 8) k_put_vertex<double><<<g, 256, 0, s>>>(dst, stride, src, orig, np, k);
+  else k_put_vertex<float><<<g, 256, 0, s>>>(dst, stride, src, orig, np, k);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_get_vertex(int rsz, double *dst, const unsigned char *src, size_t stride,
+                              const int *orig, int np, int k, int c0, cudaStream_t s) {
+  if (np <= 0) return cudaSuccess;
+  const int g = (np + 255) / 256;
+  if (rsz == 8) k_get_vertex<double><<<g, 256, 0, s>>>(dst, src, stride, orig, np, k, c0);
+  else k_get_vertex<float><<<g, 256, 0, s>>>(dst, src, stride, orig, np, k, c0);
+  return cudaGetLastError();
+}
+
 }  // namespace fvm

@@ -226,3 +226,27 @@ def test_autotuner_changes_no_result(fvm_lib, prec):
         np.testing.assert_array_equal(b.history(s, 0, n)["fres"], h0["fres"])
         np.testing.assert_array_equal(b.get_state(s)["prim"], st0["prim"])
     b.close()
+
+
+@pytest.mark.parametrize("prec", [L.FP64, L.FP32])
+def test_state_round_trip_in_driver_order(fvm_lib, prec):
+    """set_state/get_state permute and convert on the device: a state set in
+    driver order reads back in driver order (exactly in FP64; rounded once
+    to FP32 in FP32), and asking for some fields reads the same values."""
+    from fvm2d_gb300.batch import Batch
+    m = mesh(fvm_lib, 96, 40, seed=3)
+    b = Batch(prec, vertices=m.np, meshes=1)
+    s = b.add(fvm_lib.make_params(precision=prec, mach=0.8, aoa_deg=1.25), m)
+    rng = np.random.default_rng(7)
+    prim = 1.0 + 0.1 * rng.random((m.np, 4))
+    nut = 1e-3 * rng.random(m.np)
+    b.set_state(s, prim, nut=nut)
+    full = b.get_state(s)
+    want = prim if prec == L.FP64 else prim.astype(np.float32).astype(np.float64)
+    np.testing.assert_array_equal(full["prim"], want)
+    wnut = nut if prec == L.FP64 else nut.astype(np.float32).astype(np.float64)
+    np.testing.assert_array_equal(full["nut"], wnut)
+    only = b.get_state(s, fields=("prim",))
+    assert set(only) == {"prim"}
+    np.testing.assert_array_equal(only["prim"], full["prim"])
+    b.close()
