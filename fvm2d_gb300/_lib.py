@@ -131,6 +131,7 @@ SIGNATURES = {
     "fvm_serve_state": (C.c_int32, [C.c_void_p, C.c_int64, _pd, _pd]),
     "fvm_serve_release": (C.c_int32, [C.c_void_p, C.c_int64]),
     "fvm_serve_stats": (C.c_int32, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "fvm_serve_times": (C.c_int32, [C.c_void_p, C.POINTER(C.c_double)]),
     "fvm_serve_destroy": (C.c_int32, [C.c_void_p]),
     "fvm_layout_stats": (C.c_int32, [C.POINTER(FvmMesh), C.POINTER(C.c_int64)]),
     "fvm_gpu_conres_noalloc": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, _pd,

@@ -81,6 +81,7 @@ enum Pool { P_V, P_BLK, P_BE, P_BB, P_BT, P_TRI, P_VE, P_VT, P_VA, P_SW, P_HALO,
 
 struct Slot {
   bool used = false;
+  bool staged = false;        // uploaded on the side stream, not yet in the work list
   fvm_params par{};
   MeshLayout L;
   int64_t off[P_COUNT] = {0};
@@ -152,8 +153,13 @@ struct fvm_batch {
   int64_t t_launch[K_COUNT] = {0};
   int64_t launches = 0;           // kernels launched since creation
   int kernels_per_iter = 0;
+  cudaStream_t upload = nullptr;      // side stream of deferred admissions
+  bool pending = false;               // staged slots wait for batch_commit
   double *dstage = nullptr;           // device staging of driver-order state transfers
   size_t dstage_size = 0;
+  // autotuner: each candidate form's last measured ms per iteration, calls
+  double tune_last[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  int tune_calls = 0;
   std::string last_error;
 };
 
@@ -379,9 +385,11 @@ int32_t get_vertex(fvm_batch *b, const Slot &s, double *dst, const void *src_bas
 }
 
 template <typename T>
-cudaError_t put_range(fvm_batch *b, T *base, int64_t off, const std::vector<T> &h) {
+cudaError_t put_range(fvm_batch *b, T *base, int64_t off, const std::vector<T> &h,
+                      cudaStream_t s = nullptr) {
   if (h.empty()) return cudaSuccess;
-  return cudaMemcpyAsync(base + off, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, b->stream);
+  return cudaMemcpyAsync(base + off, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice,
+                         s ? s : b->stream);
 }
 
 void drop_graphs(fvm_batch *b);
@@ -390,7 +398,7 @@ int32_t update_work(fvm_batch *b) {
   std::vector<int> work, mesh_first;
   int flux = -1;
   for (const Slot &s : b->slots)
-    if (s.used) {
+    if (s.used && !s.staged) {
       mesh_first.push_back((int)work.size());
       for (int k = 0; k < s.L.nblk; k++) work.push_back((int)(s.off[P_BLK] + k));
       flux = (flux == -1 || flux == s.par.iflux) ? s.par.iflux : 0;
@@ -403,7 +411,7 @@ int32_t update_work(fvm_batch *b) {
   int max_halo = 0;
   bool any_visc = false, any_turb = false, tri_loc = true;
   for (const Slot &s : b->slots)
-    if (s.used) {
+    if (s.used && !s.staged) {
       any_visc |= s.par.iflow != FVM_INVISCID;
       any_turb |= s.par.iflow == FVM_TURBULENT;
       tile[0] = std::max(tile[0], s.L.max_tri);
@@ -465,7 +473,7 @@ int32_t update_work(fvm_batch *b) {
   {
     size_t m = 0;
     for (size_t i = 0; i < b->slots.size(); i++)
-      if (b->slots[i].used) {
+      if (b->slots[i].used && !b->slots[i].staged) {
         const int first = mesh_first[m++];
         int k = 1;
         while (k < kMaxChains && first >= head[k]) k++;
@@ -479,6 +487,15 @@ int32_t update_work(fvm_batch *b) {
                              cudaMemcpyHostToDevice, b->stream));
   FVM_TRY(b, cudaStreamSynchronize(b->stream));
   return FVM_OK;
+}
+
+// Deferred admissions join the work list once their uploads have finished.
+int32_t batch_commit(fvm_batch *b) {
+  if (!b->pending) return FVM_OK;
+  FVM_TRY(b, cudaStreamSynchronize(b->upload));
+  for (Slot &s : b->slots) s.staged = false;
+  b->pending = false;
+  return update_work(b);
 }
 
 // kernels of `iters` iterations, in order; optional timing events around
@@ -609,6 +626,7 @@ int32_t build_graph(fvm_batch *b, int iters) {
 }
 
 void drop_graphs(fvm_batch *b) {
+  if ((b->graph || b->graph_multi) && b->stream) cudaStreamSynchronize(b->stream);
   if (b->graph) cudaGraphExecDestroy(b->graph);
   if (b->graph_multi) cudaGraphExecDestroy(b->graph_multi);
   b->graph = b->graph_multi = nullptr;
@@ -692,6 +710,7 @@ extern "C" int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *cap
     if (_e != cudaSuccess) return fail(cuda_status(b, _e));  \
   } while (0)
   TRYB(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+  TRYB(cudaStreamCreateWithFlags(&b->upload, cudaStreamNonBlocking));
   for (int k = 0; k < kMaxChains; k++) {
     if (k) TRYB(cudaStreamCreateWithFlags(&b->chain_stream[k], cudaStreamNonBlocking));
     TRYB(cudaEventCreateWithFlags(&b->ev_fork[k], cudaEventDisableTiming));
@@ -797,7 +816,9 @@ extern "C" int32_t fvm_batch_destroy(fvm_batch *b) {
   drop_graphs(b);
   for (cudaEvent_t e : b->ev) cudaEventDestroy(e);
   for (void *p : b->owned) cudaFree(p);
+  if (b->upload) cudaStreamSynchronize(b->upload);
   if (b->dstage) cudaFree(b->dstage);
+  if (b->upload) cudaStreamDestroy(b->upload);
   if (b->stream) cudaStreamDestroy(b->stream);
   for (int k = 0; k < kMaxChains; k++) {
     if (b->chain_stream[k]) cudaStreamDestroy(b->chain_stream[k]);
@@ -920,7 +941,10 @@ extern "C" int64_t fvm_prepared_bytes(const fvm_prepared *prep, int32_t precisio
   return bytes;
 }
 
-extern "C" int32_t fvm_batch_add_prepared(fvm_batch *b, fvm_prepared *prep, int32_t *slot_out) {
+// Admits a prepared mesh.  Deferred: every upload goes to the side stream
+// (it may run beside kernels on the batch's stream: the mesh's ranges are
+// free) and the mesh joins the work list at batch_commit.
+static int32_t add_prepared(fvm_batch *b, fvm_prepared *prep, int32_t *slot_out, bool deferred) {
   if (!b || !prep || !slot_out) return FVM_ERR_ARG;
   *slot_out = -1;
   const fvm_params *par = &prep->par;
@@ -1029,96 +1053,96 @@ extern "C" int32_t fvm_batch_add_prepared(fvm_batch *b, fvm_prepared *prep, int3
     return cuda_status(b, e);
   };
   S.used = true;
+  S.staged = deferred;
+  const cudaStream_t us = deferred ? b->upload : b->stream;
   cudaError_t e = cudaSuccess;
 #define PUT(expr)                  \
   if ((e = (expr)) != cudaSuccess) \
     return err(e);
-  PUT(put_range(b, b->coord, v0, prep->coord));
-  PUT(put_range(b, b->ais, v0, prep->ais));
-  PUT(put_range(b, b->cvarea, v0, prep->cvarea));
-  PUT(put_range(b, b->drmin, v0, prep->drmin));
+  PUT(put_range(b, b->coord, v0, prep->coord, us));
+  PUT(put_range(b, b->ais, v0, prep->ais, us));
+  PUT(put_range(b, b->cvarea, v0, prep->cvarea, us));
+  PUT(put_range(b, b->drmin, v0, prep->drmin, us));
   if (b->ais32) {
     std::vector<float> f(prep->ais.size());
     for (size_t i = 0; i < f.size(); i++) f[i] = (float)prep->ais[i];
-    PUT(put_range(b, b->ais32, v0, f));
+    PUT(put_range(b, b->ais32, v0, f, us));
     for (size_t i = 0; i < f.size(); i++) f[i] = (float)prep->cvarea[i];
-    PUT(put_range(b, b->cvarea32, v0, f));
+    PUT(put_range(b, b->cvarea32, v0, f, us));
     for (size_t i = 0; i < f.size(); i++) f[i] = (float)prep->drmin[i];
-    PUT(put_range(b, b->drmin32, v0, f));
+    PUT(put_range(b, b->drmin32, v0, f, us));
     for (size_t i = 0; i < f.size(); i++) f[i] = (float)prep->wd[i];
-    PUT(put_range(b, b->wd32, v0, f));
+    PUT(put_range(b, b->wd32, v0, f, us));
   }
-  PUT(put_range(b, b->wd, v0, prep->wd));
-  PUT(put_range(b, b->orig, v0, prep->orig));
-  PUT(put_range(b, b->vflag, v0, L.vflag));
-  PUT(put_range(b, b->ve_rng, v0, ve));
-  PUT(put_range(b, b->vt_rng, v0, vt));
-  PUT(put_range(b, b->va_rng, v0, va));
-  PUT(put_range(b, b->ve_list, S.off[P_VE], L.ve_list));
-  PUT(put_range(b, b->vt_list, S.off[P_VT], L.vt_list));
-  PUT(put_range(b, b->va_list, S.off[P_VA], valist));
-  PUT(put_range(b, b->blocks, S.off[P_BLK], blocks));
-  PUT(put_range(b, b->be_nodes, S.off[P_BE], be));
-  PUT(put_range(b, b->be_loc, S.off[P_BE], L.be_loc));
-  PUT(put_range(b, b->halo_ids, S.off[P_HALO], halo));
-  PUT(put_range(b, b->hl_ptr, S.off[P_HP], hlp));
-  PUT(put_range(b, b->hl_list, S.off[P_HL], L.hl_list));
-  PUT(put_range(b, b->be_ds, S.off[P_BE], prep->be_ds));
+  PUT(put_range(b, b->wd, v0, prep->wd, us));
+  PUT(put_range(b, b->orig, v0, prep->orig, us));
+  PUT(put_range(b, b->vflag, v0, L.vflag, us));
+  PUT(put_range(b, b->ve_rng, v0, ve, us));
+  PUT(put_range(b, b->vt_rng, v0, vt, us));
+  PUT(put_range(b, b->va_rng, v0, va, us));
+  PUT(put_range(b, b->ve_list, S.off[P_VE], L.ve_list, us));
+  PUT(put_range(b, b->vt_list, S.off[P_VT], L.vt_list, us));
+  PUT(put_range(b, b->va_list, S.off[P_VA], valist, us));
+  PUT(put_range(b, b->blocks, S.off[P_BLK], blocks, us));
+  PUT(put_range(b, b->be_nodes, S.off[P_BE], be, us));
+  PUT(put_range(b, b->be_loc, S.off[P_BE], L.be_loc, us));
+  PUT(put_range(b, b->halo_ids, S.off[P_HALO], halo, us));
+  PUT(put_range(b, b->hl_ptr, S.off[P_HP], hlp, us));
+  PUT(put_range(b, b->hl_list, S.off[P_HL], L.hl_list, us));
+  PUT(put_range(b, b->be_ds, S.off[P_BE], prep->be_ds, us));
   if (b->be_csl)
-    PUT(launch_edge_csl(b->be_ds + S.off[P_BE], b->be_csl + S.off[P_BE], (int)be.size(), b->stream));
-  PUT(put_range(b, b->bb_nodes, S.off[P_BB], bb));
-  PUT(put_range(b, b->bt_nodes, S.off[P_BT], bt));
-  PUT(put_range(b, b->elarea, S.off[P_TRI], prep->elarea));
+    PUT(launch_edge_csl(b->be_ds + S.off[P_BE], b->be_csl + S.off[P_BE], (int)be.size(), us));
+  PUT(put_range(b, b->bb_nodes, S.off[P_BB], bb, us));
+  PUT(put_range(b, b->bt_nodes, S.off[P_BT], bt, us));
+  PUT(put_range(b, b->elarea, S.off[P_TRI], prep->elarea, us));
   if (b->be_g32) {
     std::vector<EdgeGeo32> g(prep->be_g32);
     for (EdgeGeo32 &x : g) {
       x.n1 += v0;
       x.n2 += v0;
     }
-    PUT(put_range(b, b->be_g32, S.off[P_BE], g));
+    PUT(put_range(b, b->be_g32, S.off[P_BE], g, us));
   }
-  if (b->tri_g32) PUT(put_range(b, b->tri_g32, S.off[P_BT], prep->tri_g32));
-  PUT(put_range(b, b->sw_nodes, S.off[P_SW], sw));
-  PUT(cudaMemcpyAsync(b->mc + sid, &mc, sizeof(mc), cudaMemcpyHostToDevice, b->stream));
-  PUT(cudaMemcpyAsync(b->ctl + sid, &ctl, sizeof(ctl), cudaMemcpyHostToDevice, b->stream));
+  if (b->tri_g32) PUT(put_range(b, b->tri_g32, S.off[P_BT], prep->tri_g32, us));
+  PUT(put_range(b, b->sw_nodes, S.off[P_SW], sw, us));
+  PUT(cudaMemcpyAsync(b->mc + sid, &mc, sizeof(mc), cudaMemcpyHostToDevice, us));
+  PUT(cudaMemcpyAsync(b->ctl + sid, &ctl, sizeof(ctl), cudaMemcpyHostToDevice, us));
   const size_t r = b->rsz;
-  PUT(cudaMemsetAsync(static_cast<unsigned char *>(b->grad) + (size_t)v0 * 8 * r, 0, 8 * r * np, b->stream));
-  PUT(cudaMemsetAsync(static_cast<unsigned char *>(b->resv) + (size_t)v0 * 4 * r, 0, 4 * r * np, b->stream));
-  PUT(cudaStreamSynchronize(b->stream));
+  PUT(cudaMemsetAsync(static_cast<unsigned char *>(b->grad) + (size_t)v0 * 8 * r, 0, 8 * r * np, us));
+  PUT(cudaMemsetAsync(static_cast<unsigned char *>(b->resv) + (size_t)v0 * 4 * r, 0, 4 * r * np, us));
 #undef PUT
-  // freestream state (initialize.f:60-89)
+  // freestream state (initialize.f:60-89): the same values at every
+  // vertex, written on the device into the phase-0 buffers of the control
+  // record uploaded above (iteration 0, nothing active)
   int32_t st;
   {
-    std::vector<double> prim(4 * (size_t)np), nut(np, 0.0), mul(np, 0.0), mu(np, 0.0);
-    for (int v = 0; v < np; v++) {
-      prim[4 * v] = par->r_inf;
-      prim[4 * v + 1] = par->u_inf;
-      prim[4 * v + 2] = par->v_inf;
-      prim[4 * v + 3] = par->p_inf;
-    }
+    double nut0 = 0.0, mul0 = 0.0, mu0 = 0.0;
     if (par->iflow != FVM_INVISCID) {
       const double temp = par->p_inf / par->r_inf / par->gas_const;
-      const double mul0 = std::pow(temp / par->t_inf, 1.5) *
-                          ((par->t_inf + par->sconst) / (temp + par->sconst)) / par->rey;
-      for (int v = 0; v < np; v++) {
-        mul[v] = mul0;
-        if (par->iflow == FVM_TURBULENT) {
-          nut[v] = par->nut_inf;
-          const double chi = nut[v] * par->r_inf / mul0;
-          const double chi3 = (chi * chi) * chi;
-          mu[v] = mul0 + par->r_inf * nut[v] * (chi3 / (chi3 + par->cv11));
-        } else {
-          mu[v] = mul0;
-        }
+      mul0 = std::pow(temp / par->t_inf, 1.5) *
+             ((par->t_inf + par->sconst) / (temp + par->sconst)) / par->rey;
+      mu0 = mul0;
+      if (par->iflow == FVM_TURBULENT) {
+        nut0 = par->nut_inf;
+        const double chi = nut0 * par->r_inf / mul0;
+        const double chi3 = (chi * chi) * chi;
+        mu0 = mul0 + par->r_inf * nut0 * (chi3 / (chi3 + par->cv11));
       }
     }
-    st = fvm_batch_set_state(b, sid, prim.data(), nut.data(), mul.data(), mu.data(), 0);
-    if (st) {
-      fvm_batch_remove(b, sid);
-      return st;
-    }
+    const double prim0[4] = {par->r_inf, par->u_inf, par->v_inf, par->p_inf};
+    auto at = [&](void *base, size_t stride) {
+      return static_cast<unsigned char *>(base) + (size_t)v0 * stride;
+    };
+    cudaError_t fe = launch_fill_vertex((int)r, at(b->st[0], 4 * r), 4 * r, np, 4, prim0, us);
+    if (fe == cudaSuccess) fe = launch_fill_vertex((int)r, at(b->nut[0], r), r, np, 1, &nut0, us);
+    if (fe == cudaSuccess) fe = launch_fill_vertex((int)r, at(b->mul, r), r, np, 1, &mul0, us);
+    if (fe == cudaSuccess) fe = launch_fill_vertex((int)r, at(b->mu, r), r, np, 1, &mu0, us);
+    if (fe == cudaSuccess && !deferred) fe = cudaStreamSynchronize(us);
+    if (fe != cudaSuccess) return err(fe);
   }
-  if ((st = update_work(b))) {
+  if (deferred) {
+    b->pending = true;
+  } else if ((st = update_work(b))) {
     fvm_batch_remove(b, sid);
     return st;
   }
@@ -1126,6 +1150,24 @@ extern "C" int32_t fvm_batch_add_prepared(fvm_batch *b, fvm_prepared *prep, int3
   *slot_out = sid;
   return FVM_OK;
 }
+
+extern "C" int32_t fvm_batch_add_prepared(fvm_batch *b, fvm_prepared *prep, int32_t *slot_out) {
+  if (!b) return FVM_ERR_ARG;
+  int32_t st = batch_commit(b);
+  if (st) return st;
+  return add_prepared(b, prep, slot_out, false);
+}
+
+namespace fvm {
+int32_t batch_add_prepared_deferred(fvm_batch *b, fvm_prepared *prep, int32_t *slot_out) {
+  if (!b) return FVM_ERR_ARG;
+  return add_prepared(b, prep, slot_out, true);
+}
+int32_t batch_commit_admissions(fvm_batch *b) {
+  if (!b) return FVM_ERR_ARG;
+  return batch_commit(b);
+}
+}  // namespace fvm
 
 extern "C" int32_t fvm_batch_add(fvm_batch *b, const fvm_params *par, const fvm_mesh *m,
                                  int32_t *slot_out) {
@@ -1142,6 +1184,10 @@ extern "C" int32_t fvm_batch_add(fvm_batch *b, const fvm_params *par, const fvm_
 }
 
 extern "C" int32_t fvm_batch_remove(fvm_batch *b, int32_t slot) {
+  if (b && b->pending) {   // deferred admissions first
+    const int32_t cst = batch_commit(b);
+    if (cst) return cst;
+  }
   Slot *S = slot_of(b, slot);
   if (!S) return FVM_ERR_ARG;
   MeshCtl z;
@@ -1156,6 +1202,10 @@ extern "C" int32_t fvm_batch_remove(fvm_batch *b, int32_t slot) {
 extern "C" int32_t fvm_batch_set_state(fvm_batch *b, int32_t slot, const double *prim,
                                        const double *nut, const double *mul, const double *mu,
                                        int32_t iterlast) {
+  if (b && b->pending) {   // deferred admissions first
+    const int32_t cst = batch_commit(b);
+    if (cst) return cst;
+  }
   Slot *S = slot_of(b, slot);
   if (!S || !prim) return FVM_ERR_ARG;
   MeshCtl c;
@@ -1177,6 +1227,10 @@ extern "C" int32_t fvm_batch_set_state(fvm_batch *b, int32_t slot, const double 
 
 extern "C" int32_t fvm_batch_get_state(fvm_batch *b, int32_t slot, double *prim, double *nut,
                                        double *mul, double *mu, double *qx, double *qy) {
+  if (b && b->pending) {   // deferred admissions first
+    const int32_t cst = batch_commit(b);
+    if (cst) return cst;
+  }
   Slot *S = slot_of(b, slot);
   if (!S) return FVM_ERR_ARG;
   MeshCtl c;
@@ -1193,6 +1247,10 @@ extern "C" int32_t fvm_batch_get_state(fvm_batch *b, int32_t slot, double *prim,
 }
 
 extern "C" int32_t fvm_batch_start(fvm_batch *b, int32_t slot, int32_t nmax, double minres) {
+  if (b && b->pending) {   // deferred admissions first
+    const int32_t cst = batch_commit(b);
+    if (cst) return cst;
+  }
   Slot *S = slot_of(b, slot);
   if (!S || nmax < 0) return FVM_ERR_ARG;
   MeshCtl c;
@@ -1208,6 +1266,10 @@ extern "C" int32_t fvm_batch_start(fvm_batch *b, int32_t slot, int32_t nmax, dou
 }
 
 extern "C" int32_t fvm_batch_step(fvm_batch *b, int32_t niter) {
+  if (b && b->pending) {   // deferred admissions first
+    const int32_t cst = batch_commit(b);
+    if (cst) return cst;
+  }
   if (!b || niter < 0) return FVM_ERR_ARG;
   int32_t st;
   if (!b->timing && niter >= kGraphIters) {
@@ -1273,6 +1335,10 @@ static int32_t apply_form(fvm_batch *b, const Form &f) {
 }
 
 extern "C" int32_t fvm_batch_set_form(fvm_batch *b, int32_t form) {
+  if (b && b->pending) {   // deferred admissions first
+    const int32_t cst = batch_commit(b);
+    if (cst) return cst;
+  }
   if (!b || form < 0 || form >= kForms) return FVM_ERR_ARG;
   const Form f = form_of(b, form);
   if (!form_fits(b, f)) return FVM_ERR_ARG;
@@ -1281,6 +1347,10 @@ extern "C" int32_t fvm_batch_set_form(fvm_batch *b, int32_t form) {
 
 extern "C" int32_t fvm_batch_tune(fvm_batch *b, int32_t iters, int32_t max, double *ms_per_iter,
                                   int32_t *choice) {
+  if (b && b->pending) {   // deferred admissions first
+    const int32_t cst = batch_commit(b);
+    if (cst) return cst;
+  }
   if (!b || iters < 1 || max < 0 || (max > 0 && !ms_per_iter)) return FVM_ERR_ARG;
   // whole multi-iteration graphs when the steps are untimed
   const int timed = b->timing ? iters : (iters + kGraphIters - 1) / kGraphIters * kGraphIters;
@@ -1295,9 +1365,27 @@ extern "C" int32_t fvm_batch_tune(fvm_batch *b, int32_t iters, int32_t max, doub
   int best = -1;
   double best_ms = 0.0;
   int32_t st = FVM_OK;
+  // every fourth call times every candidate; in between, a candidate more
+  // than kTuneSkip times slower than the best of its last timing is not
+  // re-timed (its last time is reported)
+  static_assert(kForms <= 8, "tune_last holds 8 forms");
+  constexpr double kTuneSkip = 1.25;
+  double prev_best = 0.0;
+  for (int i = 0; i < kForms; i++)
+    if (b->tune_last[i] > 0.0 && (prev_best == 0.0 || b->tune_last[i] < prev_best))
+      prev_best = b->tune_last[i];
+  const bool full = b->tune_calls % 4 == 0 || prev_best == 0.0;
+  b->tune_calls++;
   for (int i = 0; i < kForms && st == FVM_OK; i++) {
     const Form f = form_of(b, i);
-    if (!form_fits(b, f)) continue;
+    if (!form_fits(b, f)) {
+      b->tune_last[i] = 0.0;
+      continue;
+    }
+    if (!full && b->tune_last[i] > kTuneSkip * prev_best) {
+      if (i < max) ms_per_iter[i] = b->tune_last[i];
+      continue;
+    }
     if ((st = apply_form(b, f))) break;
     // timed as the steps will run: whole multi-iteration graphs (captured
     // before the timing), so each form is timed over at least one
@@ -1312,6 +1400,7 @@ extern "C" int32_t fvm_batch_tune(fvm_batch *b, int32_t iters, int32_t max, doub
     if (e != cudaSuccess) st = cuda_status(b, e);
     if (st) break;
     const double per = (double)ms / timed;
+    b->tune_last[i] = per;
     if (i < max) ms_per_iter[i] = per;
     if (best < 0 || per < best_ms) {
       best = i;
@@ -1335,6 +1424,10 @@ extern "C" int32_t fvm_batch_sync(fvm_batch *b) {
 extern "C" int32_t fvm_batch_poll(fvm_batch *b, int32_t slot, int32_t *active, int32_t *niter,
                                   double *fres, double *cl, double *cd, int32_t *status,
                                   int32_t *bad_point) {
+  if (b && b->pending) {   // deferred admissions first
+    const int32_t cst = batch_commit(b);
+    if (cst) return cst;
+  }
   if (!slot_of(b, slot)) return FVM_ERR_ARG;
   MeshCtl c;
   int32_t st = get_ctl(b, slot, c);
@@ -1352,6 +1445,10 @@ extern "C" int32_t fvm_batch_poll(fvm_batch *b, int32_t slot, int32_t *active, i
 extern "C" int32_t fvm_batch_history(fvm_batch *b, int32_t slot, int32_t first, int32_t count,
                                      double *fres, int32_t *iresi, double *fresi, double *cl,
                                      double *cd) {
+  if (b && b->pending) {   // deferred admissions first
+    const int32_t cst = batch_commit(b);
+    if (cst) return cst;
+  }
   if (!slot_of(b, slot) || first < 0 || count < 0) return FVM_ERR_ARG;
   MeshCtl c;
   int32_t st = get_ctl(b, slot, c);
@@ -1386,6 +1483,10 @@ extern "C" int32_t fvm_batch_history(fvm_batch *b, int32_t slot, int32_t first, 
 extern "C" void *fvm_batch_stream(fvm_batch *b) { return b ? (void *)b->stream : nullptr; }
 
 extern "C" int32_t fvm_batch_timing(fvm_batch *b, int32_t on) {
+  if (b && b->pending) {   // deferred admissions first
+    const int32_t cst = batch_commit(b);
+    if (cst) return cst;
+  }
   if (!b) return FVM_ERR_ARG;
   const bool want = on != 0;
   for (int k = 0; k < K_COUNT; k++) {

@@ -63,5 +63,7 @@ cudaError_t launch_put_vertex(int rsz, unsigned char *dst, size_t stride, const 
                               const int *orig, int np, int k, cudaStream_t s);
 cudaError_t launch_get_vertex(int rsz, double *dst, const unsigned char *src, size_t stride,
                               const int *orig, int np, int k, int c0, cudaStream_t s);
+cudaError_t launch_fill_vertex(int rsz, unsigned char *dst, size_t stride, int np, int k,
+                               const double *values, cudaStream_t s);
 
 }  // namespace fvm

@@ -29,6 +29,11 @@
 
 #include "../../include/fvm_gpu.h"
 
+namespace fvm {   // fvm_batch.cpp: admission beside a running step
+int32_t batch_add_prepared_deferred(fvm_batch *b, fvm_prepared *prep, int32_t *slot_out);
+int32_t batch_commit_admissions(fvm_batch *b);
+}  // namespace fvm
+
 namespace {
 
 using Clock = std::chrono::steady_clock;
@@ -64,6 +69,10 @@ struct fvm_server {
   std::map<int64_t, Ticket> tickets;
   std::map<int32_t, int64_t> resident;  // slot -> ticket (service thread only)
   int64_t next_id = 1, submitted = 0, done = 0, steps = 0;
+  // service-thread seconds: admitting, tuning, stepping (launch + waiting
+  // for the GPU), retiring
+  double t_admit = 0, t_tune = 0, t_step = 0, t_retire = 0;
+  double t_admit_beside = 0;            // admission work overlapped with a step
   int32_t error = FVM_OK;               // a CUDA failure stops the service
   bool stop = false;
   std::thread worker;
@@ -138,7 +147,16 @@ int32_t retire(fvm_server *s) {
 }
 
 // Admits queued solves in arrival order while they fit.
-int32_t admit(fvm_server *s) {
+// Admits queued solves while the arena has room.  Deferred (a step is
+// running): the uploads go beside it and the solves start at
+// start_admitted, after the step.
+struct Admitted {
+  int64_t id;
+  int32_t slot, nmax;
+  double minres;
+};
+
+int32_t admit(fvm_server *s, bool deferred, std::vector<Admitted> *staged) {
   for (;;) {
     int64_t id;
     fvm_prepared *prep;
@@ -154,7 +172,8 @@ int32_t admit(fvm_server *s) {
       minres = t.minres;
     }
     int32_t slot = -1;
-    int32_t st = fvm_batch_add_prepared(s->b, prep, &slot);
+    int32_t st = deferred ? fvm::batch_add_prepared_deferred(s->b, prep, &slot)
+                          : fvm_batch_add_prepared(s->b, prep, &slot);
     std::lock_guard<std::mutex> lk(s->mu);
     Ticket &t = s->tickets[id];
     if (st == FVM_ERR_CAPACITY && !s->resident.empty()) return FVM_OK;   // waits for room
@@ -171,9 +190,25 @@ int32_t admit(fvm_server *s) {
     t.slot = slot;
     t.state = 1;
     t.t_admit = Clock::now();
+    if (deferred) {
+      staged->push_back({id, slot, nmax, minres});
+      continue;
+    }
     s->resident[slot] = id;
     if ((st = fvm_batch_start(s->b, slot, nmax, minres))) return st;
   }
+}
+
+// The solves admitted beside the last step join the batch and start.
+int32_t start_admitted(fvm_server *s, std::vector<Admitted> &staged) {
+  if (staged.empty()) return FVM_OK;
+  int32_t st = fvm::batch_commit_admissions(s->b);
+  for (const Admitted &a : staged) {
+    s->resident[a.slot] = a.id;
+    if (!st) st = fvm_batch_start(s->b, a.slot, a.nmax, a.minres);
+  }
+  staged.clear();
+  return st;
 }
 
 void service(fvm_server *s) {
@@ -188,15 +223,38 @@ void service(fvm_server *s) {
         continue;
       }
     }
-    if ((st = admit(s))) break;
+    auto sec = [](Clock::time_point a, Clock::time_point b) {
+      return std::chrono::duration<double>(b - a).count();
+    };
+    const Clock::time_point t0 = Clock::now();
+    // with nothing resident, admit now; otherwise beside the next step
+    if (s->resident.empty()) st = admit(s, false, nullptr);
+    const Clock::time_point t1 = Clock::now();
+    s->t_admit += sec(t0, t1);
+    if (st) break;
     if (s->resident.empty()) continue;
     if (s->tune_every > 0 && s->steps % s->tune_every == 0) {
       int32_t choice = 0;
       if ((st = fvm_batch_tune(s->b, 10, 0, nullptr, &choice))) break;
     }
+    const Clock::time_point t2 = Clock::now();
+    s->t_tune += sec(t1, t2);
+    std::vector<Admitted> staged;
     if ((st = fvm_batch_step(s->b, s->chunk))) break;
+    // uploads of waiting solves while the step runs
+    const Clock::time_point ta = Clock::now();
+    st = admit(s, true, &staged);
+    const Clock::time_point tb = Clock::now();
+    s->t_admit_beside += sec(ta, tb);
+    if (st || (st = fvm_batch_sync(s->b))) break;
+    const Clock::time_point t3 = Clock::now();
+    s->t_step += sec(t2, t3);
+    if ((st = start_admitted(s, staged))) break;
+    s->t_admit += sec(t3, Clock::now());
     s->steps++;
-    if ((st = retire(s))) break;
+    st = retire(s);
+    s->t_retire += sec(t3, Clock::now());
+    if (st) break;
     s->cv_done.notify_all();
   }
   std::lock_guard<std::mutex> lk(s->mu);
@@ -344,6 +402,17 @@ extern "C" int32_t fvm_serve_stats(fvm_server *s, int64_t *out) {
   out[3] = running;
   out[4] = s->steps;
   out[5] = s->error;
+  return FVM_OK;
+}
+
+extern "C" int32_t fvm_serve_times(fvm_server *s, double *out) {
+  if (!s || !out) return FVM_ERR_ARG;
+  std::lock_guard<std::mutex> lk(s->mu);
+  out[0] = s->t_admit;
+  out[1] = s->t_tune;
+  out[2] = s->t_step;
+  out[3] = s->t_retire;
+  out[4] = s->t_admit_beside;
   return FVM_OK;
 }
 

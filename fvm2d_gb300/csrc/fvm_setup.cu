@@ -139,6 +139,29 @@ __global__ void k_get_vertex(double *dst, const unsigned char *src, size_t strid
   }
 }
 
+// every row of a mesh's per-vertex array set to the same k values
+template <typename R>
+__global__ void k_fill_vertex(unsigned char *dst, size_t stride, int np, int k, double a0,
+                              double a1, double a2, double a3) {
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < np; v += gridDim.x * blockDim.x) {
+    R *d = reinterpret_cast<R *>(dst + (size_t)v * stride);
+    const double a[4] = {a0, a1, a2, a3};
+    for (int c = 0; c < k; c++) d[c] = (R)a[c];
+  }
+}
+
+cudaError_t launch_fill_vertex(int rsz, unsigned char *dst, size_t stride, int np, int k,
+                               const double *values, cudaStream_t s) {
+  if (np <= 0) return cudaSuccess;
+  if (k < 1 || k > 4) return cudaErrorInvalidValue;
+  double a[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int c = 0; c < k; c++) a[c] = values[c];
+  const int g = (np + 255) / 256;
+  if (rsz == 8) k_fill_vertex<double><<<g, 256, 0, s>>>(dst, stride, np, k, a[0], a[1], a[2], a[3]);
+  else k_fill_vertex<float><<<g, 256, 0, s>>>(dst, stride, np, k, a[0], a[1], a[2], a[3]);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_put_vertex(int rsz, unsigned char *dst, size_t stride, const double *src,
                               const int *orig, int np, int k, cudaStream_t s) {
   if (np <= 0) return cudaSuccess;

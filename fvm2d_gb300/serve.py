@@ -311,6 +311,16 @@ class NativeServer:
         return dict(zip(("submitted", "done", "queued", "running", "steps", "status"),
                         [int(x) for x in out]))
 
+    def times(self) -> dict:
+        """Seconds the service thread spent admitting between steps,
+        tuning, stepping (launching and waiting for the GPU, including the
+        admissions made beside a running step) and retiring."""
+        import ctypes as C
+        out = (C.c_double * 5)()
+        L.check(L.lib().fvm_serve_times(self.h, out), "fvm_serve_times")
+        return dict(zip(("admit_s", "tune_s", "step_s", "retire_s", "admit_beside_step_s"),
+                        [float(x) for x in out]))
+
     def run(self, requests: list[Request]) -> tuple[list[Result], dict]:
         """The request workload: each request is submitted at its arrival
         time (grid generation and layout on the worker pool)."""
@@ -353,7 +363,8 @@ class NativeServer:
                      p50_latency_s=float(np.percentile(lat, 50)),
                      p99_latency_s=float(np.percentile(lat, 99)),
                      vertex_stage_updates=float(sum(r.npts * 3 * r.niter for r in res)),
-                     steps=st["steps"], chunk=self.chunk, service="native")
+                     steps=st["steps"], chunk=self.chunk, service="native",
+                     service_thread=self.times())
         stats["vertex_stage_updates_per_s"] = stats["vertex_stage_updates"] / makespan
         return res, stats
 

@@ -362,6 +362,9 @@ int64_t fvm_batch_launch_count(fvm_batch *b);
  * two overlapped ones) and keeps the fastest.  Every
  * form gives the same bits, so the tuning iterations are ordinary
  * iterations of the solves (they count toward each solve's iterations).
+ * The first call and every fourth call after it time every candidate; the
+ * calls in between skip a candidate whose last time was more than 1.25x
+ * the best last time, and report that last time for it.
  * ms_per_iter[i] (i < max) receives candidate i's device time per
  * iteration (0 for a candidate that does not fit), *choice the candidate
  * kept: 0 bulk, 1 loads, 2 per vertex, 3 fused, 4 bulk (FP32) or loads
@@ -411,6 +414,10 @@ int32_t fvm_serve_state(fvm_server *s, int64_t ticket, double *prim,
 int32_t fvm_serve_release(fvm_server *s, int64_t ticket);
 /* out[6]: submitted, done, queued, running, steps, service status. */
 int32_t fvm_serve_stats(fvm_server *s, int64_t *out);
+/* out[5]: seconds the service thread spent admitting (between steps),
+ * tuning, stepping (launching and waiting for the GPU; this includes
+ * out[4]), retiring, and admitting beside a running step. */
+int32_t fvm_serve_times(fvm_server *s, double *out);
 /* Stops the service thread after its current step and frees everything. */
 int32_t fvm_serve_destroy(fvm_server *s);
 
