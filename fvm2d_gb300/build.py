@@ -5,7 +5,7 @@ Every translation unit is compiled in parallel:
     the FP64 kernels and the set-up kernels with ``--fmad=false`` so their
     arithmetic is rounded exactly as written; the FP32 kernels with
     contraction allowed, approximate division and square root (a few ulp)
-    and subnormals flushed to zero (the FP32 path is judged against the
+    and subnormals flushed to zero (the FP32 path is checked against the
     FP64 oracle by tolerance);
   * host C++ with ``-ffp-contract=off`` (the driver-side geometry must equal
     the serial FP64 arithmetic on x86 and on Arm alike).
