@@ -195,3 +195,14 @@ def test_ctypes_mirrors_match_the_abi_structs(fvm_lib):
     assert list(out) == [C.sizeof(L.FvmParams), C.sizeof(L.FvmMesh), C.sizeof(L.FvmGeom),
                          C.sizeof(L.FvmBatchCaps)]
 
+
+
+def test_probe_cli_parses():
+    """fvm2d_gb300.probe's options (the run itself needs a GPU)."""
+    import subprocess
+    import sys
+    r = subprocess.run([sys.executable, "-m", "fvm2d_gb300.probe", "--help"],
+                       capture_output=True, text=True, cwd=ROOT, timeout=120)
+    assert r.returncode == 0
+    for opt in ("--flow", "--meshes", "--iters", "--form", "--precision"):
+        assert opt in r.stdout
