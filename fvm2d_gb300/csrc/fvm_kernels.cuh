@@ -14,6 +14,9 @@
 
 #include "fvm_device.cuh"
 
+#ifndef FVM_FLUX_THREADS
+#define FVM_FLUX_THREADS 256  // threads of the FP32 flux pass's CTAs (one block of vertices each)
+#endif
 #ifndef FVM_FLUX_MINB32
 #define FVM_FLUX_MINB32 6   // resident CTAs per SM asked of the FP32 flux kernel
 #endif
@@ -25,6 +28,13 @@
 #endif
 
 namespace fvm {
+
+// FP32 flux pass: threads per CTA (one block of kBlockVerts vertices; the
+// edge trips spread over all of them, the per-vertex gather uses the first
+// kBlockVerts)
+constexpr int kFluxThreads = FVM_FLUX_THREADS;
+static_assert(kFluxThreads % 32 == 0 && kFluxThreads >= kBlockVerts && kFluxThreads <= 1024,
+              "flux CTA size");
 
 enum { MODE_RESIDUAL = 0, MODE_UPDATE = 1 };
 
@@ -700,7 +710,7 @@ __device__ __forceinline__ void block_conres_partial(bool have, R rho_new, R rho
       }
     }
     // warps' pairs summed by thread 0, still as pairs; one conversion to FP64
-    __shared__ DFloat s_sq[kBlockVerts / 32], s_mx[kBlockVerts / 32];
+    __shared__ DFloat s_sq[kFluxThreads / 32], s_mx[kFluxThreads / 32];
     if (lane == 0) {
       s_sq[wid] = sq2;
       s_mx[wid] = mx;
@@ -827,13 +837,14 @@ __device__ __forceinline__ void edge_flux(const ArenaPtrs<R> &A, const FluxConst
 }
 
 template <typename R, int FLUX>
-__global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_FLUX_MINB32 : 2) k_flux(ArenaPtrs<R> A, int stage, int mode,
-                                                      int irk, int routine) {
+__global__ void __launch_bounds__(sizeof(R) == 4 ? kFluxThreads : kBlockVerts,
+                                  sizeof(R) == 4 ? FVM_FLUX_MINB32 : 2)
+    k_flux(ArenaPtrs<R> A, int stage, int mode, int irk, int routine) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   R4<R> *s_flux = reinterpret_cast<R4<R> *>(smem_raw);
-  __shared__ double s_red[kBlockVerts / 32];
-  __shared__ double s_max[kBlockVerts / 32];
-  __shared__ int s_arg[kBlockVerts / 32];
+  __shared__ double s_red[kFluxThreads / 32];
+  __shared__ double s_max[kFluxThreads / 32];
+  __shared__ int s_arg[kFluxThreads / 32];
   int w0, nwork;
   work_range(A, w0, nwork);
   for (int w = w0 + blockIdx.x; w < nwork; w += gridDim.x) {

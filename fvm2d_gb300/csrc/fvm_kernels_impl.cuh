@@ -11,10 +11,10 @@ namespace fvm {
 // the device at once (its occupancy with this shared memory), so that no
 // partial second wave idles most SMs at the end of a launch.
 template <typename K>
-inline int fit_grid(const LaunchCfg &c, K kern, size_t smem) {
+inline int fit_grid(const LaunchCfg &c, K kern, size_t smem, int threads = kBlockVerts) {
   if (!c.fit) return c.grid;
   int occ = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kBlockVerts, smem) != cudaSuccess) {
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, smem) != cudaSuccess) {
     (void)cudaGetLastError();
     occ = 1;
   }
@@ -58,11 +58,12 @@ inline int fit_grid(const LaunchCfg &c, K kern, size_t smem) {
                           int irk, int routine) {                                          \
     size_t sm = smem_flux(c, (R *)nullptr);                                                \
     if (sm > kMaxSmem) return cudaErrorInvalidConfiguration;                              \
+    const int nt = sizeof(R) == 4 ? kFluxThreads : kBlockVerts;                           \
     switch (c.flux) {                                                                      \
-      case 1: k_flux<R, 1><<<fit_grid(c, k_flux<R, 1>, sm), kBlockVerts, sm, c.stream>>>(A, stage, mode, irk, routine); break; \
-      case 2: k_flux<R, 2><<<fit_grid(c, k_flux<R, 2>, sm), kBlockVerts, sm, c.stream>>>(A, stage, mode, irk, routine); break; \
-      case 3: k_flux<R, 3><<<fit_grid(c, k_flux<R, 3>, sm), kBlockVerts, sm, c.stream>>>(A, stage, mode, irk, routine); break; \
-      default: k_flux<R, 0><<<fit_grid(c, k_flux<R, 0>, sm), kBlockVerts, sm, c.stream>>>(A, stage, mode, irk, routine); \
+      case 1: k_flux<R, 1><<<fit_grid(c, k_flux<R, 1>, sm, nt), nt, sm, c.stream>>>(A, stage, mode, irk, routine); break; \
+      case 2: k_flux<R, 2><<<fit_grid(c, k_flux<R, 2>, sm, nt), nt, sm, c.stream>>>(A, stage, mode, irk, routine); break; \
+      case 3: k_flux<R, 3><<<fit_grid(c, k_flux<R, 3>, sm, nt), nt, sm, c.stream>>>(A, stage, mode, irk, routine); break; \
+      default: k_flux<R, 0><<<fit_grid(c, k_flux<R, 0>, sm, nt), nt, sm, c.stream>>>(A, stage, mode, irk, routine); \
     }                                                                                      \
     return cudaGetLastError();                                                             \
   }                                                                                        \
