@@ -226,34 +226,58 @@ void service(fvm_server *s) {
     auto sec = [](Clock::time_point a, Clock::time_point b) {
       return std::chrono::duration<double>(b - a).count();
     };
+    // this pass's times, published under the lock (fvm_serve_times reads them)
+    double d_admit = 0, d_tune = 0, d_step = 0, d_retire = 0, d_beside = 0;
+    int64_t d_steps = 0;
+    auto publish = [&]() {
+      std::lock_guard<std::mutex> lk(s->mu);
+      s->t_admit += d_admit;
+      s->t_tune += d_tune;
+      s->t_step += d_step;
+      s->t_retire += d_retire;
+      s->t_admit_beside += d_beside;
+      s->steps += d_steps;
+    };
     const Clock::time_point t0 = Clock::now();
     // with nothing resident, admit now; otherwise beside the next step
     if (s->resident.empty()) st = admit(s, false, nullptr);
     const Clock::time_point t1 = Clock::now();
-    s->t_admit += sec(t0, t1);
-    if (st) break;
-    if (s->resident.empty()) continue;
-    if (s->tune_every > 0 && s->steps % s->tune_every == 0) {
+    d_admit += sec(t0, t1);
+    if (st || s->resident.empty()) {
+      publish();
+      if (st) break;
+      continue;
+    }
+    int64_t steps_now;
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      steps_now = s->steps;
+    }
+    if (s->tune_every > 0 && steps_now % s->tune_every == 0) {
       int32_t choice = 0;
-      if ((st = fvm_batch_tune(s->b, 10, 0, nullptr, &choice))) break;
+      st = fvm_batch_tune(s->b, 10, 0, nullptr, &choice);
     }
     const Clock::time_point t2 = Clock::now();
-    s->t_tune += sec(t1, t2);
+    d_tune += sec(t1, t2);
     std::vector<Admitted> staged;
-    if ((st = fvm_batch_step(s->b, s->chunk))) break;
+    if (!st) st = fvm_batch_step(s->b, s->chunk);
     // uploads of waiting solves while the step runs
     const Clock::time_point ta = Clock::now();
-    st = admit(s, true, &staged);
+    if (!st) st = admit(s, true, &staged);
     const Clock::time_point tb = Clock::now();
-    s->t_admit_beside += sec(ta, tb);
-    if (st || (st = fvm_batch_sync(s->b))) break;
+    d_beside += sec(ta, tb);
+    if (!st) st = fvm_batch_sync(s->b);
     const Clock::time_point t3 = Clock::now();
-    s->t_step += sec(t2, t3);
-    if ((st = start_admitted(s, staged))) break;
-    s->t_admit += sec(t3, Clock::now());
-    s->steps++;
-    st = retire(s);
-    s->t_retire += sec(t3, Clock::now());
+    d_step += sec(t2, t3);
+    if (!st) st = start_admitted(s, staged);
+    const Clock::time_point t4 = Clock::now();
+    d_admit += sec(t3, t4);
+    if (!st) {
+      d_steps = 1;
+      st = retire(s);
+    }
+    d_retire += sec(t4, Clock::now());
+    publish();
     if (st) break;
     s->cv_done.notify_all();
   }
