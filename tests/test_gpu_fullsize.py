@@ -137,3 +137,29 @@ def test_fp32_converged_lift_drag_160x48(oracle_lib, fvm_lib):
     assert ost == 0
     assert abs(q["cl"] - oh["cl"][-1]) <= FP32_CL_ABS
     assert abs(q["cd"] - oh["cd"][-1]) <= FP32_CD_ABS
+
+
+def test_converged_naca0012_transonic_lift_and_drag(fvm_lib):
+    """Physics check, not parity: the 160 x 48 Euler case (NACA 0012,
+    M 0.8, 1.25 deg, Roe + limiter) run to a stalled residual.  The oracle
+    gives cl 0.3214, cd 0.02234 after 12000 iterations; published
+    fine-grid inviscid results for this case are near cl 0.35 and
+    cd 0.022.  FP64 and FP32 must both land in that neighbourhood, and FP32
+    within 1e-3 / 2e-4 of FP64."""
+    g = workload_grid("euler_160x48")
+    mesh = fvm_lib.build_geometry(g.coord, g.elem, g.ptype)
+    out = {}
+    for prec in (L.FP64, L.FP32):
+        b = Batch(prec, vertices=g.coord.shape[0], meshes=1)
+        s = b.add(fvm_lib.make_params(precision=prec, iflux=L.ROE, **EULER), mesh)
+        b.start(s, 12000)
+        b.step(12000)
+        b.sync()
+        q = b.poll(s)
+        assert q["status"] == 0 and q["niter"] == 12000
+        out[prec] = (q["cl"], q["cd"])
+        b.close()
+    cl64, cd64 = out[L.FP64]
+    cl32, cd32 = out[L.FP32]
+    assert abs(cl64 - 0.3214) < 2e-3 and abs(cd64 - 0.02234) < 2e-4
+    assert abs(cl32 - cl64) < 1e-3 and abs(cd32 - cd64) < 2e-4
