@@ -380,9 +380,10 @@ int32_t fvm_batch_set_form(fvm_batch *b, int32_t form);
  * Serving (no counterpart in the reference, whose driver runs one solve per
  * process, main.f:42-76): a continuous-batching service on one GPU.  One
  * service thread owns a batch arena; solves submitted from any thread are
- * admitted in arrival order while the arena has room, advanced together
- * `chunk` iterations at a time, and retired at their residual drop or
- * iteration cap, freeing room for the next.  With tune_every > 0 the
+ * admitted in arrival order while the arena has room (their uploads run
+ * beside the current step, and they join the batch when it ends), advanced
+ * together `chunk` iterations at a time, and retired at their residual
+ * drop or iteration cap, freeing room for the next.  With tune_every > 0 the
  * autotuner re-picks the form of the iteration every tune_every steps.
  * ---------------------------------------------------------------------- */
 typedef struct fvm_server fvm_server;
