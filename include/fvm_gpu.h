@@ -317,6 +317,10 @@ int32_t fvm_batch_add_prepared(fvm_batch *b, fvm_prepared *prep,
 int32_t fvm_prepared_free(fvm_prepared *prep);
 /* Device bytes a prepared mesh occupies in a batch of this precision. */
 int64_t fvm_prepared_bytes(const fvm_prepared *prep, int32_t precision);
+/* A slot's state in the driver's vertex order and FP64 (prim(4,np),
+ * nut, mul, mu(np), qx, qy(4,np)); the arrays cross as they are and are
+ * permuted and converted on the device.  set: prim is required, a NULL
+ * nut/mul/mu is left as it is; get: a NULL array is not read back. */
 int32_t fvm_batch_set_state(fvm_batch *b, int32_t slot, const double *prim,
                             const double *nut, const double *mul,
                             const double *mu, int32_t iterlast);
