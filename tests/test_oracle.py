@@ -7,7 +7,8 @@ tests/golden/ (which the oracle must keep reproducing):
   * Roe and KFVS return the exact Euler flux for equal states; so does
     HLLC once its momentum flux is rotated back (bugcompat=0);
   * every flux is rotationally invariant;
-  * a uniform freestream gives a zero residual at interior points;
+  * a uniform freestream gives a zero residual at interior points, with
+    and without the viscous terms;
   * Green-Gauss reproduces linear fields exactly at every point;
   * the van Albada limiter is 0 on a sign change;
   * the residual history falls on the 160x48 workload.
@@ -174,3 +175,22 @@ def test_oracle_reproduces_golden_fluxes(oracle_lib):
             st, f = o.flux(iflux, ref["ds"][k], ref["priml"][k], ref["primr"][k])
             assert st == ref[key + "_status"][k]
             np.testing.assert_allclose(f, ref[key][k], rtol=tol, atol=1e-300, err_msg=key)
+
+
+@pytest.mark.parametrize("iflow", [2, 3])
+def test_freestream_preservation_viscous(oracle_lib, small_grid, iflow):
+    """A uniform state has zero gradients, so the Green-Gauss viscous terms
+    (stresses and heat flux from the triangle gradients, with the SA eddy
+    viscosity in the turbulent case) vanish with the inviscid fluxes at
+    interior points."""
+    kw = dict(iflow=iflow, mach=0.5, aoa_deg=2.0, rey=5000.0 if iflow == 2 else 6.5e6, cfl=0.5,
+              bugcompat=0)
+    if iflow == 3:
+        kw.update(iflux=3, nut_ratio=3.0)
+    o = oracle_lib.Oracle(small_grid.coord, small_grid.elem, small_grid.ptype, **kw)
+    o.residu()
+    res = o.d("res")
+    interior = small_grid.ptype == 0
+    scale = np.abs(o.d("ds")).max()
+    assert np.abs(res[interior]).max() < 1e-12 * scale
+    assert np.abs(o.d("qx")).max() < 1e-12 and np.abs(o.d("qy")).max() < 1e-12
