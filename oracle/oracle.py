@@ -1,9 +1,13 @@
 """ctypes wrapper of the CPU oracle (test infrastructure).
 
-Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
-``bench.py`` import this module, as the checker.  The oracle is a serial
+Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU legs of
+``bench.py`` (its cpu_baseline and the reference arm) import this module,
+as the checker and the timed CPU implementation.  The oracle is a serial
 FP64 C restatement of the reference's Fortran hot path (fvm_oracle.c);
-``build()`` compiles it with the Makefile beside this file.
+``build()`` compiles it with the Makefile beside this file.  Parity is
+unpinned by the reference, which ships no tests or vectors and cannot be
+compiled here; tests/test_oracle.py pins it by answers derived from the
+equations.
 """
 from __future__ import annotations
 
