@@ -268,13 +268,18 @@ def run_gpu(args):
                               "device time of whole iterations"}
 
     # ---- e2e through the C ABI with host buffers -----------------------------
-    import numpy as np
-    init = []
+    # the driver's prim(4,np) arrays in pinned host memory (page-locked, as a
+    # driver that keeps its state for device transfers allocates it), filled
+    # before the timed region
+    init, finals = [], []
     for m in meshes:
         par = F.make_params(precision=F.FP32, **FLOW)
-        prim = np.tile([par.r_inf, par.u_inf, par.v_inf, par.p_inf], (m.np, 1)).astype(np.float64)
+        prim = torch.empty((m.np, 4), dtype=torch.float64, pin_memory=True).numpy()
+        prim[:] = [par.r_inf, par.u_inf, par.v_inf, par.p_inf]
         init.append(prim)
-    finals = [np.zeros((m.np, 4)) for m in meshes]
+        out = torch.empty((m.np, 4), dtype=torch.float64, pin_memory=True).numpy()
+        out[:] = 0.0
+        finals.append(out)
     b.sync()
     replicas.barrier()
     t0 = time.perf_counter()
@@ -296,7 +301,7 @@ def run_gpu(args):
                 rows += len(b.history(s, drained[j], n)["fres"])
                 drained[j] = st["niter"]
     for s, out in zip(slots, finals):     # the solution (prim) of each solve
-        out[:] = b.get_state(s, fields=("prim",))["prim"]
+        b.get_state(s, fields=("prim",), out={"prim": out})
     b.sync()
     e2e_s = replicas.max_over_ranks(time.perf_counter() - t0)
     e2e_value = replicas.sum_over_ranks(V * 3 * args.steps) / e2e_s
@@ -307,8 +312,9 @@ def run_gpu(args):
     e2e = {"value": e2e_value, "unit": UNIT,
            "h2d_bytes_per_step": round(h2d / args.steps, 1),
            "d2h_bytes_per_step": round(d2h / args.steps, 1),
-           "what": "fvm_batch_set_state (host FP64 prim -> device, permuted and converted "
-                   "there) + start + steps + RES.DAT rows + fvm_batch_get_state, wall clock"}
+           "what": "fvm_batch_set_state (pinned host FP64 prim -> device, permuted and "
+                   "converted there) + start + steps + RES.DAT rows + fvm_batch_get_state "
+                   "(into pinned host arrays), wall clock"}
     b.close()
 
     extra = {}
@@ -700,6 +706,49 @@ def run_accuracy(args):
     print(json.dumps(out), flush=True)
 
 
+PROBE_FLOWS = {
+    "euler": dict(mach=0.8, aoa_deg=1.25, cfl=1.0, iflux=1),
+    "laminar": dict(iflow=2, mach=0.5, aoa_deg=0.0, rey=5000.0, cfl=0.8, iflux=1),
+    "rans": dict(iflow=3, mach=0.7, aoa_deg=2.0, rey=6.5e6, cfl=0.5, iflux=3, nut_ratio=3.0),
+}
+
+
+def run_probe(args):
+    """A few iterations of a batch of jittered ni x nr O-grid solves of one
+    flow type (the flow parameters of the 512x192 laminar and 768x256 RANS-SA
+    workloads), for profiling that flow's kernels under ncu; prints one JSON
+    line with the wall time per iteration."""
+    import fvm2d_gb300 as F
+    from fvm2d_gb300.batch import Batch
+    from fvm2d_gb300.ogrid import naca_ogrid
+    prec = F.FP32 if args.precision == "fp32" else F.FP64
+    flow = PROBE_FLOWS[args.flow]
+    meshes = []
+    for k in range(args.meshes):
+        g = naca_ogrid(args.ni, args.nr, radius=20.0, first_spacing=5e-4, jitter=0.1, seed=2 + k)
+        meshes.append(F.build_geometry(g.coord, g.elem, g.ptype,
+                                       wall_distance=args.flow == "rans", bugcompat=0))
+    b = Batch(prec, vertices=sum(m.np for m in meshes), meshes=args.meshes,
+              viscous=args.flow != "euler")
+    par = F.make_params(precision=prec, bugcompat=0, **flow)
+    slots = [b.add(par, m) for m in meshes]
+    for s in slots:
+        b.start(s, args.warmup + args.steps)
+    b.set_form(args.form or "bulk")
+    b.step(args.warmup)
+    b.sync()
+    t0 = time.perf_counter()
+    b.step(args.steps)
+    b.sync()
+    dt = (time.perf_counter() - t0) / max(args.steps, 1)
+    polls = [b.poll(s) for s in slots]
+    out = {"mode": "probe", "flow": args.flow, "precision": args.precision,
+           "meshes": args.meshes, "vertices_per_mesh": meshes[0].np, "form": args.form or "bulk",
+           "iters": args.steps, "ms_per_iter": dt * 1e3, "status": [p["status"] for p in polls]}
+    b.close()
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -713,7 +762,14 @@ def main():
                     choices=["bulk", "loads", "vertex", "fused", "split+overlap", "fused+overlap",
                              "split+overlap4", "split+overlap8"],
                     help="use this form of the iteration instead of the autotuner's choice")
-    ap.add_argument("--mode", choices=["throughput", "serve", "accuracy"], default="throughput")
+    ap.add_argument("--mode", choices=["throughput", "serve", "accuracy", "probe"],
+                    default="throughput")
+    ap.add_argument("--flow", choices=sorted(PROBE_FLOWS), default="euler",
+                    help="probe: flow type of the batch")
+    ap.add_argument("--ni", type=int, default=NI, help="probe: wall points per grid")
+    ap.add_argument("--nr", type=int, default=NR, help="probe: radial points per grid")
+    ap.add_argument("--precision", choices=["fp32", "fp64"], default="fp32",
+                    help="probe: precision of the batch")
     ap.add_argument("--requests", type=int, default=512)
     ap.add_argument("--rate", type=float, default=20.0)
     ap.add_argument("--seed", type=int, default=0)
@@ -739,6 +795,10 @@ def main():
         from fvm2d_gb300 import build
         build.build()
         run_accuracy(args)
+    elif args.mode == "probe":
+        from fvm2d_gb300 import build
+        build.build()
+        run_probe(args)
     else:
         from fvm2d_gb300 import build
         build.build()

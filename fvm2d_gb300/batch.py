@@ -131,15 +131,26 @@ class Batch:
 
     STATE_FIELDS = ("prim", "nut", "mul", "mu", "qx", "qy")
 
-    def get_state(self, slot, fields=STATE_FIELDS) -> dict:
+    def get_state(self, slot, fields=STATE_FIELDS, out=None) -> dict:
         """The slot's state in driver order (FP64); `fields` limits the
-        arrays read back (the others are passed to the C ABI as NULL)."""
+        arrays read back (the others are passed to the C ABI as NULL).
+        `out` may hold caller-owned C-contiguous float64 arrays (for example
+        in pinned memory) for some of the fields; they are filled in place."""
         n = self._meshes[slot].np
         bad = set(fields) - set(self.STATE_FIELDS)
         if bad:
             raise ValueError(f"unknown state fields {sorted(bad)}")
-        out = {k: np.zeros((n, 4)) if k in ("prim", "qx", "qy") else np.zeros(n)
-               for k in fields}
+        given = dict(out or {})
+        out = {}
+        for k in fields:
+            shape = (n, 4) if k in ("prim", "qx", "qy") else (n,)
+            a = given.get(k)
+            if a is None:
+                a = np.zeros(shape)
+            elif (a.shape != shape or a.dtype != np.float64 or not a.flags.c_contiguous
+                  or not a.flags.writeable):
+                raise ValueError(f"out[{k!r}] must be a writeable C-contiguous float64 {shape}")
+            out[k] = a
         ptr = [dptr(out[k]) if k in out else None for k in self.STATE_FIELDS]
         check(L.lib().fvm_batch_get_state(self.h, slot, *ptr), "fvm_batch_get_state")
         return out

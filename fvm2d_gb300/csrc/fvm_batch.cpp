@@ -353,7 +353,9 @@ int32_t put_ctl(fvm_batch *b, int slot, const MeshCtl &c) {
 
 // host double [np][k] (driver order) -> device [np][k] of the slot: the
 // array goes to the device as it is; a kernel permutes it into arena order
-// and converts it to the batch precision
+// and converts it to the batch precision.  Queued on the batch stream (the
+// staging buffer is reused in stream order); the caller synchronises once
+// after its last transfer.
 int32_t put_vertex(fvm_batch *b, const Slot &s, void *dst_base, const double *src, int k,
                    size_t stride) {
   const int np = s.L.np;
@@ -364,12 +366,12 @@ int32_t put_vertex(fvm_batch *b, const Slot &s, void *dst_base, const double *sr
   unsigned char *dst = static_cast<unsigned char *>(dst_base) + (size_t)s.off[P_V] * stride;
   FVM_TRY(b, cudaMemcpyAsync(stage, src, n, cudaMemcpyHostToDevice, b->stream));
   FVM_TRY(b, launch_put_vertex(b->rsz, dst, stride, stage, b->orig + s.off[P_V], np, k, b->stream));
-  FVM_TRY(b, cudaStreamSynchronize(b->stream));
   return FVM_OK;
 }
 
 // device [np][stride] of the slot, values c0..c0+k-1 -> host double [np][k]
-// in driver order (permuted and widened on the device)
+// in driver order (permuted and widened on the device); queued on the batch
+// stream, complete after the caller's synchronisation
 int32_t get_vertex(fvm_batch *b, const Slot &s, double *dst, const void *src_base, int k,
                    size_t stride, int c0 = 0) {
   const int np = s.L.np;
@@ -380,6 +382,10 @@ int32_t get_vertex(fvm_batch *b, const Slot &s, double *dst, const void *src_bas
   const unsigned char *src = static_cast<const unsigned char *>(src_base) + (size_t)s.off[P_V] * stride;
   FVM_TRY(b, launch_get_vertex(b->rsz, stage, src, stride, b->orig + s.off[P_V], np, k, c0, b->stream));
   FVM_TRY(b, cudaMemcpyAsync(dst, stage, n, cudaMemcpyDeviceToHost, b->stream));
+  return FVM_OK;
+}
+
+int32_t sync_stream(fvm_batch *b) {
   FVM_TRY(b, cudaStreamSynchronize(b->stream));
   return FVM_OK;
 }
@@ -1243,7 +1249,7 @@ extern "C" int32_t fvm_batch_get_state(fvm_batch *b, int32_t slot, double *prim,
   if (mu && (st = get_vertex(b, *S, mu, b->mu, 1, r))) return st;
   if (qx && (st = get_vertex(b, *S, qx, b->grad, 4, 8 * r, 0))) return st;
   if (qy && (st = get_vertex(b, *S, qy, b->grad, 4, 8 * r, 4))) return st;
-  return FVM_OK;
+  return sync_stream(b);
 }
 
 extern "C" int32_t fvm_batch_start(fvm_batch *b, int32_t slot, int32_t nmax, double minres) {
@@ -1660,12 +1666,14 @@ extern "C" int32_t fvm_gpu_get_state(fvm_handle *h, double *prim, double *nut, d
 
 extern "C" int32_t fvm_gpu_get_residual(fvm_handle *h, double *res) {
   if (!h || !res) return FVM_ERR_ARG;
-  return get_vertex(h->b, hslot(h), res, h->b->res, 4, 4 * h->b->rsz);
+  const int32_t st = get_vertex(h->b, hslot(h), res, h->b->res, 4, 4 * h->b->rsz);
+  return st ? st : sync_stream(h->b);
 }
 
 extern "C" int32_t fvm_gpu_get_dt(fvm_handle *h, double *dt) {
   if (!h || !dt) return FVM_ERR_ARG;
-  return get_vertex(h->b, hslot(h), dt, h->b->dt, 1, h->b->rsz);
+  const int32_t st = get_vertex(h->b, hslot(h), dt, h->b->dt, 1, h->b->rsz);
+  return st ? st : sync_stream(h->b);
 }
 
 extern "C" int32_t fvm_gpu_get_prim_old(fvm_handle *h, double *prim_old) {
@@ -1673,7 +1681,8 @@ extern "C" int32_t fvm_gpu_get_prim_old(fvm_handle *h, double *prim_old) {
   MeshCtl c;
   int32_t st = get_ctl(h->b, h->slot, c);
   if (st) return st;
-  return get_vertex(h->b, hslot(h), prim_old, h->b->st[(c.phase + 2) % 3], 4, 4 * h->b->rsz);
+  st = get_vertex(h->b, hslot(h), prim_old, h->b->st[(c.phase + 2) % 3], 4, 4 * h->b->rsz);
+  return st ? st : sync_stream(h->b);
 }
 
 extern "C" int32_t fvm_gpu_save_old(fvm_handle *h) {

@@ -668,7 +668,10 @@ __device__ __forceinline__ void block_conres_partial(bool have, R rho_new, R rho
       const double gra = double(rho_new) - double(rho_old);
       d2 = gra * gra;
       dabs = fabs(gra);
+      // conres.f:17-21 keeps a point only when |gra| > fresi, which a NaN
+      // never is: a NaN poisons the sum of squares, not the maximum
       if (dabs > 0.0) darg = orig;
+      else dabs = 0.0;
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
@@ -695,6 +698,7 @@ __device__ __forceinline__ void block_conres_partial(bool have, R rho_new, R rho
       sq2 = two_sum(h2, l2);
       mx = g.hi >= 0.f ? g : DFloat{-g.hi, -g.lo};
       if (mx.hi > 0.f) darg = orig;
+      else mx = DFloat{0.f, 0.f};   // NaN or no change (see the FP64 branch)
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
@@ -1701,6 +1705,7 @@ __global__ void __launch_bounds__(kBlockVerts) k_conres_part(ArenaPtrs<R> A) {
       d2 = gra * gra;
       dabs = fabs(gra);
       if (dabs > 0.0) darg = A.orig[v];
+      else dabs = 0.0;   // a NaN never becomes the maximum (conres.f:17-21)
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {

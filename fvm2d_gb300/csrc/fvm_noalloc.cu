@@ -35,6 +35,7 @@ struct Result {
   int argmax;
   int pad;
 };
+static_assert(sizeof(Partial) == 24 && sizeof(Result) == 24, "scratch record sizes");
 
 // The scratch: partials of the first pass, and the reduced result.  Shared
 // by every call on a device; each call overwrites the partials it reads.
@@ -67,7 +68,10 @@ __global__ void __launch_bounds__(kThreads) k_parts(const double *__restrict__ p
     const double gra = prim[4 * (size_t)i] - prim_old[4 * (size_t)i];   // conres.f:15
     s = gra * gra;
     m = fabs(gra);
+    // conres.f:17-21 takes a point only when |gra| > fresi, which a NaN
+    // never is: a NaN poisons the sum of squares but not the maximum
     if (m > 0.0) a = i + 1;
+    else m = 0.0;
   }
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1)

@@ -15,7 +15,9 @@
 //           state when asked) are kept for the caller, the arena ranges
 //           freed;
 // and, when asked, re-runs the autotuner every `tune_every` steps.
+#include <atomic>
 #include <chrono>
+#include <cmath>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
@@ -52,6 +54,10 @@ struct Ticket {
 };
 
 constexpr int kTail = 256;
+// fvm_serve_wait timeouts at or above this many seconds (about 32 years,
+// and +inf) wait until the ticket is done; the bound keeps the conversion
+// to clock ticks finite
+constexpr double kWaitForever = 1e9;
 
 double seconds(Clock::time_point a, Clock::time_point b) {
   return std::chrono::duration<double>(b - a).count();
@@ -76,9 +82,20 @@ struct fvm_server {
   int32_t error = FVM_OK;               // a CUDA failure stops the service
   bool stop = false;
   std::thread worker;
+  // API calls in progress (counted before the mutex is taken): destroy
+  // frees the server only when none is left inside
+  std::atomic<int> callers{0};
 };
 
 namespace {
+
+// Counts an API call as in progress for its whole duration, including the
+// wait for the mutex.
+struct InCall {
+  fvm_server *s;
+  explicit InCall(fvm_server *srv) : s(srv) { s->callers.fetch_add(1); }
+  ~InCall() { s->callers.fetch_sub(1); }
+};
 
 void finish(fvm_server *s, int64_t id, Ticket &t, int32_t status) {
   t.status = status;
@@ -321,6 +338,7 @@ extern "C" int32_t fvm_serve_submit(fvm_server *s, const fvm_params *p, const fv
                                     int32_t nmax, double minres, int32_t keep_state,
                                     int64_t *ticket) {
   if (!s || !p || !m || !ticket || nmax < 1) return FVM_ERR_ARG;
+  InCall in_call(s);
   *ticket = 0;
   fvm_prepared *prep = nullptr;
   const int32_t st = fvm_batch_prepare(p, m, &prep);   // on the caller's thread
@@ -347,6 +365,7 @@ extern "C" int32_t fvm_serve_submit(fvm_server *s, const fvm_params *p, const fv
 
 extern "C" int32_t fvm_serve_poll(fvm_server *s, int64_t ticket, int32_t *state) {
   if (!s || !state) return FVM_ERR_ARG;
+  InCall in_call(s);
   std::lock_guard<std::mutex> lk(s->mu);
   auto it = s->tickets.find(ticket);
   if (it == s->tickets.end()) return FVM_ERR_ARG;
@@ -356,12 +375,22 @@ extern "C" int32_t fvm_serve_poll(fvm_server *s, int64_t ticket, int32_t *state)
 
 extern "C" int32_t fvm_serve_wait(fvm_server *s, int64_t ticket, double timeout_s,
                                   int32_t *state) {
-  if (!s || !state) return FVM_ERR_ARG;
+  if (!s || !state || std::isnan(timeout_s)) return FVM_ERR_ARG;
+  InCall in_call(s);
   std::unique_lock<std::mutex> lk(s->mu);
+  if (s->tickets.find(ticket) == s->tickets.end()) return FVM_ERR_ARG;
+  // the ticket is looked up again after every wake-up: another thread may
+  // have released it meanwhile
+  auto done = [&] {
+    auto it = s->tickets.find(ticket);
+    return it == s->tickets.end() || it->second.state == 2;
+  };
+  if (timeout_s >= kWaitForever)
+    s->cv_done.wait(lk, done);
+  else if (timeout_s > 0)
+    s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), done);
   auto it = s->tickets.find(ticket);
   if (it == s->tickets.end()) return FVM_ERR_ARG;
-  s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s < 0 ? 0 : timeout_s),
-                      [&] { return it->second.state == 2; });
   *state = it->second.state;
   return FVM_OK;
 }
@@ -370,6 +399,7 @@ extern "C" int32_t fvm_serve_result(fvm_server *s, int64_t ticket, int32_t *stat
                                     int32_t *niter, double *fres, double *cl, double *cd,
                                     double *tail, double *times) {
   if (!s) return FVM_ERR_ARG;
+  InCall in_call(s);
   std::lock_guard<std::mutex> lk(s->mu);
   auto it = s->tickets.find(ticket);
   if (it == s->tickets.end() || it->second.state != 2) return FVM_ERR_ARG;
@@ -394,6 +424,7 @@ extern "C" int32_t fvm_serve_result(fvm_server *s, int64_t ticket, int32_t *stat
 
 extern "C" int32_t fvm_serve_state(fvm_server *s, int64_t ticket, double *prim, double *nut) {
   if (!s || !prim) return FVM_ERR_ARG;
+  InCall in_call(s);
   std::lock_guard<std::mutex> lk(s->mu);
   auto it = s->tickets.find(ticket);
   if (it == s->tickets.end() || it->second.state != 2 || it->second.prim.empty())
@@ -405,6 +436,7 @@ extern "C" int32_t fvm_serve_state(fvm_server *s, int64_t ticket, double *prim, 
 
 extern "C" int32_t fvm_serve_release(fvm_server *s, int64_t ticket) {
   if (!s) return FVM_ERR_ARG;
+  InCall in_call(s);
   std::lock_guard<std::mutex> lk(s->mu);
   auto it = s->tickets.find(ticket);
   if (it == s->tickets.end() || it->second.state != 2) return FVM_ERR_ARG;
@@ -414,6 +446,7 @@ extern "C" int32_t fvm_serve_release(fvm_server *s, int64_t ticket) {
 
 extern "C" int32_t fvm_serve_stats(fvm_server *s, int64_t *out) {
   if (!s || !out) return FVM_ERR_ARG;
+  InCall in_call(s);
   std::lock_guard<std::mutex> lk(s->mu);
   int64_t queued = 0, running = 0;
   for (const auto &kv : s->tickets) {
@@ -431,6 +464,7 @@ extern "C" int32_t fvm_serve_stats(fvm_server *s, int64_t *out) {
 
 extern "C" int32_t fvm_serve_times(fvm_server *s, double *out) {
   if (!s || !out) return FVM_ERR_ARG;
+  InCall in_call(s);
   std::lock_guard<std::mutex> lk(s->mu);
   out[0] = s->t_admit;
   out[1] = s->t_tune;
@@ -448,8 +482,20 @@ extern "C" int32_t fvm_serve_destroy(fvm_server *s) {
   }
   s->cv_work.notify_all();
   if (s->worker.joinable()) s->worker.join();
-  for (auto &kv : s->tickets)
-    if (kv.second.prep) fvm_prepared_free(kv.second.prep);
+  {
+    // solves that never finished end with FVM_ERR_STATE, which wakes their
+    // waiters
+    std::lock_guard<std::mutex> lk(s->mu);
+    for (auto &kv : s->tickets) {
+      if (kv.second.prep) fvm_prepared_free(kv.second.prep);
+      kv.second.prep = nullptr;
+      if (kv.second.state != 2) finish(s, kv.first, kv.second, FVM_ERR_STATE);
+    }
+  }
+  s->cv_done.notify_all();
+  // calls already inside the API (waiters woken above, callers queued on
+  // the mutex) leave before the server is freed
+  while (s->callers.load() > 0) std::this_thread::sleep_for(std::chrono::microseconds(100));
   const int32_t st = fvm_batch_destroy(s->b);
   delete s;
   return st;

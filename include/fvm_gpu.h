@@ -246,7 +246,11 @@ int32_t fvm_geom_free(fvm_geom *g);
  * The first call on a device looks up the scratch address on that device,
  * so make it before any stream capture.  All calls share the scratch and
  * run on the default stream, synchronously: calls that overlap on the GPU
- * (from several host threads) race. */
+ * (from several host threads) race.  The legacy default stream is not
+ * ordered against non-blocking streams or async queues, so finish the
+ * writes of prim and prim_old first (`!$acc wait`, cudaStreamSynchronize
+ * on the writing stream).  A NaN density change makes fres NaN but, as in
+ * conres.f, never becomes fresi/iresi. */
 #define FVM_NOALLOC_MAX_POINTS (1 << 20)
 int32_t fvm_gpu_conres_noalloc(const double *prim, const double *prim_old,
                                int32_t np, int32_t first, double *fres1,
@@ -402,6 +406,8 @@ int32_t fvm_serve_submit(fvm_server *s, const fvm_params *p,
                          int32_t keep_state, int64_t *ticket);
 /* *state: 0 queued, 1 running, 2 done. */
 int32_t fvm_serve_poll(fvm_server *s, int64_t ticket, int32_t *state);
+/* Waits until the ticket is done or timeout_s seconds pass (<= 0: do not
+ * wait; >= 1e9 or +inf: wait until done; NaN: FVM_ERR_ARG). */
 int32_t fvm_serve_wait(fvm_server *s, int64_t ticket, double timeout_s,
                        int32_t *state);
 /* Results of a done solve: status (FVM_OK, a stop of the method, or
@@ -423,7 +429,11 @@ int32_t fvm_serve_stats(fvm_server *s, int64_t *out);
  * tuning, stepping (launching and waiting for the GPU; this includes
  * out[4]), retiring, and admitting beside a running step. */
 int32_t fvm_serve_times(fvm_server *s, double *out);
-/* Stops the service thread after its current step and frees everything. */
+/* Stops the service thread after its current step and frees everything.
+ * Solves not yet done end with FVM_ERR_STATE, so threads blocked in
+ * fvm_serve_wait wake up; destroy returns only after every fvm_serve_* call
+ * already in progress on other threads has returned.  No fvm_serve_* call
+ * on this server may start once destroy has been called. */
 int32_t fvm_serve_destroy(fvm_server *s);
 
 /* Layout statistics of a mesh after renumbering (no GPU needed):

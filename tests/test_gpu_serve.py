@@ -90,3 +90,40 @@ def test_native_service_equals_alone(fvm_lib):
     st = srv.stats()
     assert st["submitted"] == 7 and st["done"] == 7 and st["status"] == 0
     srv.close()
+
+
+def test_native_service_destroy_wakes_waiters(fvm_lib):
+    """Destroying the service while other threads wait on unfinished solves
+    (one waiting 'forever') ends those solves with FVM_ERR_STATE: the waiters
+    return, and destroy frees the server only after they have left."""
+    import ctypes as C
+    import threading
+
+    from fvm2d_gb300 import serve
+    reqs = serve.generate_requests(n=2, rate=100.0, seed=6, pmin=4000, pmax=4000, laminar_frac=0.0)
+    srv = serve.NativeServer(vertices=20000, meshes=2, chunk=10, workers=1, max_iter=10 ** 6,
+                             minres=0.0)
+    tickets = []
+    for r in reqs:
+        g = serve.grid_for(r)
+        tickets.append(srv.submit(serve.params_for(r, L.FP32),
+                                  fvm_lib.build_geometry(g.coord, g.elem, g.ptype)))
+    states = {}
+
+    def waiter(t, timeout):
+        st = C.c_int32(-1)
+        rc = L.lib().fvm_serve_wait(srv.h, t, timeout, C.byref(st))
+        states[t] = (rc, st.value)
+
+    th = [threading.Thread(target=waiter, args=(tickets[0], float("inf"))),
+          threading.Thread(target=waiter, args=(tickets[1], 1e12))]
+    for t in th:
+        t.start()
+    assert not srv.wait(tickets[0], 0.5)      # still running (10^6 iterations allowed)
+    st = C.c_int32(-1)
+    assert L.lib().fvm_serve_wait(srv.h, tickets[0], float("nan"), C.byref(st)) == L.ERR_ARG
+    srv.close()                               # returns only after both waiters left
+    for t in th:
+        t.join(timeout=30.0)
+        assert not t.is_alive()
+    assert states == {tickets[0]: (L.OK, 2), tickets[1]: (L.OK, 2)}

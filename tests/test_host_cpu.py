@@ -197,12 +197,14 @@ def test_ctypes_mirrors_match_the_abi_structs(fvm_lib):
 
 
 
-def test_probe_cli_parses():
-    """fvm2d_gb300.probe's options (the run itself needs a GPU)."""
+def test_bench_cli_parses():
+    """bench.py's options, including the probe mode used by the viscous-path
+    profiles (the runs themselves need a GPU)."""
     import subprocess
     import sys
-    r = subprocess.run([sys.executable, "-m", "fvm2d_gb300.probe", "--help"],
+    r = subprocess.run([sys.executable, "bench.py", "--help"],
                        capture_output=True, text=True, cwd=ROOT, timeout=120)
     assert r.returncode == 0
-    for opt in ("--flow", "--meshes", "--iters", "--form", "--precision"):
+    for opt in ("--mode", "probe", "--flow", "--meshes", "--steps", "--form", "--precision",
+                "--ni", "--nr"):
         assert opt in r.stdout

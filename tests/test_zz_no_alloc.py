@@ -72,3 +72,23 @@ def test_noalloc_refuses_oversize_and_zero(fvm_lib):
     st = L.lib().fvm_gpu_conres_noalloc(C.c_void_p(small.data_ptr()), C.c_void_p(small.data_ptr()),
                                         8, 1, C.byref(f1), C.byref(f), None, None)
     assert st == L.ERR_ZERO_FIRST_RES
+
+
+def test_noalloc_nan_density_change_is_never_the_maximum(fvm_lib):
+    """conres.f:17-21 compares |gra| > fresi, which is false for a NaN: a NaN
+    density change makes fres NaN but fresi/iresi come from the finite
+    points (first maximum on ties)."""
+    rng = np.random.default_rng(9)
+    n = 3000
+    prim_old = rng.uniform(0.5, 1.5, (n, 4))
+    prim = prim_old.copy()
+    prim[:, 0] += rng.uniform(-1e-3, 1e-3, n)
+    prim_old[700, 0] = prim_old[2500, 0] = 1.0
+    prim[700, 0] = 1.0 + 2.0 ** -8                    # the largest finite change
+    prim[2500, 0] = 1.0 - 2.0 ** -8                   # ties it exactly, later index
+    prim[10, 0] = np.nan
+    for first in (True, False):
+        st, _, f, fi, ir = noalloc(prim, prim_old, first, 1.0)
+        assert st == L.OK
+        assert np.isnan(f)
+        assert fi == 2.0 ** -8 and ir == 701
