@@ -24,9 +24,18 @@ Also reported on the same line:
   cpu_baseline  the CPU oracle (the serial FP64 restatement of the
                 reference, single thread) on one mesh of the same workload;
   vs_fp64_gpu   the plain FP64 single-mesh GPU path on the same workload;
-  fluxes        FP32 batched throughput with KFVS and HLLC.
+  fluxes        FP32 batched throughput with KFVS and HLLC;
+  serving       the request workload (512 seeded NACA 4-digit solves,
+                Poisson arrivals at 20/s, 5k-400k vertices, 70% Euler / 30%
+                laminar) through the continuous-batching service: converged
+                solves/s, p50/p99 latency, how many solves reached the
+                residual drop, hit the iteration cap or failed; the plain
+                FP64 single-mesh path measured on a size-stratified sample
+                of the same requests (strict and FMA builds), and the
+                served lift/drag against those FP64 solves.
 ``--impl reference`` times the reference's CPU implementation (the oracle
-port; no Fortran compiler exists here) on all host cores instead.
+port; no Fortran compiler exists on this machine or the GPU host, probed
+and recorded in the line) on all host cores instead.
 """
 from __future__ import annotations
 
@@ -212,7 +221,8 @@ def run_gpu(args):
     # kernels one at a time (no overlapped chains), so each launch's time
     # is its own
     alone = {"split+overlap": "bulk", "split+overlap4": "bulk", "split+overlap8": "bulk",
-             "fused+overlap": "fused"}.get(b.form, b.form)
+             "fused+overlap": "fused", "pipe+overlap": "pipe",
+             "pipe+overlap4": "pipe"}.get(b.form, b.form)
     b.set_form(alone)
     b.timing(True)
     b.step(1)
@@ -360,6 +370,10 @@ def run_gpu(args):
         extra["fluxes"] = fl
         # CPU oracle, single thread, bounded sample on one mesh of the workload
         extra["cpu_baseline"] = cpu_baseline(meshes, args)
+        # the serving half of the metric: converged solves/s and latency of
+        # the request workload against the FP64 path measured on a sample
+        if size == 1:
+            extra["serving"] = serving(args)
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": size,
@@ -418,9 +432,27 @@ def cpu_baseline(meshes, args):
                       f"serial FP64 oracle (gcc -O3 -ffp-contract=off), {wall:.1f} s"}
 
 
+def fortran_probe():
+    """Whether a Fortran compiler exists on this machine (the reference is
+    Fortran 77 built with gfortran -O3); recorded in the reference line."""
+    import shutil
+    found = {}
+    for c in ("gfortran", "f95", "f77", "flang", "flang-new", "lfortran"):
+        path = shutil.which(c)
+        if path:
+            try:
+                v = subprocess.run([path, "--version"], capture_output=True, text=True,
+                                   timeout=30).stdout.splitlines()[:1]
+            except (OSError, subprocess.TimeoutExpired):
+                v = []
+            found[c] = {"path": path, "version": v[0] if v else None}
+    return found
+
+
 def run_reference(args):
     """The reference's CPU implementation of the path: the oracle port (the
-    Fortran reference cannot be compiled here), one independent solve per
+    Fortran reference cannot be compiled: no Fortran compiler on this
+    machine, see the line's `fortran` record), one independent solve per
     host core."""
     from fvm2d_gb300 import replicas
     rank, local, size = replicas.world()
@@ -470,69 +502,72 @@ def run_reference(args):
                        "parallelism": f"{cores} host threads"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": sample},
+            "fortran": fortran_probe() or "no Fortran compiler on PATH (gfortran, f95, f77, "
+                                          "flang, flang-new, lfortran probed)",
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     replicas.finish()
 
 
-def fp64_iteration_ladder(sizes=(5000, 20000, 80000, 200000, 400000)):
-    """Per-iteration time of the plain FP64 single-mesh GPU path (one mesh per
-    batch, CUDA-event timed) on a ladder of grid sizes, Euler and laminar."""
-    import torch
+def fp64_solves(reqs, max_iter, minres):
+    """The plain FP64 single-mesh path, one solve at a time: for each request
+    a handle is created from its grid (upload, renumbering, device
+    structures) and fvm_gpu_iterate runs it to its own stop (residual drop
+    or iteration cap).  Wall seconds of create + iterate per solve, with the
+    mean lift and drag of its last Result.TAIL iterations."""
+    import numpy as np
 
     import fvm2d_gb300 as F
     from fvm2d_gb300 import serve
-    from fvm2d_gb300.batch import Batch
-    out = {}
-    for lam in (False, True):
-        pts = []
-        for n in sizes:
-            req = serve.Request(rid=0, arrival=0.0, thickness=0.12, camber=0.02, camber_pos=0.4,
-                                npts=n, laminar=lam, mach=0.6, aoa_deg=2.0,
-                                rey=5000.0 if lam else 0.0, seed=0)
-            prep = serve.prepare(req, F.FP64)
-            P = prep.np
-            b = Batch(F.FP64, vertices=P, meshes=1, viscous=True)
-            s = b.add_prepared(prep)
-            b.start(s, 40)
-            b.step(3)
-            b.sync()
-            ext = torch.cuda.ExternalStream(b.stream())
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            k = 10 if P < 100000 else 5
-            e0.record(ext)
-            b.step(k)
-            e1.record(ext)
-            b.sync()
-            pts.append((P, e0.elapsed_time(e1) / 1e3 / k))
-            b.close()
-        out["laminar" if lam else "euler"] = pts
+    out = []
+    for req in reqs:
+        g = serve.grid_for(req)
+        mesh = F.build_geometry(g.coord, g.elem, g.ptype)
+        par = serve.params_for(req, F.FP64)
+        t0 = time.perf_counter()
+        s = F.Solver(par, mesh)
+        st, h = s.iterate(max_iter, minres, raise_on_error=False)
+        dt = time.perf_counter() - t0
+        s.close()
+        k = min(serve.Result.TAIL, len(h["cl"]))
+        out.append({"rid": req.rid, "vertices": mesh.np, "laminar": req.laminar,
+                    "seconds": dt, "status": int(st), "iterations": int(len(h["fres"])),
+                    "fres": float(h["fres"][-1]) if len(h["fres"]) else None,
+                    "cl_tail": float(np.mean(h["cl"][-k:])) if k else None,
+                    "cd_tail": float(np.mean(h["cd"][-k:])) if k else None})
     return out
 
 
-def interp_time(ladder, P):
-    """Per-iteration time at P vertices: log-log interpolation on the
-    ladder, proportional to P beyond its ends."""
-    import numpy as np
-    ps = np.array([p for p, _ in ladder], dtype=float)
-    ts = np.array([t for _, t in ladder], dtype=float)
-    if P <= ps[0]:
-        return float(ts[0] * P / ps[0])
-    if P >= ps[-1]:
-        return float(ts[-1] * P / ps[-1])
-    return float(np.exp(np.interp(np.log(P), np.log(ps), np.log(ts))))
+def fp64_solves_subprocess(rids, args, variant):
+    """fp64_solves in a child process that loads the given library variant."""
+    env = dict(os.environ, FVM_LIB_VARIANT=variant)
+    cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--mode", "fp64-solves",
+           "--rids", ",".join(str(r) for r in rids), "--requests", str(args.requests),
+           "--rate", str(args.rate), "--seed", str(args.seed), "--max-iter", str(args.max_iter),
+           "--minres", str(args.minres)]
+    r = subprocess.run(cmd, capture_output=True, text=True, env=env, timeout=1800)
+    if r.returncode != 0:
+        raise RuntimeError(f"fp64 solves ({variant}) failed: {r.stderr[-2000:]}")
+    return json.loads(r.stdout.strip().splitlines()[-1])["solves"]
 
 
-def run_serve(args):
-    """Batched FP32 serving of the request workload; converged solves/s and
-    latency percentiles, with the FP64 single-mesh path's solves/s."""
-    import torch
-
-    import fvm2d_gb300 as F
+def run_fp64_solves(args):
+    """--mode fp64-solves: fp64_solves on the given requests of the workload."""
     from fvm2d_gb300 import serve
-    torch.cuda.init()
+    reqs = {r.rid: r for r in serve.generate_requests(n=args.requests, rate=args.rate,
+                                                      seed=args.seed)}
+    pick = [reqs[int(x)] for x in args.rids.split(",") if x]
+    print(json.dumps({"mode": "fp64-solves", "library": os.environ.get("FVM_LIB_VARIANT", ""),
+                      "solves": fp64_solves(pick, args.max_iter, args.minres)}), flush=True)
+
+
+def serving(args):
+    """Batched FP32 serving of the request workload (the native continuous-
+    batching service), and the plain FP64 single-mesh path measured on a
+    sample of the same requests, in the strict build (no FMA contraction,
+    bitwise the reference's arithmetic) and the FMA build."""
+    from fvm2d_gb300 import serve
     reqs = serve.generate_requests(n=args.requests, rate=args.rate, seed=args.seed)
     cls = serve.NativeServer if args.service == "native" else serve.Server
     srv = cls(vertices=args.arena_vertices, meshes=512, chunk=args.chunk,
@@ -540,80 +575,65 @@ def run_serve(args):
               tune_every=args.tune_every)
     res, stats = srv.run(reqs)
     srv.close()
-    acc = fp64_accuracy(reqs, res)
-    ladder = fp64_iteration_ladder()
-    t64 = sum(interp_time(ladder["laminar" if r.laminar else "euler"], r.npts) * r.niter
-              for r in res if r.status == 0)
-    solves64 = stats["completed_ok"] / t64
-    line = {"metric": METRIC, "mode": "serve", "value": stats["solves_per_s"],
-            "unit": "converged solves/s", "higher_is_better": True, "n_gpus": 1,
-            "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"{args.requests} NACA 4-digit requests, Poisson {args.rate}/s, "
-                                   "5k-400k vertices log-uniform, 70% Euler / 30% laminar, "
-                                   f"stop at drop {args.minres} or {args.max_iter} iterations",
-                       "arena_vertices": args.arena_vertices, "chunk": args.chunk,
-                       "tune_every_steps": args.tune_every, "service": args.service},
-            "latency_s": {"p50": stats["p50_latency_s"], "p99": stats["p99_latency_s"]},
-            "stats": stats,
-            "vs_fp64_gpu": {"solves_per_s": solves64, "ratio": stats["solves_per_s"] / solves64,
-                            "what": "FP64 single-mesh path, one solve at a time: per-iteration "
-                                    "time measured on a ladder of grid sizes (CUDA events), "
-                                    "interpolated per request, times the iterations the request "
-                                    "took", "ladder_s_per_iteration": ladder},
-            "accuracy_vs_fp64": acc,
-            "vs_baseline": None}
-    print(json.dumps(line), flush=True)
-
-
-def fp64_accuracy(reqs, res, nmax=6, pmax=60000):
-    """cl/cd of served FP32 solves against the same requests solved by the
-    FP64 path (whose arithmetic equals the serial FP64 oracle's) for the
-    same number of iterations: up to nmax completed requests of at most
-    pmax vertices, spread over the sizes."""
-    import numpy as np
-
-    import fvm2d_gb300 as F
-    from fvm2d_gb300 import _lib as L
-    from fvm2d_gb300 import serve
-    from fvm2d_gb300.batch import Batch
     by_rid = {r.rid: r for r in reqs}
-    ok = sorted((r for r in res if r.status == 0 and r.npts <= pmax), key=lambda r: r.npts)
-    bad = sorted((r for r in res if r.status not in (0, L.ERR_CAPACITY) and r.npts <= pmax),
-                 key=lambda r: r.npts)[:3]
-    if not ok:
-        return None
-    pick = [ok[round(i * (len(ok) - 1) / max(nmax - 1, 1))] for i in range(min(nmax, len(ok)))]
-    pick = list({r.rid: r for r in pick}.values()) + bad
-    preps = [serve.prepare(by_rid[r.rid], F.FP64) for r in pick]
-    b = Batch(F.FP64, vertices=sum(p.np for p in preps), meshes=len(preps), viscous=True)
-    slots = []
-    for r, p in zip(pick, preps):
-        s = b.add_prepared(p)
-        b.start(s, r.niter + (1 if r.status else 0))
-        slots.append(s)
-    b.step(max(r.niter for r in pick) + 1)
-    rows, failed = [], []
-    for r, s in zip(pick, slots):
-        q = b.poll(s)
-        if r.status:
-            failed.append({"rid": r.rid, "vertices": r.npts, "status32": r.status,
-                           "iteration32": r.niter, "status64": q["status"],
-                           "iteration64": q["niter"]})
-            continue
-        k = min(serve.Result.TAIL, r.niter)
-        h = b.history(s, r.niter - k, k)
-        rows.append({"rid": r.rid, "vertices": r.npts, "laminar": r.laminar, "iterations": r.niter,
-                     "cl32": r.cl, "cl64": q["cl"], "cd32": r.cd, "cd64": q["cd"],
-                     "cl32_tail": r.cl_tail, "cl64_tail": float(np.mean(h["cl"])),
-                     "cd32_tail": r.cd_tail, "cd64_tail": float(np.mean(h["cd"]))})
-    b.close()
-    return {"solves": rows,
-            "max_abs_cl": max(abs(x["cl32"] - x["cl64"]) for x in rows),
-            "max_abs_cd": max(abs(x["cd32"] - x["cd64"]) for x in rows),
-            "max_abs_cl_tail_mean": max(abs(x["cl32_tail"] - x["cl64_tail"]) for x in rows),
-            "max_abs_cd_tail_mean": max(abs(x["cd32_tail"] - x["cd64_tail"]) for x in rows),
-            "tail": serve.Result.TAIL, "target": {"cl": 1e-4, "cd": 2e-5},
-            "failed_requests_in_fp64": failed}
+    done = sorted((r for r in res if r.status == 0), key=lambda r: r.npts)
+    k = min(args.fp64_sample, len(done))
+    # stratified by grid size: the completed requests at the quantiles (2i+1)/2k
+    sample = [done[int((2 * i + 1) * len(done) / (2 * k))] for i in range(k)]
+    strict = fp64_solves([by_rid[r.rid] for r in sample], args.max_iter, args.minres)
+    fma = fp64_solves_subprocess([r.rid for r in sample], args, "fp64fma")
+    solves_s = stats["solves_per_s"]
+    out = {"metric": "converged solves/s", "value": solves_s, "unit": "converged solves/s",
+           "workload": f"{args.requests} NACA 4-digit requests, Poisson {args.rate}/s, "
+                       "5k-400k vertices log-uniform, 70% Euler / 30% laminar NS, stop at drop "
+                       f"{args.minres} or {args.max_iter} iterations, FP32 state",
+           "latency_s": {"p50": stats["p50_latency_s"], "p99": stats["p99_latency_s"]},
+           "solves": {"requests": stats["requests"], "reached_drop": stats["reached_minres"],
+                      "hit_iteration_cap": stats["iteration_cap"],
+                      "failed": len(stats["failures"]), "failures": stats["failures"]},
+           "makespan_s": stats["makespan_s"],
+           "vertex_stage_updates_per_s": stats["vertex_stage_updates_per_s"],
+           "service_thread_s": stats.get("service_thread"),
+           "arena_vertices": args.arena_vertices, "chunk": args.chunk,
+           "tune_every_steps": args.tune_every}
+    vs = {}
+    for name, runs in (("fp64_strict", strict), ("fp64_fma", fma)):
+        t = sum(x["seconds"] for x in runs)
+        sps = len(runs) / t if t > 0 else None
+        vs[name] = {"solves_per_s": sps, "ratio": solves_s / sps if sps else None,
+                    "sample_seconds": [round(x["seconds"], 3) for x in runs],
+                    "sample_iterations": [x["iterations"] for x in runs],
+                    "sample_status": [x["status"] for x in runs]}
+    vs["what"] = ("plain FP64 single-mesh path (fvm_gpu_create + fvm_gpu_iterate to the "
+                  "request's own stop), one solve at a time, wall clock, on the served requests "
+                  f"at the size quantiles (2i+1)/{2 * k}; solves/s = sample size / total seconds; "
+                  "fp64_strict: no FMA contraction (bitwise the reference's arithmetic), "
+                  "fp64_fma: the same kernels with FMA contraction")
+    vs["sample"] = [{"rid": r.rid, "vertices": r.npts, "laminar": r.laminar} for r in sample]
+    out["vs_fp64_gpu"] = vs
+    rows = []
+    for r, x in zip(sample, strict):
+        dcl = abs(r.cl_tail - x["cl_tail"])
+        dcd = abs(r.cd_tail - x["cd_tail"])
+        rows.append({"rid": r.rid, "vertices": r.npts, "laminar": r.laminar,
+                     "iterations32": r.niter, "iterations64": x["iterations"],
+                     "status64": x["status"], "abs_dcl_tail": dcl, "abs_dcd_tail": dcd,
+                     "within_target": bool(dcl <= 1e-4 and dcd <= 2e-5)})
+    out["accuracy_vs_fp64"] = {
+        "what": f"mean cl, cd over the last {serve.Result.TAIL} iterations, served FP32 vs "
+                "the same request's FP64 strict solve", "target": {"cl": 1e-4, "cd": 2e-5},
+        "solves": rows, "within_target": sum(x["within_target"] for x in rows)}
+    return out
+
+
+def run_serve(args):
+    """--mode serve: the serving measurement alone, as one JSON line."""
+    import torch
+    torch.cuda.init()
+    out = serving(args)
+    out.update({"mode": "serve", "higher_is_better": True, "n_gpus": 1, "dtype": "f32",
+                "data": "synthetic", "vs_baseline": None})
+    print(json.dumps(out), flush=True)
 
 
 ACCURACY_CASES = [
@@ -760,9 +780,10 @@ def main():
     ap.add_argument("--quick", action="store_true", help="skip the side measurements")
     ap.add_argument("--form", default=None,
                     choices=["bulk", "loads", "vertex", "fused", "split+overlap", "fused+overlap",
-                             "split+overlap4", "split+overlap8"],
+                             "split+overlap4", "split+overlap8", "pipe", "pipe+overlap",
+                             "pipe+overlap4"],
                     help="use this form of the iteration instead of the autotuner's choice")
-    ap.add_argument("--mode", choices=["throughput", "serve", "accuracy", "probe"],
+    ap.add_argument("--mode", choices=["throughput", "serve", "accuracy", "probe", "fp64-solves"],
                     default="throughput")
     ap.add_argument("--flow", choices=sorted(PROBE_FLOWS), default="euler",
                     help="probe: flow type of the batch")
@@ -782,6 +803,9 @@ def main():
                     help="serving loop: serve.Server (Python) or the C++ fvm_serve_* service")
     ap.add_argument("--tune-every", type=int, default=40,
                     help="serving: re-run the autotuner every N steps (0: never)")
+    ap.add_argument("--fp64-sample", type=int, default=4,
+                    help="serving: requests re-solved on the plain FP64 path")
+    ap.add_argument("--rids", default="", help="fp64-solves: request ids")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -795,6 +819,10 @@ def main():
         from fvm2d_gb300 import build
         build.build()
         run_accuracy(args)
+    elif args.mode == "fp64-solves":
+        from fvm2d_gb300 import build
+        build.build()
+        run_fp64_solves(args)
     elif args.mode == "probe":
         from fvm2d_gb300 import build
         build.build()

@@ -8,7 +8,15 @@ from __future__ import annotations
 import ctypes as C
 import os
 
-from .build import LIB
+from .build import LIB as _LIB_MAIN
+from .build import LIB_FP64FMA as _LIB_FP64FMA
+
+# FVM_LIB_VARIANT=fp64fma loads the library whose FP64 kernels contract
+# multiply-adds (for FP64 speed baselines); otherwise the main library
+_VARIANT = os.environ.get("FVM_LIB_VARIANT", "")
+if _VARIANT not in ("", "fp64fma"):
+    raise RuntimeError(f"FVM_LIB_VARIANT={_VARIANT!r}: expected '' or 'fp64fma'")
+LIB = _LIB_FP64FMA if _VARIANT == "fp64fma" else _LIB_MAIN
 
 # codes (include/fvm_gpu.h, after src/param.h:97-142)
 INVISCID, LAMINAR, TURBULENT = 1, 2, 3
@@ -20,6 +28,7 @@ FP64, FP32 = 0, 1
 OK = 0
 ERR_ARG, ERR_CUDA, ERR_NONPOSITIVE, ERR_ROE_SONIC, ERR_ZERO_FIRST_RES = 1, 2, 3, 4, 5
 ERR_TIMEOUT, ERR_NOMEM, ERR_STATE, ERR_GEOMETRY, ERR_CAPACITY = 6, 7, 8, 9, 10
+CHECKPOINTED = 11
 
 _PARAM_DOUBLES = [
     "gamma", "gamma1", "gas_const", "pi", "prandtl", "prandtl_turb",
@@ -67,7 +76,7 @@ class FvmBatchCaps(C.Structure):
                 ("grid", C.c_int32), ("max_tri2", C.c_int32), ("max_loc", C.c_int32),
                 ("fused", C.c_int32), ("halo_entries", C.c_int64),
                 ("halo_incidence", C.c_int64), ("grad_mode", C.c_int32),
-                ("overlap", C.c_int32)]
+                ("overlap", C.c_int32), ("pipe_groups", C.c_int32), ("pipe_stages", C.c_int32)]
 
 
 # every function the header declares, with its signature
@@ -118,6 +127,7 @@ SIGNATURES = {
     "fvm_batch_timing_read": (C.c_int32, [C.c_void_p, C.c_int32, C.c_char_p, _pd,
                                           C.POINTER(C.c_int64), _pi]),
     "fvm_batch_launch_count": (C.c_int64, [C.c_void_p]),
+    "fvm_batch_test_wait_timeout": (C.c_int32, [C.c_void_p, C.c_int64]),
     "fvm_batch_tune": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, _pd, _pi]),
     "fvm_batch_set_form": (C.c_int32, [C.c_void_p, C.c_int32]),
     "fvm_abi_sizes": (None, [C.POINTER(C.c_int64)]),
@@ -130,6 +140,11 @@ SIGNATURES = {
     "fvm_serve_result": (C.c_int32, [C.c_void_p, C.c_int64, _pi, _pi, _pd, _pd, _pd, _pd, _pd]),
     "fvm_serve_state": (C.c_int32, [C.c_void_p, C.c_int64, _pd, _pd]),
     "fvm_serve_release": (C.c_int32, [C.c_void_p, C.c_int64]),
+    "fvm_serve_checkpoint": (C.c_int32, [C.c_void_p, C.c_int64]),
+    "fvm_serve_checkpoint_read": (C.c_int32, [C.c_void_p, C.c_int64, _pd, _pd, _pd, _pd, _pi]),
+    "fvm_serve_resume": (C.c_int32, [C.c_void_p, C.POINTER(FvmParams), C.POINTER(FvmMesh),
+                                     C.c_int32, C.c_double, _pd, _pd, _pd, _pd, C.c_int32,
+                                     C.c_int32, C.POINTER(C.c_int64)]),
     "fvm_serve_stats": (C.c_int32, [C.c_void_p, C.POINTER(C.c_int64)]),
     "fvm_serve_times": (C.c_int32, [C.c_void_p, C.POINTER(C.c_double)]),
     "fvm_serve_destroy": (C.c_int32, [C.c_void_p]),

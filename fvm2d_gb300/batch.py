@@ -67,15 +67,17 @@ class Batch:
         self.h = h
         self.precision = precision
         self._meshes = {}
-        gm = int(caps.get("grad_mode", 0)) or (3 if precision == L.FP32 else 1)
+        gm = int(caps.get("grad_mode", 0)) or (4 if precision == L.FP32 else 1)
         ch = int(caps.get("overlap", 0))
         if int(caps.get("fused", 0)) > 0:
             self.form = "fused+overlap" if ch > 1 else "fused"
+        elif ch > 1 and gm == 4:
+            self.form = {2: "pipe+overlap", 4: "pipe+overlap4"}.get(ch, "pipe+overlap")
         elif ch > 1:
             self.form = {2: "split+overlap", 4: "split+overlap4", 8: "split+overlap8"}.get(
                 ch, "split+overlap")
         else:
-            self.form = {3: "bulk", 1: "loads", 2: "vertex"}[gm]
+            self.form = {4: "pipe", 3: "bulk", 1: "loads", 2: "vertex"}[gm]
 
     def close(self):
         if getattr(self, "h", None) is not None and self.h.value:
@@ -204,7 +206,8 @@ class Batch:
         return int(L.lib().fvm_batch_launch_count(self.h))
 
     TUNE_CANDIDATES = ("bulk", "loads", "vertex", "fused", "split+overlap", "fused+overlap",
-                       "split+overlap4", "split+overlap8")
+                       "split+overlap4", "split+overlap8", "pipe", "pipe+overlap",
+                       "pipe+overlap4")
 
     def set_form(self, name: str):
         """Set the form of the iteration to one of TUNE_CANDIDATES."""

@@ -10,6 +10,12 @@ Every translation unit is compiled in parallel:
   * host C++ with ``-ffp-contract=off`` (the driver-side geometry must equal
     the serial FP64 arithmetic on x86 and on Arm alike).
 No CPU fallback is built: without this library the package refuses to run.
+
+A second library, ``libfvm2d_gb300_fp64fma.so``, differs only in its FP64
+kernels, compiled with FMA contraction: the FP64 method rounded as the
+compiler pleases, not bitwise the reference, and faster on this GPU's FP64
+pipe.  It is the fair FP64 baseline for speed comparisons; the package
+loads it instead of the main library when FVM_LIB_VARIANT=fp64fma.
 """
 from __future__ import annotations
 
@@ -29,6 +35,7 @@ INC = os.path.join(os.path.dirname(HERE), "include")
 TAG = os.environ.get("FVM_BUILD_TAG", "")
 OUT = os.path.join(HERE, "_build", platform.machine() + (("-" + TAG) if TAG else ""))
 LIB = os.path.join(OUT, "libfvm2d_gb300.so")
+LIB_FP64FMA = os.path.join(OUT, "libfvm2d_gb300_fp64fma.so")
 
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
@@ -41,6 +48,7 @@ CXX_COMMON = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wext
 
 UNITS = [
     ("fvm_kernels_fp64.cu", "nvcc", ["--fmad=false"]),
+    ("fvm_kernels_fp64.cu@fma", "nvcc", ["--fmad=true"]),   # the FMA library only
     ("fvm_kernels_fp32.cu", "nvcc", os.environ.get(
         "FVM_FP32_FLAGS", "-prec-div=false -prec-sqrt=false -ftz=true").split()),
     ("fvm_setup.cu", "nvcc", ["--fmad=false"]),
@@ -63,12 +71,20 @@ def _headers_digest() -> str:
 
 
 def _compile(unit, kind, extra, digest, verbose):
-    src = os.path.join(SRC, unit)
-    obj = os.path.join(OUT, unit + ".o")
+    src = os.path.join(SRC, unit.split("@")[0])
+    obj = os.path.join(OUT, unit.replace("@", "_") + ".o")
     stamp = obj + ".stamp"
     with open(src, "rb") as f:
         key = hashlib.sha256(f.read() + digest.encode() + " ".join(extra).encode()).hexdigest()
     if os.path.exists(obj) and os.path.exists(stamp) and open(stamp).read() == key:
+        return obj, ""
+    # an alternative build reuses the main build's object of an unchanged unit
+    base = os.path.join(os.path.dirname(OUT), platform.machine())
+    bobj = os.path.join(base, os.path.basename(obj))
+    if TAG and os.path.exists(bobj + ".stamp") and open(bobj + ".stamp").read() == key:
+        shutil.copyfile(bobj, obj)
+        with open(stamp, "w") as f:
+            f.write(key)
         return obj, ""
     if kind == "nvcc":
         cmd = [NVCC] + NVCC_COMMON + extra + ["-c", src, "-o", obj]
@@ -97,20 +113,25 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
         units.append((unit, kind, e))
     with cf.ThreadPoolExecutor(max_workers=len(units)) as ex:
         futs = [ex.submit(_compile, u, k, e, digest, verbose or ptxas_info) for u, k, e in units]
-        objs = []
-        for f in futs:
+        objs = {}
+        for (u, _, _), f in zip(units, futs):
             obj, log = f.result()
-            objs.append(obj)
+            objs[u] = obj
             if log:
                 sys.stderr.write(log)
-    newest = max(os.path.getmtime(o) for o in objs)
-    if not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
-        tmp = LIB + ".tmp"
-        cmd = [NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread"]
+    main = [o for u, o in objs.items() if u != "fvm_kernels_fp64.cu@fma"]
+    fma = [objs["fvm_kernels_fp64.cu@fma"] if u == "fvm_kernels_fp64.cu" else o
+           for u, o in objs.items() if u != "fvm_kernels_fp64.cu@fma"]
+    for lib, group in ((LIB, main), (LIB_FP64FMA, fma)):
+        newest = max(os.path.getmtime(o) for o in group)
+        if os.path.exists(lib) and os.path.getmtime(lib) >= newest:
+            continue
+        tmp = lib + ".tmp"
+        cmd = [NVCC] + ARCH + ["-shared", "-o", tmp] + group + ["-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
-        shutil.move(tmp, LIB)
+        shutil.move(tmp, lib)
     return LIB
 
 

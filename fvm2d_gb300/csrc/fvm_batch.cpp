@@ -118,6 +118,7 @@ struct fvm_batch {
   int2 *ve_rng = nullptr, *vt_rng = nullptr, *va_rng = nullptr;
   uint16_t *ve_list = nullptr, *vt_list = nullptr;
   int *va_list = nullptr;
+  float2 *va_w = nullptr;   // FP32: Green-Gauss stencil weights per va_list entry
   BlockInfo *blocks = nullptr;
   int2 *be_nodes = nullptr, *sw_nodes = nullptr;
   double2 *be_ds = nullptr;
@@ -158,7 +159,7 @@ struct fvm_batch {
   double *dstage = nullptr;           // device staging of driver-order state transfers
   size_t dstage_size = 0;
   // autotuner: each candidate form's last measured ms per iteration, calls
-  double tune_last[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  double tune_last[16] = {};
   int tune_calls = 0;
   std::string last_error;
 };
@@ -234,6 +235,7 @@ ArenaPtrs<R> ptrs(const fvm_batch *b) {
   A.sw_nodes = b->sw_nodes;
   A.va_rng = b->va_rng;
   A.va_list = b->va_list;
+  A.va_w = b->va_w;
   A.mc = b->mc;
   A.ctl = b->ctl;
   A.part = b->part;
@@ -415,10 +417,11 @@ int32_t update_work(fvm_batch *b) {
   // capacities: smaller tiles let more CTAs share an SM.
   int tile[4] = {0, 0, 0, 0};
   int max_halo = 0;
-  bool any_visc = false, any_turb = false, tri_loc = true;
+  bool any_visc = false, any_turb = false, any_inv = false, tri_loc = true;
   for (const Slot &s : b->slots)
     if (s.used && !s.staged) {
       any_visc |= s.par.iflow != FVM_INVISCID;
+      any_inv |= s.par.iflow == FVM_INVISCID;
       any_turb |= s.par.iflow == FVM_TURBULENT;
       tile[0] = std::max(tile[0], s.L.max_tri);
       tile[1] = std::max(tile[1], s.L.max_slots);
@@ -447,8 +450,9 @@ int32_t update_work(fvm_batch *b) {
   // kernels for viscous terms and the SA model only while such meshes are
   // resident (the shared memory of viscous terms likewise)
   const bool visc_now = b->caps.viscous != 0 && any_visc;
-  changed |= visc_now != b->cfg.viscous || any_turb != b->run_sa;
+  changed |= visc_now != b->cfg.viscous || any_turb != b->run_sa || any_inv != b->cfg.any_inviscid;
   b->cfg.viscous = visc_now;
+  b->cfg.any_inviscid = any_inv;
   b->run_sa = any_turb;
   // the fused pass needs every resident block's halo within its tiles
   b->fused_fits = tile[2] <= cap[2] && tile[3] <= cap[3];
@@ -753,7 +757,7 @@ extern "C" int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *cap
   TRYB(dalloc(O, &b->mesh_part, (size_t)c.meshes));
   TRYB(dalloc(O, &b->be_nodes, (size_t)c.edge_entries));
   TRYB(dalloc(O, &b->be_loc, (size_t)c.edge_entries));
-  TRYB(dalloc(O, &b->halo_ids, (size_t)b->cap[P_HALO]));
+  TRYB(dalloc(O, &b->halo_ids, (size_t)b->cap[P_HALO] + 4));   // slack: 16-byte copies
   TRYB(dalloc(O, &b->hl_ptr, (size_t)b->cap[P_HP]));
   TRYB(dalloc(O, &b->hl_list, (size_t)b->cap[P_HL]));
   TRYB(dalloc(O, &b->be_ds, (size_t)c.edge_entries));
@@ -763,6 +767,7 @@ extern "C" int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *cap
   TRYB(dalloc(O, &b->elarea, (size_t)c.triangles));
   if (precision == FVM_PREC_FP32) {
     TRYB(dalloc(O, &b->be_g32, (size_t)c.edge_entries));
+    TRYB(dalloc(O, &b->va_w, (size_t)c.all_incidence));
     TRYB(dalloc(O, &b->ais32, V));
     TRYB(dalloc(O, &b->cvarea32, V));
     TRYB(dalloc(O, &b->drmin32, V));
@@ -790,15 +795,25 @@ extern "C" int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *cap
   b->cfg.max_loc = c.max_loc;
   b->cfg.max_halo = 0;
   b->cfg.tri_loc = true;
+  // the fused pass computes triangle-form gradients: FP64 only (FP32
+  // inviscid meshes take the vertex-stencil gradient)
+  if (c.fused > 0 && precision != FVM_PREC_FP64) return fail(FVM_ERR_ARG);
   b->fused = b->fused_wanted = c.fused > 0;
+  b->cfg.stencil = precision == FVM_PREC_FP32;
+  b->cfg.any_inviscid = false;
   b->chains = std::min(std::max(c.overlap, 1), kMaxChains);
-  // gradient pass: bulk-copy staging by default in FP32 (when its shared
-  // memory fits), per-thread loads in FP64
+  // gradient pass: in FP32 the pipelined form by default (launched as the
+  // bulk-copy form while the resident meshes' tiles leave no room for a
+  // stage ring), per-thread loads in FP64
   const bool bulk_fits = grad_bulk_layout(c.max_tri, kTriLocMax, c.viscous != 0).total <= kMaxSmem;
+  if (c.pipe_groups < 0 || c.pipe_groups > 2 || c.pipe_stages < 0 || c.pipe_stages > kPipeMaxStages)
+    return fail(FVM_ERR_ARG);
+  b->cfg.pipe_groups = c.pipe_groups == 1 ? 1 : 2;
+  b->cfg.pipe_stages = c.pipe_stages;
   b->cfg.grad_mode = c.grad_mode > 0 ? c.grad_mode
-                                      : (precision == FVM_PREC_FP32 && bulk_fits ? 3 : 1);
-  if (b->cfg.grad_mode < 1 || b->cfg.grad_mode > 3 ||
-      (b->cfg.grad_mode == 3 && (precision != FVM_PREC_FP32 || !bulk_fits)))
+                                      : (precision == FVM_PREC_FP32 && bulk_fits ? 4 : 1);
+  if (b->cfg.grad_mode < 1 || b->cfg.grad_mode > 4 ||
+      (b->cfg.grad_mode >= 3 && (precision != FVM_PREC_FP32 || !bulk_fits)))
     return fail(FVM_ERR_ARG);
   b->cfg.viscous = c.viscous != 0;
   b->cfg.stream = b->stream;
@@ -845,6 +860,7 @@ struct fvm_prepared {
   std::vector<int> orig;
   std::vector<double2> be_ds;
   std::vector<EdgeGeo32> be_g32;   // FP32 batches (mesh-local vertex ids)
+  std::vector<float2> va_w;        // FP32 batches: Green-Gauss weights per va_list entry
   std::vector<TriGeo32> tri_g32;   // FP32 batches
 };
 
@@ -904,6 +920,56 @@ extern "C" int32_t fvm_batch_prepare(const fvm_params *par, const fvm_mesh *m, f
     g.loc = L.be_loc[k];
     P->be_g32[k] = g;
   }
+  // Green-Gauss as a vertex stencil (FP32 batches).  green_gauss.f:23-39
+  // sums, for each triangle t around v, (1/6 mcarea_v) * sum_j prim_j *
+  // (dbxx_j, dbyy_j)(t) over t's three vertices j.  The three coefficients
+  // of a triangle sum to zero, so the same sum is
+  //   sum over v's neighbours u of W(v,u) * (prim_u - prim_v),
+  //   W(v,u) = (1/6 mcarea_v) * sum over the triangles t holding v and u of
+  //            (dbxx, dbyy) at u's position in t,
+  // which a uniform state maps to zero exactly.  W is formed in FP64 and
+  // rounded once, one entry per va_list entry of v (its edges, in edge
+  // order).
+  if (par->precision == FVM_PREC_FP32) {
+    P->va_w.assign(L.va_list.size(), make_float2(0.f, 0.f));
+    std::vector<double> wx(L.va_list.size(), 0.0), wy(L.va_list.size(), 0.0);
+    auto slot = [&](int v, int u) -> int {
+      for (int j = L.va_ptr[v]; j < L.va_ptr[v + 1]; j++)
+        if ((L.va_list[j] & 0x7fffffff) == u) return j;
+      return -1;
+    };
+    bool ok = true;
+    for (int t = 0; t < L.nt && ok; t++) {
+      int a[3];
+      double x[3], y[3];
+      for (int i = 0; i < 3; i++) {
+        const int o = m->elem[3 * t + i] - 1;
+        a[i] = L.iperm[o];
+        x[i] = m->coord[2 * o];
+        y[i] = m->coord[2 * o + 1];
+      }
+      const double bx[3] = {y[1] - y[2], y[2] - y[0], y[0] - y[1]};
+      const double by[3] = {x[2] - x[1], x[0] - x[2], x[1] - x[0]};
+      for (int i = 0; i < 3 && ok; i++)
+        for (int jj = 0; jj < 3; jj++) {
+          if (jj == i) continue;
+          const int k = slot(a[i], a[jj]);
+          if (k < 0) {
+            ok = false;
+            break;
+          }
+          wx[k] += bx[jj];
+          wy[k] += by[jj];
+        }
+    }
+    if (!ok) {
+      delete P;
+      return FVM_ERR_GEOMETRY;   // a triangle side that is not an edge
+    }
+    for (int v = 0; v < np; v++)
+      for (int j = L.va_ptr[v]; j < L.va_ptr[v + 1]; j++)
+        P->va_w[j] = make_float2((float)(P->ais[v] * wx[j]), (float)(P->ais[v] * wy[j]));
+  }
   P->tri_g32.resize(L.bt_nodes.size());
   for (size_t k = 0; k < L.bt_nodes.size(); k++) {
     const int t = L.bt_nodes[k].w;   // driver triangle of this block entry
@@ -940,7 +1006,7 @@ extern "C" int64_t fvm_prepared_bytes(const fvm_prepared *prep, int32_t precisio
   bytes += (int64_t)L.be_nodes.size() * (8 + 16 + 32);
   bytes += (int64_t)L.bb_nodes.size() * 16 + (int64_t)L.bt_nodes.size() * (16 + (r == 4 ? 32 : 0));
   bytes += (int64_t)L.nt * 8 + (int64_t)L.ve_list.size() * 2 + (int64_t)L.vt_list.size() * 2;
-  bytes += (int64_t)L.va_list.size() * 4 + (int64_t)L.sw_nodes.size() * 8;
+  bytes += (int64_t)L.va_list.size() * (4 + (r == 4 ? 8 : 0)) + (int64_t)L.sw_nodes.size() * 8;
   bytes += (int64_t)L.nblk * (sizeof(BlockInfo) + sizeof(BlockPartial) + 4);
   bytes += (int64_t)L.be_loc.size() * 4 + (int64_t)L.halo_ids.size() * 4;
   bytes += (int64_t)L.hl_ptr.size() * 4 + (int64_t)L.hl_list.size() * 2;
@@ -1110,6 +1176,7 @@ static int32_t add_prepared(fvm_batch *b, fvm_prepared *prep, int32_t *slot_out,
     PUT(put_range(b, b->be_g32, S.off[P_BE], g, us));
   }
   if (b->tri_g32) PUT(put_range(b, b->tri_g32, S.off[P_BT], prep->tri_g32, us));
+  if (b->va_w) PUT(put_range(b, b->va_w, S.off[P_VA], prep->va_w, us));
   PUT(put_range(b, b->sw_nodes, S.off[P_SW], sw, us));
   PUT(cudaMemcpyAsync(b->mc + sid, &mc, sizeof(mc), cudaMemcpyHostToDevice, us));
   PUT(cudaMemcpyAsync(b->ctl + sid, &ctl, sizeof(ctl), cudaMemcpyHostToDevice, us));
@@ -1309,22 +1376,25 @@ struct Form {
   int grad;
   int chains;
 };
-constexpr int kForms = 8;
+constexpr int kForms = 11;
 
 static Form form_of(const fvm_batch *b, int i) {
   const bool bulk = b->prec == FVM_PREC_FP32 &&
                     grad_bulk_layout(b->caps.max_tri, kTriLocMax, b->caps.viscous != 0).total <= kMaxSmem;
   const int g = bulk ? 3 : 1;
+  const int gp = 4;   // the pipelined forms exist in FP32 only
   const Form f[kForms] = {{false, 3, 1}, {false, 1, 1}, {false, 2, 1}, {true, 1, 1},
-                          {false, g, 2}, {true, 1, 2},  {false, g, 4}, {false, g, 8}};
+                          {false, g, 2}, {true, 1, 2},  {false, g, 4}, {false, g, 8},
+                          {false, gp, 1}, {false, gp, 2}, {false, gp, 4}};
   return f[i];
 }
 
 static bool form_fits(const fvm_batch *b, const Form &f) {
   const bool fp32 = b->prec == FVM_PREC_FP32;
-  if (f.grad == 3 && !(fp32 && grad_bulk_layout(b->caps.max_tri, kTriLocMax, b->caps.viscous != 0).total <= kMaxSmem))
+  if (f.grad >= 3 && !(fp32 && grad_bulk_layout(b->caps.max_tri, kTriLocMax, b->caps.viscous != 0).total <= kMaxSmem))
     return false;
   if (f.fused) {
+    if (fp32) return false;   // FP64 only (the FP32 stencil gradient)
     const size_t sm = fp32 ? smem_step(b->cfg, (float *)nullptr) : smem_step(b->cfg, (double *)nullptr);
     if (sm > kMaxSmem || !b->fused_fits) return false;
   }
@@ -1374,7 +1444,7 @@ extern "C" int32_t fvm_batch_tune(fvm_batch *b, int32_t iters, int32_t max, doub
   // every fourth call times every candidate; in between, a candidate more
   // than kTuneSkip times slower than the best of its last timing is not
   // re-timed (its last time is reported)
-  static_assert(kForms <= 8, "tune_last holds 8 forms");
+  static_assert(kForms <= 16, "tune_last holds 16 forms");
   constexpr double kTuneSkip = 1.25;
   double prev_best = 0.0;
   for (int i = 0; i < kForms; i++)
@@ -1527,6 +1597,21 @@ extern "C" int32_t fvm_batch_timing_read(fvm_batch *b, int32_t max, char *names,
 
 extern "C" int64_t fvm_batch_launch_count(fvm_batch *b) { return b ? b->launches : -1; }
 
+extern "C" int32_t fvm_batch_test_wait_timeout(fvm_batch *b, int64_t budget_cycles) {
+  if (b && b->pending) {   // deferred admissions first
+    const int32_t cst = batch_commit(b);
+    if (cst) return cst;
+  }
+  if (!b || budget_cycles <= 0 || b->prec != FVM_PREC_FP32) return FVM_ERR_ARG;
+  // one stage-1 gradient pass over every resident mesh (routine mode), each
+  // CTA's first block armed but never copied
+  const cudaError_t e = launch_grad_pipe(ptrs<float>(b), b->cfg, 1, 0, 1, budget_cycles, 1, 0);
+  if (e == cudaErrorNotSupported) return FVM_ERR_STATE;
+  FVM_TRY(b, e);
+  FVM_TRY(b, cudaStreamSynchronize(b->stream));
+  return FVM_OK;
+}
+
 extern "C" int32_t fvm_layout_stats(const fvm_mesh *m, int64_t *out) {
   if (!m || !out) return FVM_ERR_ARG;
   MeshLayout L;
@@ -1593,6 +1678,7 @@ extern "C" const char *fvm_gpu_strerror(int32_t s) {
     case FVM_ERR_STATE: return "call out of order";
     case FVM_ERR_GEOMETRY: return "degenerate or inconsistent geometry";
     case FVM_ERR_CAPACITY: return "capacity exceeded";
+    case FVM_CHECKPOINTED: return "stopped at a checkpoint";
     default: return "unknown status";
   }
 }

@@ -92,6 +92,35 @@ FVM_HD inline GradBulkLayout grad_bulk_layout(int max_tri, int max_halo, bool vi
   return l;
 }
 
+// One stage of the pipelined gradient pass (FP32): everything a consumer
+// group needs for one block, filled by the producer warp's bulk copies
+// (triangle records, incidence ranges and list, own states, halo ids, the
+// own vertices' (1/6)/mcarea and drmin) plus the halo states the consumers
+// gather themselves.  Stages are 128-byte aligned.
+struct GradPipeLayout {
+  uint32_t geo, vis, vtr, vtl, pv, hst, hid, ais, drm, stage;
+};
+FVM_HD inline GradPipeLayout grad_pipe_layout(int max_tri, int max_halo, bool viscous) {
+  GradPipeLayout l;
+  const uint32_t mt = (uint32_t)max_tri, mh = (uint32_t)max_halo;
+  const uint32_t nvr = (uint32_t)(kBlockVerts + kVertAlign);
+  l.geo = 0;
+  l.vis = fvm_up16(mt * 32u);
+  l.vtr = l.vis + (viscous ? fvm_up16(mt * 36u) : 0u);
+  l.vtl = l.vtr + fvm_up16(nvr * 8u);
+  l.pv = l.vtl + fvm_up16((3u * mt + 16u) * 2u);
+  l.hst = l.pv + (uint32_t)kBlockVerts * 16u;
+  l.hid = l.hst + fvm_up16(mh * 16u);
+  l.ais = l.hid + fvm_up16((mh + 8u) * 4u);   // copied from a 16-byte boundary
+  l.drm = l.ais + fvm_up16(nvr * 4u);
+  l.stage = (l.drm + fvm_up16(nvr * 4u) + 127u) & ~127u;
+  return l;
+}
+constexpr int kPipeMaxStages = 8;
+// Shared memory of a pipelined kernel's CTA besides its stages (barriers,
+// stage headers, flags)
+constexpr uint32_t kPipeStaticSmem = 2048;
+
 // Per-mesh constants (read-only during a solve).  Mirrors fvm_params plus
 // arena placement.
 // FP32 copies of a mesh's constants (each the FP64 value rounded once, as a
@@ -232,6 +261,7 @@ struct ArenaPtrs {
   // all-edge incidence (limitgrad.f loops over netot edges)
   const int2 *va_rng;
   const int *va_list;     // other vertex | (is n2) << 31
+  const float2 *va_w;     // FP32: Green-Gauss stencil weight of each va_list entry
   // per mesh
   const MeshConst *mc;
   MeshCtl *ctl;

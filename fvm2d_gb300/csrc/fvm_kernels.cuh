@@ -26,6 +26,12 @@
 #ifndef FVM_GRADV_MINB32
 #define FVM_GRADV_MINB32 4  // the same for its per-vertex form
 #endif
+#ifndef FVM_STENCIL_MINB
+#define FVM_STENCIL_MINB 1  // resident CTAs per SM asked of the stencil gradient kernel
+#endif
+#ifndef FVM_STENCIL_BATCH
+#define FVM_STENCIL_BATCH 4 // edges whose loads are in flight at once per thread
+#endif
 
 namespace fvm {
 
@@ -309,10 +315,52 @@ __device__ __forceinline__ void tri_visc_term(const TriVisc<R> &tv, R dbx, R dby
   out[2] = (tv.efx * dbx + tv.efy * dby) * tv.areat;
 }
 
+// Sums of one vertex's triangle terms in the order of its incidence list
+// (green_gauss.f:23-39 visits triangles in ascending order): entries
+// [j0, j1) of `vtl`, each a triangle slot and the vertex's position in it.
+// The slots and terms of up to B triangles are loaded before they are
+// added, so the shared-memory latency is paid once per B triangles; the
+// additions stay in list order (same bits as one triangle at a time).
+// vis = nullptr: inviscid (rv is zero).
+template <typename R, int B>
+__device__ __forceinline__ void grad_vertex_sums(const uint16_t *vtl, int j0, int j1,
+                                                 const TriSmem<R> *tri, const R *vis, R qx[4],
+                                                 R qy[4], R rv[3]) {
+#pragma unroll
+  for (int q = 0; q < 4; q++) qx[q] = qy[q] = R(0);
+  rv[0] = rv[1] = rv[2] = R(0);
+  for (int j = j0; j < j1; j += B) {
+    const int n = j1 - j;
+    uint16_t e[B];
+#pragma unroll
+    for (int u = 0; u < B; u++) e[u] = u < n ? vtl[j + u] : uint16_t(0);
+    TriSmem<R> ts[B];
+#pragma unroll
+    for (int u = 0; u < B; u++)
+      if (u < n) ts[u] = tri[e[u] & 0x3fff];
+#pragma unroll
+    for (int u = 0; u < B; u++) {
+      if (u < n) {
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          qx[q] = qx[q] + ts[u].dxt[q];
+          qy[q] = qy[q] + ts[u].dyt[q];
+        }
+        if (vis) {
+          const R *sv = vis + 9 * (e[u] & 0x3fff) + 3 * (e[u] >> kTriPosShift);
+          rv[0] = rv[0] + sv[0];
+          rv[1] = rv[1] + sv[1];
+          rv[2] = rv[2] + sv[2];
+        }
+      }
+    }
+  }
+}
+
 template <typename R>
 __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRAD_MINB32 : 1)
     k_grad(ArenaPtrs<R> A, int stage, int do_dt,
-                                                      int routine, int max_tri) {
+                                                      int routine, int max_tri, int skip_inviscid) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   TriSmem<R> *s_tri = reinterpret_cast<TriSmem<R> *>(smem_raw);
   R *s_vis = reinterpret_cast<R *>(s_tri + max_tri);   // [max_tri][3 pos][3 comp]
@@ -323,6 +371,7 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRAD_MINB32 
     const MeshCtl &ctl = A.ctl[bi.mesh];
     if (!routine && !ctl.active) continue;
     const MeshConst &mc = A.mc[bi.mesh];
+    if (skip_inviscid && mc.iflow == 1) continue;   // the stencil pass's meshes
     const bool visc = mc.iflow != 1;
     const R4<R> *P = A.st[cur_buf(ctl.phase, stage)];
     if (threadIdx.x == 0) {
@@ -357,25 +406,11 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRAD_MINB32 
     // phase 2: one thread per vertex, triangles in original order
     if (threadIdx.x < bi.nv) {
       const int v = bi.v0 + threadIdx.x;
-      R qx[4] = {R(0), R(0), R(0), R(0)}, qy[4] = {R(0), R(0), R(0), R(0)};
-      R rv[3] = {R(0), R(0), R(0)};
+      R qx[4], qy[4], rv[3];
       const int2 jr = A.vt_rng[v];
-      for (int j = jr.x; j < jr.y; j++) {
-        const uint16_t e = A.vt_list[j];
-        const int slot = e & 0x3fff;
-        const TriSmem<R> ts = s_tri[slot];
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-          qx[q] = qx[q] + ts.dxt[q];
-          qy[q] = qy[q] + ts.dyt[q];
-        }
-        if (visc) {
-          const R *sv = s_vis + 9 * slot + 3 * (e >> kTriPosShift);
-          rv[0] = rv[0] + sv[0];
-          rv[1] = rv[1] + sv[1];
-          rv[2] = rv[2] + sv[2];
-        }
-      }
+      // (FP32: one triangle at a time, the 48 registers of five CTAs per SM)
+      grad_vertex_sums<R, sizeof(R) == 8 ? 2 : 1>(A.vt_list, jr.x, jr.y, s_tri,
+                                                  visc ? s_vis : nullptr, qx, qy, rv);
       const R ais = v_ais(A, v);
       Grad<R> g;
 #pragma unroll
@@ -410,7 +445,7 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRAD_MINB32 
 template <typename R>
 __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRAD_MINB32 : 1)
     k_grad_bulk(ArenaPtrs<R> A, int stage, int do_dt, int routine, int max_tri, int max_halo,
-                int viscous) {
+                int viscous, int skip_inviscid) {
   if constexpr (sizeof(R) == 4) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bar;
@@ -432,6 +467,7 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRAD_MINB32 
       const MeshCtl &ctl = A.ctl[bi.mesh];
       if (!routine && !ctl.active) continue;
       const MeshConst &mc = A.mc[bi.mesh];
+      if (skip_inviscid && mc.iflow == 1) continue;   // the stencil pass's meshes
       const bool visc = mc.iflow != 1;
       const R4<R> *P = A.st[cur_buf(ctl.phase, stage)];
       const int vt_a = bi.vt0 & ~7;                       // 16-byte units of uint16
@@ -501,25 +537,11 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRAD_MINB32 
       // phase 2: one thread per vertex, triangles in original order
       if (threadIdx.x < bi.nv) {
         const int v = bi.v0 + threadIdx.x;
-        R qx[4] = {R(0), R(0), R(0), R(0)}, qy[4] = {R(0), R(0), R(0), R(0)};
-        R rv[3] = {R(0), R(0), R(0)};
+        R qx[4], qy[4], rv[3];
         const int2 jr = s_vtr[threadIdx.x];
-        for (int j = jr.x - vt_a; j < jr.y - vt_a; j++) {
-          const uint16_t e = s_vtl[j];
-          const int slot = e & 0x3fff;
-          const TriSmem<R> ts = s_tri[slot];
-#pragma unroll
-          for (int q = 0; q < 4; q++) {
-            qx[q] = qx[q] + ts.dxt[q];
-            qy[q] = qy[q] + ts.dyt[q];
-          }
-          if (visc) {
-            const R *sv = s_vis + 9 * slot + 3 * (e >> kTriPosShift);
-            rv[0] = rv[0] + sv[0];
-            rv[1] = rv[1] + sv[1];
-            rv[2] = rv[2] + sv[2];
-          }
-        }
+        // one triangle at a time: batched loads spill at 48 registers
+        grad_vertex_sums<R, 1>(s_vtl, jr.x - vt_a, jr.y - vt_a, s_tri, visc ? s_vis : nullptr, qx,
+                               qy, rv);
         const R ais = v_ais(A, v);
         Grad<R> g;
 #pragma unroll
@@ -545,6 +567,69 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRAD_MINB32 
   }
 }
 
+// Gradient pass, vertex-stencil form (FP32, inviscid meshes): green_gauss.f
+// (2-42) as precomputed per-vertex weights over the vertex's edges,
+//   qx, qy (v) = sum over edges (v,u) of W(v,u) * (prim_u - prim_v),
+// W formed on the host in FP64 from the triangles around the edge and
+// rounded once (fvm_batch_prepare).  Equal to the triangle sums in exact
+// arithmetic; in FP32 it rounds differently (and maps a uniform state to
+// zero exactly).  One thread per vertex, no shared memory and no barrier;
+// the weights and neighbour states of FVM_STENCIL_BATCH edges are in flight
+// at once.  At stage 1 also time_step.f:22-27.
+template <typename R>
+__global__ void __launch_bounds__(kBlockVerts, FVM_STENCIL_MINB)
+    k_grad_stencil(ArenaPtrs<R> A, int stage, int do_dt, int routine) {
+  constexpr int B = FVM_STENCIL_BATCH;
+  if constexpr (sizeof(R) == 4) {
+    int w0, nwork;
+    work_range(A, w0, nwork);
+    for (int w = w0 + blockIdx.x; w < nwork; w += gridDim.x) {
+      const BlockInfo bi = A.blocks[A.work[w]];
+      const MeshCtl &ctl = A.ctl[bi.mesh];
+      if (!routine && !ctl.active) continue;
+      const MeshConst &mc = A.mc[bi.mesh];
+      if (mc.iflow != 1 || threadIdx.x >= bi.nv) continue;
+      const int v = bi.v0 + threadIdx.x;
+      const R4<R> *P = A.st[cur_buf(ctl.phase, stage)];
+      const R4<R> pv = P[v];
+      const int2 r = A.va_rng[v];
+      R qx[4] = {R(0), R(0), R(0), R(0)}, qy[4] = {R(0), R(0), R(0), R(0)};
+      for (int j = r.x; j < r.y; j += B) {
+        const int n = r.y - j;
+        int u[B];
+        float2 wt[B];
+#pragma unroll
+        for (int k = 0; k < B; k++) {
+          u[k] = k < n ? (A.va_list[j + k] & 0x7fffffff) : v;
+          wt[k] = k < n ? A.va_w[j + k] : make_float2(0.f, 0.f);
+        }
+        R4<R> pu[B];
+#pragma unroll
+        for (int k = 0; k < B; k++) pu[k] = k < n ? P[u[k]] : pv;
+#pragma unroll
+        for (int k = 0; k < B; k++) {
+          if (k < n) {
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+              const R d = comp(pu[k], q) - comp(pv, q);
+              qx[q] = fmaf(wt[k].x, d, qx[q]);
+              qy[q] = fmaf(wt[k].y, d, qy[q]);
+            }
+          }
+        }
+      }
+      Grad<R> g;
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        g.qx[q] = qx[q];
+        g.qy[q] = qy[q];
+      }
+      A.grad[v] = g;
+      if (do_dt) A.dt[v] = time_step<R>(mc, pv, R(0), v_drmin(A, v));
+    }
+  }
+}
+
 // Gradient pass, per-vertex form: each thread walks its vertex's triangles
 // (ascending, as green_gauss.f visits them) and computes each triangle's
 // terms itself, straight from the triangle entries; no shared memory and no
@@ -552,7 +637,7 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRAD_MINB32 
 // arithmetic of each term is that of k_grad, so both give the same sums.
 template <typename R>
 __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRADV_MINB32 : 1)
-    k_grad_v(ArenaPtrs<R> A, int stage, int do_dt, int routine) {
+    k_grad_v(ArenaPtrs<R> A, int stage, int do_dt, int routine, int skip_inviscid) {
   int w0, nwork;
   work_range(A, w0, nwork);
   for (int w = w0 + blockIdx.x; w < nwork; w += gridDim.x) {
@@ -560,6 +645,7 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRADV_MINB32
     const MeshCtl &ctl = A.ctl[bi.mesh];
     if (!routine && !ctl.active) continue;
     const MeshConst &mc = A.mc[bi.mesh];
+    if (skip_inviscid && mc.iflow == 1) continue;   // the stencil pass's meshes
     const bool visc = mc.iflow != 1;
     const R4<R> *P = A.st[cur_buf(ctl.phase, stage)];
     if (threadIdx.x == 0) {
@@ -1849,3 +1935,5 @@ __global__ void __launch_bounds__(kBlockVerts) k_limitgrad(ArenaPtrs<R> A) {
 }
 
 }  // namespace fvm
+
+#include "fvm_pipe.cuh"

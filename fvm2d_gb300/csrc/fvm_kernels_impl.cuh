@@ -35,23 +35,61 @@ inline int fit_grid(const LaunchCfg &c, K kern, size_t smem, int threads = kBloc
     k_visc<R><<<fit_grid(c, k_visc<R>, 0), kBlockVerts, 0, c.stream>>>(A, stage, do_dt, routine);             \
     return cudaGetLastError();                                                             \
   }                                                                                        \
+  cudaError_t launch_grad_pipe(const ArenaPtrs<R> &A, const LaunchCfg &c, int stage,       \
+                               int do_dt, int routine, long long budget, int inject,      \
+                               int skip_inviscid) {                                       \
+    if (sizeof(R) != 4 || !c.tri_loc) return cudaErrorNotSupported;                      \
+    const GradPipeLayout pl = grad_pipe_layout(c.max_tri, c.max_halo, c.viscous);         \
+    const int groups = c.pipe_groups == 1 ? 1 : 2;                                        \
+    const int ns = pipe_stage_count(pl.stage, groups, c.pipe_stages);                      \
+    if (!ns) return cudaErrorNotSupported;                                                 \
+    const size_t sb = (size_t)ns * pl.stage;                                               \
+    const int vis = c.viscous ? 1 : 0;                                                     \
+    if (groups == 1)                                                                       \
+      k_grad_pipe<R, 1><<<fit_grid(c, k_grad_pipe<R, 1>, sb, 32 + kBlockVerts),            \
+                          32 + kBlockVerts, sb, c.stream>>>(A, stage, do_dt, routine,      \
+                          c.max_tri, c.max_halo, vis, ns, budget, inject, skip_inviscid);  \
+    else                                                                                   \
+      k_grad_pipe<R, 2><<<fit_grid(c, k_grad_pipe<R, 2>, sb, 32 + 2 * kBlockVerts),        \
+                          32 + 2 * kBlockVerts, sb, c.stream>>>(A, stage, do_dt, routine,  \
+                          c.max_tri, c.max_halo, vis, ns, budget, inject, skip_inviscid);  \
+    return cudaGetLastError();                                                             \
+  }                                                                                        \
   cudaError_t launch_grad(const ArenaPtrs<R> &A, const LaunchCfg &c, int stage, int do_dt,  \
                           int routine) {                                                   \
     size_t sm = smem_grad(c, (R *)nullptr);                                                \
     if (sm > kMaxSmem) return cudaErrorInvalidConfiguration;                              \
+    /* FP32: inviscid meshes take the vertex-stencil pass, viscous ones the */             \
+    /* triangle pass below */                                                              \
+    int skip = 0;                                                                          \
+    if (sizeof(R) == 4 && c.stencil) {                                                     \
+      if (c.any_inviscid) {                                                                \
+        k_grad_stencil<R><<<fit_grid(c, k_grad_stencil<R>, 0), kBlockVerts, 0, c.stream>>>( \
+            A, stage, do_dt, routine);                                                     \
+        const cudaError_t se = cudaGetLastError();                                         \
+        if (se != cudaSuccess) return se;                                                  \
+      }                                                                                    \
+      if (!c.viscous) return cudaSuccess;                                                  \
+      skip = 1;                                                                            \
+    }                                                                                      \
+    if (c.grad_mode == 4 && sizeof(R) == 4 && c.tri_loc) {                                 \
+      const cudaError_t pe = launch_grad_pipe(A, c, stage, do_dt, routine, kPipeBudget, 0, \
+                                              skip);                                       \
+      if (pe != cudaErrorNotSupported) return pe;                                          \
+    }                                                                                      \
     if (c.grad_mode == 2) {                                                                \
-      k_grad_v<R><<<fit_grid(c, k_grad_v<R>, 0), kBlockVerts, 0, c.stream>>>(A, stage, do_dt, routine); \
+      k_grad_v<R><<<fit_grid(c, k_grad_v<R>, 0), kBlockVerts, 0, c.stream>>>(A, stage, do_dt, routine, skip); \
       return cudaGetLastError();                                                           \
     }                                                                                      \
-    if (c.grad_mode == 3 && c.tri_loc) {  /* else the per-thread form, same sums */      \
+    if (c.grad_mode >= 3 && c.tri_loc) {  /* else the per-thread form, same sums */      \
       if (sizeof(R) != 4) return cudaErrorNotSupported;                                    \
       const size_t sb = grad_bulk_layout(c.max_tri, c.max_halo, c.viscous).total;          \
       if (sb > kMaxSmem) return cudaErrorInvalidConfiguration;                            \
       k_grad_bulk<R><<<fit_grid(c, k_grad_bulk<R>, sb), kBlockVerts, sb, c.stream>>>(       \
-          A, stage, do_dt, routine, c.max_tri, c.max_halo, c.viscous ? 1 : 0);             \
+          A, stage, do_dt, routine, c.max_tri, c.max_halo, c.viscous ? 1 : 0, skip);       \
       return cudaGetLastError();                                                           \
     }                                                                                      \
-    k_grad<R><<<fit_grid(c, k_grad<R>, sm), kBlockVerts, sm, c.stream>>>(A, stage, do_dt, routine, c.max_tri);  \
+    k_grad<R><<<fit_grid(c, k_grad<R>, sm), kBlockVerts, sm, c.stream>>>(A, stage, do_dt, routine, c.max_tri, skip);  \
     return cudaGetLastError();                                                             \
   }                                                                                        \
   cudaError_t launch_flux(const ArenaPtrs<R> &A, const LaunchCfg &c, int stage, int mode,   \
@@ -151,6 +189,11 @@ inline int fit_grid(const LaunchCfg &c, K kern, size_t smem, int threads = kBloc
     const size_t gb = grad_bulk_layout(c.max_tri, kTriLocMax, c.viscous).total;            \
     if (e == cudaSuccess && sizeof(R) == 4 && gb <= kMaxSmem)                              \
       e = cudaFuncSetAttribute(k_grad_bulk<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gb); \
+    const int pmax = (int)(kMaxSmem - kPipeStaticSmem);                                    \
+    if (e == cudaSuccess && sizeof(R) == 4)                                                \
+      e = cudaFuncSetAttribute(k_grad_pipe<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, pmax); \
+    if (e == cudaSuccess && sizeof(R) == 4)                                                \
+      e = cudaFuncSetAttribute(k_grad_pipe<R, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, pmax); \
     return e;                                                                              \
   }
 

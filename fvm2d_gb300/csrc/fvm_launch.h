@@ -24,14 +24,31 @@ struct LaunchCfg {
                      // (k_grad_v), 3 bulk copies to shared memory (k_grad_bulk, FP32)
   int max_halo;      // max halo vertices of a block (k_grad_bulk's halo ids)
   bool tri_loc;      // every resident block's triangle records carry local slots
+  bool stencil;      // FP32: inviscid meshes take the vertex-stencil gradient pass
+  bool any_inviscid; // an inviscid mesh is resident
+  int pipe_groups;   // consumer groups of a pipelined kernel's CTA (1 or 2)
+  int pipe_stages;   // stages of its ring (0: as many as fit, at most kPipeMaxStages)
   cudaStream_t stream;
 };
+
+// Stages of a pipelined kernel's ring for stages of `stage_bytes`: as many as
+// fit the shared memory (at most `want` when want > 0), 0 when fewer than
+// groups + 1 fit.
+inline int pipe_stage_count(uint32_t stage_bytes, int groups, int want) {
+  int n = (int)((kMaxSmem - kPipeStaticSmem) / stage_bytes);
+  if (n > kPipeMaxStages) n = kPipeMaxStages;
+  if (want > 0 && n > want) n = want;
+  return n >= groups + 1 ? n : 0;
+}
 
 #define FVM_DECLARE_LAUNCHERS(R)                                                          \
   cudaError_t launch_visc(const ArenaPtrs<R> &A, const LaunchCfg &c, int stage, int do_dt, \
                           int routine);                                                   \
   cudaError_t launch_grad(const ArenaPtrs<R> &A, const LaunchCfg &c, int stage, int do_dt, \
                           int routine);                                                   \
+  cudaError_t launch_grad_pipe(const ArenaPtrs<R> &A, const LaunchCfg &c, int stage,       \
+                               int do_dt, int routine, long long budget, int inject,      \
+                               int skip_inviscid);                                        \
   cudaError_t launch_flux(const ArenaPtrs<R> &A, const LaunchCfg &c, int stage, int mode,  \
                           int irk, int routine);                                          \
   cudaError_t launch_sa(const ArenaPtrs<R> &A, const LaunchCfg &c, int stage, int routine);\

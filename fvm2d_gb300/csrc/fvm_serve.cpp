@@ -10,6 +10,10 @@
 //           FVM_ERR_CAPACITY);
 //   step    every resident solve `chunk` iterations (one CUDA graph launch
 //           per iteration, every mesh in each kernel);
+//   checkpoint  running solves the caller asked to stop: their state is
+//           read back and kept, the arena ranges freed (status
+//           FVM_CHECKPOINTED); fvm_serve_resume queues a solve that starts
+//           from such a state;
 //   retire  solves that reached their residual drop or iteration cap
 //           (main.f:42) or stopped with a status: results (and the final
 //           state when asked) are kept for the caller, the arena ranges
@@ -50,7 +54,16 @@ struct Ticket {
   int32_t status = FVM_OK, niter = 0;
   double fres = 0.0, cl = 0.0, cd = 0.0;
   double cl_tail = 0.0, cd_tail = 0.0;   // means over the last kTail iterations
-  std::vector<double> prim, nut;
+  std::vector<double> prim, nut;         // final or checkpointed state
+  // checkpoint: asked by the caller; the kept viscosities and the
+  // iteration count a resume starts from
+  bool ckpt_req = false;
+  std::vector<double> ck_mul, ck_mu;
+  int32_t ck_iter = 0;
+  // resume: the state the solve starts from, at iteration iterlast
+  bool resume = false;
+  int32_t iterlast = 0;
+  std::vector<double> start_prim, start_nut, start_mul, start_mu;
 };
 
 constexpr int kTail = 256;
@@ -163,7 +176,18 @@ int32_t retire(fvm_server *s) {
   return FVM_OK;
 }
 
-// Admits queued solves in arrival order while they fit.
+// Starts an admitted solve: from the freestream, or (resume) from the
+// ticket's state at its iteration iterlast.
+int32_t start_solve(fvm_server *s, const Ticket &t, int32_t slot, int32_t nmax, double minres) {
+  if (t.resume) {
+    auto ptr = [](const std::vector<double> &v) { return v.empty() ? nullptr : v.data(); };
+    const int32_t st = fvm_batch_set_state(s->b, slot, t.start_prim.data(), ptr(t.start_nut),
+                                           ptr(t.start_mul), ptr(t.start_mu), t.iterlast);
+    if (st) return st;
+  }
+  return fvm_batch_start(s->b, slot, nmax, minres);
+}
+
 // Admits queued solves while the arena has room.  Deferred (a step is
 // running): the uploads go beside it and the solves start at
 // start_admitted, after the step.
@@ -171,6 +195,7 @@ struct Admitted {
   int64_t id;
   int32_t slot, nmax;
   double minres;
+  Ticket *t;
 };
 
 int32_t admit(fvm_server *s, bool deferred, std::vector<Admitted> *staged) {
@@ -179,6 +204,7 @@ int32_t admit(fvm_server *s, bool deferred, std::vector<Admitted> *staged) {
     fvm_prepared *prep;
     int32_t nmax;
     double minres;
+    Ticket *tp;
     {
       std::lock_guard<std::mutex> lk(s->mu);
       if (s->queue.empty()) return FVM_OK;
@@ -187,6 +213,7 @@ int32_t admit(fvm_server *s, bool deferred, std::vector<Admitted> *staged) {
       prep = t.prep;
       nmax = t.nmax;
       minres = t.minres;
+      tp = &t;   // map nodes stay put; a queued or running ticket is not released
     }
     int32_t slot = -1;
     int32_t st = deferred ? fvm::batch_add_prepared_deferred(s->b, prep, &slot)
@@ -208,11 +235,11 @@ int32_t admit(fvm_server *s, bool deferred, std::vector<Admitted> *staged) {
     t.state = 1;
     t.t_admit = Clock::now();
     if (deferred) {
-      staged->push_back({id, slot, nmax, minres});
+      staged->push_back({id, slot, nmax, minres, tp});
       continue;
     }
     s->resident[slot] = id;
-    if ((st = fvm_batch_start(s->b, slot, nmax, minres))) return st;
+    if ((st = start_solve(s, *tp, slot, nmax, minres))) return st;
   }
 }
 
@@ -222,10 +249,54 @@ int32_t start_admitted(fvm_server *s, std::vector<Admitted> &staged) {
   int32_t st = fvm::batch_commit_admissions(s->b);
   for (const Admitted &a : staged) {
     s->resident[a.slot] = a.id;
-    if (!st) st = fvm_batch_start(s->b, a.slot, a.nmax, a.minres);
+    if (!st) st = start_solve(s, *a.t, a.slot, a.nmax, a.minres);
   }
   staged.clear();
   return st;
+}
+
+// Stops the running solves whose checkpoint was asked: state read back and
+// kept, arena ranges freed, ticket done with FVM_CHECKPOINTED.  A solve
+// that finished in the same step retires as usual.
+int32_t checkpoint(fvm_server *s) {
+  std::vector<std::pair<int32_t, int64_t>> want;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    for (const auto &r : s->resident)
+      if (s->tickets[r.second].ckpt_req) want.push_back(r);
+  }
+  for (const auto &r : want) {
+    int32_t active = 0, niter = 0, status = 0, bad = 0;
+    double fres = 0, cl = 0, cd = 0;
+    int32_t st = fvm_batch_poll(s->b, r.first, &active, &niter, &fres, &cl, &cd, &status, &bad);
+    if (st) return st;
+    if (!active) continue;
+    int32_t np, iterlast;
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      np = s->tickets[r.second].np;
+      iterlast = s->tickets[r.second].iterlast;
+    }
+    std::vector<double> prim(4 * (size_t)np), nut(np), mul(np), mu(np);
+    st = fvm_batch_get_state(s->b, r.first, prim.data(), nut.data(), mul.data(), mu.data(),
+                             nullptr, nullptr);
+    if (st) return st;
+    if ((st = fvm_batch_remove(s->b, r.first))) return st;
+    s->resident.erase(r.first);
+    std::lock_guard<std::mutex> lk(s->mu);
+    Ticket &t = s->tickets[r.second];
+    t.niter = niter;
+    t.fres = fres;
+    t.cl = cl;
+    t.cd = cd;
+    t.prim.swap(prim);
+    t.nut.swap(nut);
+    t.ck_mul.swap(mul);
+    t.ck_mu.swap(mu);
+    t.ck_iter = iterlast + niter;
+    finish(s, r.second, t, FVM_CHECKPOINTED);
+  }
+  return FVM_OK;
 }
 
 void service(fvm_server *s) {
@@ -291,8 +362,9 @@ void service(fvm_server *s) {
     d_admit += sec(t3, t4);
     if (!st) {
       d_steps = 1;
-      st = retire(s);
+      st = checkpoint(s);
     }
+    if (!st) st = retire(s);
     d_retire += sec(t4, Clock::now());
     publish();
     if (st) break;
@@ -334,12 +406,25 @@ extern "C" int32_t fvm_serve_create(int32_t precision, const fvm_batch_caps *cap
   return FVM_OK;
 }
 
-extern "C" int32_t fvm_serve_submit(fvm_server *s, const fvm_params *p, const fvm_mesh *m,
-                                    int32_t nmax, double minres, int32_t keep_state,
-                                    int64_t *ticket) {
-  if (!s || !p || !m || !ticket || nmax < 1) return FVM_ERR_ARG;
+namespace {
+
+// Queues a solve (a resume when prim is given).
+int32_t submit(fvm_server *s, const fvm_params *p, const fvm_mesh *m, int32_t nmax,
+               double minres, int32_t keep_state, const double *prim, const double *nut,
+               const double *mul, const double *mu, int32_t iterlast, int64_t *ticket) {
+  if (!s || !p || !m || !ticket || nmax < 1 || m->np < 1 || iterlast < 0) return FVM_ERR_ARG;
   InCall in_call(s);
   *ticket = 0;
+  Ticket nt;
+  if (prim) {
+    const size_t np = (size_t)m->np;
+    nt.resume = true;
+    nt.iterlast = iterlast;
+    nt.start_prim.assign(prim, prim + 4 * np);
+    if (nut) nt.start_nut.assign(nut, nut + np);
+    if (mul) nt.start_mul.assign(mul, mul + np);
+    if (mu) nt.start_mu.assign(mu, mu + np);
+  }
   fvm_prepared *prep = nullptr;
   const int32_t st = fvm_batch_prepare(p, m, &prep);   // on the caller's thread
   if (st) return st;
@@ -350,6 +435,7 @@ extern "C" int32_t fvm_serve_submit(fvm_server *s, const fvm_params *p, const fv
   }
   const int64_t id = s->next_id++;
   Ticket &t = s->tickets[id];
+  t = std::move(nt);
   t.prep = prep;
   t.np = m->np;
   t.nmax = nmax;
@@ -360,6 +446,53 @@ extern "C" int32_t fvm_serve_submit(fvm_server *s, const fvm_params *p, const fv
   s->submitted++;
   s->cv_work.notify_one();
   *ticket = id;
+  return FVM_OK;
+}
+
+}  // namespace
+
+extern "C" int32_t fvm_serve_submit(fvm_server *s, const fvm_params *p, const fvm_mesh *m,
+                                    int32_t nmax, double minres, int32_t keep_state,
+                                    int64_t *ticket) {
+  return submit(s, p, m, nmax, minres, keep_state, nullptr, nullptr, nullptr, nullptr, 0,
+                ticket);
+}
+
+extern "C" int32_t fvm_serve_resume(fvm_server *s, const fvm_params *p, const fvm_mesh *m,
+                                    int32_t nmax, double minres, const double *prim,
+                                    const double *nut, const double *mul, const double *mu,
+                                    int32_t iterlast, int32_t keep_state, int64_t *ticket) {
+  if (!prim) return FVM_ERR_ARG;
+  return submit(s, p, m, nmax, minres, keep_state, prim, nut, mul, mu, iterlast, ticket);
+}
+
+extern "C" int32_t fvm_serve_checkpoint(fvm_server *s, int64_t ticket) {
+  if (!s) return FVM_ERR_ARG;
+  InCall in_call(s);
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->tickets.find(ticket);
+  if (it == s->tickets.end()) return FVM_ERR_ARG;
+  if (it->second.state != 1) return FVM_ERR_STATE;
+  it->second.ckpt_req = true;
+  s->cv_work.notify_one();
+  return FVM_OK;
+}
+
+extern "C" int32_t fvm_serve_checkpoint_read(fvm_server *s, int64_t ticket, double *prim,
+                                             double *nut, double *mul, double *mu,
+                                             int32_t *iter) {
+  if (!s) return FVM_ERR_ARG;
+  InCall in_call(s);
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->tickets.find(ticket);
+  if (it == s->tickets.end()) return FVM_ERR_ARG;
+  const Ticket &t = it->second;
+  if (t.state != 2 || t.status != FVM_CHECKPOINTED) return FVM_ERR_STATE;
+  if (prim) std::memcpy(prim, t.prim.data(), t.prim.size() * sizeof(double));
+  if (nut) std::memcpy(nut, t.nut.data(), t.nut.size() * sizeof(double));
+  if (mul) std::memcpy(mul, t.ck_mul.data(), t.ck_mul.size() * sizeof(double));
+  if (mu) std::memcpy(mu, t.ck_mu.data(), t.ck_mu.size() * sizeof(double));
+  if (iter) *iter = t.ck_iter;
   return FVM_OK;
 }
 

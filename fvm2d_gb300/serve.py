@@ -304,6 +304,41 @@ class NativeServer:
                 "fvm_serve_state")
         return dict(prim=prim, nut=nut)
 
+    def checkpoint(self, ticket: int):
+        """Stops a running solve at the end of the current step, keeping
+        its state (the ticket then finishes with status CHECKPOINTED)."""
+        L.check(L.lib().fvm_serve_checkpoint(self.h, ticket), "fvm_serve_checkpoint")
+
+    def checkpoint_read(self, ticket: int, np_: int) -> dict:
+        """The kept state of a checkpointed solve (driver order) and its
+        iteration count, from which fvm_serve_resume continues."""
+        import ctypes as C
+        prim, nut, mul, mu = np.zeros((np_, 4)), np.zeros(np_), np.zeros(np_), np.zeros(np_)
+        it = C.c_int32(0)
+        L.check(L.lib().fvm_serve_checkpoint_read(self.h, ticket, L.dptr(prim), L.dptr(nut),
+                                                  L.dptr(mul), L.dptr(mu), C.byref(it)),
+                "fvm_serve_checkpoint_read")
+        return dict(prim=prim, nut=nut, mul=mul, mu=mu, iter=it.value)
+
+    def resume(self, params: L.FvmParams, mesh, state: dict, nmax: int | None = None,
+               keep_state: bool = False) -> int:
+        """Queues a solve that starts from `state` (checkpoint_read's dict)
+        at its iteration count, for up to nmax more iterations."""
+        import ctypes as C
+        from .solver import MeshArrays
+        m = mesh if isinstance(mesh, MeshArrays) else MeshArrays(mesh)
+        ms = m.struct()
+        arr = {k: np.ascontiguousarray(state[k], dtype=np.float64)
+               for k in ("prim", "nut", "mul", "mu")}
+        t = C.c_int64(0)
+        L.check(L.lib().fvm_serve_resume(self.h, C.byref(params), C.byref(ms),
+                                         self.max_iter if nmax is None else int(nmax),
+                                         self.minres, L.dptr(arr["prim"]), L.dptr(arr["nut"]),
+                                         L.dptr(arr["mul"]), L.dptr(arr["mu"]),
+                                         int(state["iter"]), 1 if keep_state else 0,
+                                         C.byref(t)), "fvm_serve_resume")
+        return t.value
+
     def stats(self) -> dict:
         import ctypes as C
         out = (C.c_int64 * 6)()

@@ -70,6 +70,8 @@ extern "C" {
 #define FVM_ERR_GEOMETRY        9  /* tri_orient.f:28-31, geom_stat.f:18-37,
                                       flength.f:20-27, areas.f:145-150          */
 #define FVM_ERR_CAPACITY       10  /* a batch arena has no room                 */
+#define FVM_CHECKPOINTED       11  /* a served solve stopped on request with its
+                                      state kept (fvm_serve_checkpoint)        */
 
 /*
  * Scalars of the COMMON blocks that the hot path reads.  Fill with
@@ -289,14 +291,21 @@ typedef struct fvm_batch_caps {
                                    block's triangles; 2 each vertex walks its
                                    triangles itself (no shared memory); 3 the
                                    block's triangles and incidence staged by
-                                   bulk copies (FP32 only); 0 (default): 3 in
-                                   FP32, 1 in FP64                           */
+                                   bulk copies (FP32 only); 4 the same inputs
+                                   streamed through a ring of shared-memory
+                                   stages by a producer warp for consumer
+                                   groups (FP32 only); 0 (default): 4 in
+                                   FP32 (3 when no ring fits), 1 in FP64     */
   int32_t overlap;              /* 2..8: the meshes run in that many chains
                                    of kernels on their own streams (parts of
                                    the work list split at mesh boundaries),
                                    so one part's gradient pass overlaps
                                    another's flux pass; 0 or 1 (default):
                                    one chain                                */
+  int32_t pipe_groups;          /* consumer groups per CTA of the pipelined
+                                   kernels: 1 or 2 (0 = default, 2)         */
+  int32_t pipe_stages;          /* stages of their ring (0 = as many as fit
+                                   the shared memory, at most 8)            */
 } fvm_batch_caps;
 
 int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *caps,
@@ -360,6 +369,15 @@ int32_t fvm_batch_timing_read(fvm_batch *b, int32_t max, char *names,
                               double *ms, int64_t *launches, int32_t *n);
 /* Launches of this library's kernels since the batch was created. */
 int64_t fvm_batch_launch_count(fvm_batch *b);
+/* Test of the bounded device waits (no counterpart in the reference): one
+ * stage-1 gradient pass of the pipelined kernel (FP32 batches) in which the
+ * first block of every CTA is armed for its copies but the copies are never
+ * issued.  Its consumers give up after budget_cycles clock cycles with
+ * nothing in flight, and that block's mesh then reports FVM_ERR_TIMEOUT
+ * through fvm_batch_poll; the context stays usable.  Gradients of the other
+ * blocks are recomputed by the next iteration.  FVM_ERR_STATE when the
+ * pipelined kernel does not fit the resident meshes. */
+int32_t fvm_batch_test_wait_timeout(fvm_batch *b, int64_t budget_cycles);
 
 /* Autotuner (no counterpart in the reference): runs `iters` timed
  * iterations (rounded up to whole graphs of 10 iterations, which is how
@@ -423,6 +441,30 @@ int32_t fvm_serve_state(fvm_server *s, int64_t ticket, double *prim,
                         double *nut);
 /* Forgets a done solve. */
 int32_t fvm_serve_release(fvm_server *s, int64_t ticket);
+/* Checkpoint and restart of resident solves (the SOL file of
+ * finalize.f:14-24 and the restart of initialize.f:91-103, for solves that
+ * live in the service).  fvm_serve_checkpoint asks the service to stop a
+ * running solve at the end of the current step: its ticket then finishes
+ * with status FVM_CHECKPOINTED and keeps the solution, nu~, laminar and
+ * total viscosity (what the next iteration starts from) and its iteration
+ * count.  FVM_ERR_STATE when the ticket is queued or done.
+ * fvm_serve_checkpoint_read copies them out (driver order; prim(4,np),
+ * nut/mul/mu(np); any output may be NULL); results.sol_conserved writes
+ * the SOL text from prim and nut.  fvm_serve_resume queues a solve that
+ * starts from such a state at iteration iterlast: as in the reference's
+ * restart, its first iteration sets the residual normaliser
+ * (conres.f:25-29), and its state then evolves exactly as the
+ * uninterrupted solve's. */
+int32_t fvm_serve_checkpoint(fvm_server *s, int64_t ticket);
+int32_t fvm_serve_checkpoint_read(fvm_server *s, int64_t ticket, double *prim,
+                                  double *nut, double *mul, double *mu,
+                                  int32_t *iter);
+int32_t fvm_serve_resume(fvm_server *s, const fvm_params *p,
+                         const fvm_mesh *m, int32_t nmax, double minres,
+                         const double *prim, const double *nut,
+                         const double *mul, const double *mu,
+                         int32_t iterlast, int32_t keep_state,
+                         int64_t *ticket);
 /* out[6]: submitted, done, queued, running, steps, service status. */
 int32_t fvm_serve_stats(fvm_server *s, int64_t *out);
 /* out[5]: seconds the service thread spent admitting (between steps),

@@ -179,17 +179,25 @@ def test_fused_pass_and_grid_give_identical_results(fvm_lib, prec):
     loads, per-vertex walks, bulk-copy staging) sum the same triangle terms
     in the same order; the grid only changes which CTA takes a block, and
     the two overlapped chains only when a mesh's blocks run: every variant
-    must give the same bits, Euler and laminar."""
+    must give the same bits, Euler and laminar.  In FP32 the reference run
+    uses the default pipelined gradient pass (for the laminar mesh; the
+    Euler mesh takes the vertex-stencil pass in every form)."""
     g1, g2 = naca_ogrid(96, 40, jitter=0.1, seed=3), naca_ogrid(64, 24)
     ms = [fvm_lib.build_geometry(g.coord, g.elem, g.ptype) for g in (g1, g2)]
     flows = [dict(mach=0.8, aoa_deg=1.25),
              dict(iflow=L.LAMINAR, mach=0.5, aoa_deg=1.0, rey=5000.0, cfl=0.8)]
     n = 30
     ref = run_variant(fvm_lib, prec, ms, flows, n, viscous=True)
-    variants = [dict(fused=1), dict(fused=1, grid=7), dict(grid=3), dict(grad_mode=1),
-                dict(grad_mode=2), dict(overlap=2), dict(overlap=2, fused=1), dict(overlap=4)]
+    variants = [dict(grid=3), dict(grad_mode=1), dict(grad_mode=2), dict(overlap=2),
+                dict(overlap=4)]
+    if prec == L.FP64:    # the fused pass exists in FP64 only
+        variants += [dict(fused=1), dict(fused=1, grid=7), dict(overlap=2, fused=1)]
     if prec == L.FP32:
-        variants += [dict(grad_mode=3, grid=5)]
+        # the pipelined gradient pass: one CTA (the stage ring wraps many
+        # times), few CTAs, one consumer group with two stages, two chains
+        variants += [dict(grad_mode=3, grid=5), dict(grad_mode=4, grid=1, pipe_stages=3),
+                     dict(grad_mode=4, grid=5), dict(grad_mode=4, pipe_groups=1, pipe_stages=2),
+                     dict(grad_mode=4, overlap=2)]
     for caps in variants:
         got = run_variant(fvm_lib, prec, ms, flows, n, viscous=True, **caps)
         for (h, st), (h0, st0) in zip(got, ref):
@@ -250,3 +258,59 @@ def test_state_round_trip_in_driver_order(fvm_lib, prec):
     assert set(only) == {"prim"}
     np.testing.assert_array_equal(only["prim"], full["prim"])
     b.close()
+
+
+def test_bounded_wait_runs_out_with_a_status(fvm_lib):
+    """The pipelined gradient pass's waits are bounded: a pass in which each
+    CTA's first block is armed for copies that are never issued gives up
+    after a short budget (nothing is in flight), the mesh reports
+    FVM_ERR_TIMEOUT, and the context stays usable: a fresh batch then steps
+    normally and reproduces a solve run before the failure."""
+    from fvm2d_gb300.batch import Batch
+    m = mesh(fvm_lib, 64, 24)
+    flow = dict(mach=0.8, aoa_deg=1.25)
+    h0, st0 = alone(fvm_lib, L.FP32, m, flow, 10)
+    b = Batch(L.FP32, vertices=m.np, meshes=1)
+    s = b.add(fvm_lib.make_params(precision=L.FP32, **flow), m)
+    b.start(s, 10)
+    b.step(2)
+    assert b.poll(s)["status"] == L.OK
+    L.check(L.lib().fvm_batch_test_wait_timeout(b.h, 1 << 22), "fvm_batch_test_wait_timeout")
+    assert b.poll(s)["status"] == L.ERR_TIMEOUT
+    b.close()
+    h1, st1 = alone(fvm_lib, L.FP32, m, flow, 10)
+    np.testing.assert_array_equal(h1["fres"], h0["fres"])
+    np.testing.assert_array_equal(st1["prim"], st0["prim"])
+
+
+def test_fp32_fused_pass_is_refused(fvm_lib):
+    """The fused gradient+flux pass computes triangle-form gradients, which
+    FP32 inviscid meshes no longer use: an FP32 batch asking for it is
+    refused with FVM_ERR_ARG."""
+    from fvm2d_gb300.batch import Batch
+    with pytest.raises(L.FvmError) as e:
+        Batch(L.FP32, vertices=1000, meshes=1, fused=1)
+    assert e.value.status == L.ERR_ARG
+
+
+def test_fp32_stencil_gradient_matches_triangle_sums(fvm_lib, oracle_lib):
+    """The FP32 vertex-stencil Green-Gauss gradient (inviscid meshes) equals
+    the oracle's triangle sums to FP32 rounding: both from the same state,
+    after a few FP64 iterations."""
+    from fvm2d_gb300.ogrid import naca_ogrid
+    g = naca_ogrid(96, 40, jitter=0.1, seed=3)
+    o = oracle_lib.Oracle(g.coord, g.elem, g.ptype, mach=0.8, aoa_deg=1.25)
+    st, _ = o.iterate(5)
+    assert st == 0
+    s = fvm_lib.Solver(fvm_lib.make_params(precision=L.FP32, mach=0.8, aoa_deg=1.25),
+                       o.mesh_arrays())
+    sc = o.scalars()
+    s.set_state(o.d("prim"), o.d("nut"), o.d("mul"), o.d("mu"), iterlast=sc["iter"])
+    o.residu()
+    s.residu()
+    got = s.get_state()
+    for k in ("qx", "qy"):
+        ref = o.d(k)
+        scale = np.abs(ref).max(axis=0)
+        err = np.abs(got[k] - ref).max(axis=0) / scale
+        assert np.all(err < 2e-5), f"{k}: {err}"

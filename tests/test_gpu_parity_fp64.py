@@ -131,6 +131,24 @@ def test_iterate_100_fp64(oracle_lib, fvm_lib, grid1):
     np.testing.assert_array_equal(s.get_state()["prim"], o.d("prim"))
 
 
+def test_iterate_2000_fp64_config_stop_rule(oracle_lib, fvm_lib, grid1):
+    """The 160x48 Euler workload at its own stop rule (2000 iterations):
+    the whole state bit for bit, the residual's location every iteration,
+    the residual history within 1e-10 relative (a reduction in another
+    order) and the final lift and drag within 1e-8."""
+    o, s = make_pair(oracle_lib, fvm_lib, grid1)
+    st, h = s.iterate(2000)
+    ost, oh = o.iterate(2000)
+    assert st == 0 and ost == 0
+    assert len(h["fres"]) == len(oh["fres"]) == 2000
+    assert rel_err(h["fres"], oh["fres"]) <= 1e-10
+    np.testing.assert_array_equal(h["iresi"], oh["iresi"])
+    np.testing.assert_array_equal(h["fresi"], oh["fresi"])
+    assert abs(h["cl"][-1] - oh["cl"][-1]) <= 1e-8
+    assert abs(h["cd"][-1] - oh["cd"][-1]) <= 1e-8
+    np.testing.assert_array_equal(s.get_state()["prim"], o.d("prim"))
+
+
 def test_iterate_minres_stop(oracle_lib, fvm_lib, small):
     o, s = make_pair(oracle_lib, fvm_lib, small)
     st, h = s.iterate(400, minres=0.2)

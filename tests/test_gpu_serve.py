@@ -127,3 +127,48 @@ def test_native_service_destroy_wakes_waiters(fvm_lib):
         t.join(timeout=30.0)
         assert not t.is_alive()
     assert states == {tickets[0]: (L.OK, 2), tickets[1]: (L.OK, 2)}
+
+
+@pytest.mark.parametrize("laminar", [False, True])
+def test_checkpointed_and_resumed_solve_equals_uninterrupted(fvm_lib, laminar):
+    """A served solve stopped at a checkpoint and resumed from the kept
+    state (its iteration count as iterlast) ends in the same state, bit for
+    bit, as the same solve run uninterrupted for the same total number of
+    iterations; the resumed run renormalises its residual at its first
+    iteration, as the reference's restart does (conres.f:25-29)."""
+    from fvm2d_gb300 import serve
+    from fvm2d_gb300.batch import Batch
+    req = serve.generate_requests(n=1, seed=8, pmin=3000, pmax=3000,
+                                  laminar_frac=1.0 if laminar else 0.0)[0]
+    g = serve.grid_for(req)
+    mesh = fvm_lib.build_geometry(g.coord, g.elem, g.ptype)
+    par = serve.params_for(req, L.FP32)
+    srv = serve.NativeServer(vertices=20000, meshes=2, chunk=10, workers=1, max_iter=10 ** 6,
+                             minres=0.0)
+    t = srv.submit(par, mesh)
+    import time
+    t0 = time.time()
+    while srv.stats()["steps"] < 3 and time.time() - t0 < 60:
+        time.sleep(0.01)
+    srv.checkpoint(t)
+    assert srv.wait(t, 60.0)
+    r = srv.result(t)
+    assert r["status"] == L.CHECKPOINTED and r["niter"] >= 10
+    ck = srv.checkpoint_read(t, mesh.np)
+    assert ck["iter"] == r["niter"]
+    extra = 25
+    t2 = srv.resume(par, mesh, ck, nmax=extra, keep_state=True)
+    assert srv.wait(t2, 60.0)
+    r2 = srv.result(t2)
+    assert r2["status"] == L.OK and r2["niter"] == extra
+    got = srv.state(t2, mesh.np)["prim"]
+    srv.close()
+    total = ck["iter"] + extra
+    b = Batch(L.FP32, vertices=mesh.np, meshes=1, viscous=True)
+    s = b.add(par, mesh)
+    b.start(s, total)
+    b.step(total)
+    q = b.poll(s)
+    assert q["niter"] == total and q["status"] == L.OK
+    np.testing.assert_array_equal(got, b.get_state(s)["prim"])
+    b.close()

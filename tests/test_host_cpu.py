@@ -26,9 +26,11 @@ def header_functions():
 def test_library_exports_every_declared_symbol(fvm_lib):
     names = header_functions()
     assert len(names) >= 23
-    lib = ctypes.CDLL(L.LIB)
-    missing = [n for n in names if not hasattr(lib, n)]
-    assert not missing, missing
+    from fvm2d_gb300 import build
+    for path in (build.LIB, build.LIB_FP64FMA):   # the main and the FP64-FMA library
+        lib = ctypes.CDLL(path)
+        missing = [n for n in names if not hasattr(lib, n)]
+        assert not missing, (path, missing)
     assert set(names) == set(L.SIGNATURES), set(names) ^ set(L.SIGNATURES)
 
 
