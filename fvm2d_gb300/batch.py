@@ -67,7 +67,7 @@ class Batch:
         self.h = h
         self.precision = precision
         self._meshes = {}
-        gm = int(caps.get("grad_mode", 0)) or (4 if precision == L.FP32 else 1)
+        gm = int(caps.get("grad_mode", 0)) or (3 if precision == L.FP32 else 1)
         ch = int(caps.get("overlap", 0))
         if int(caps.get("fused", 0)) > 0:
             self.form = "fused+overlap" if ch > 1 else "fused"

@@ -9,6 +9,7 @@
 // of one sized exactly for its mesh.
 #include <algorithm>
 #include <climits>
+#include <cstddef>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -389,6 +390,59 @@ int32_t get_vertex(fvm_batch *b, const Slot &s, double *dst, const void *src_bas
 
 int32_t sync_stream(fvm_batch *b) {
   FVM_TRY(b, cudaStreamSynchronize(b->stream));
+  return FVM_OK;
+}
+
+// The same transfers for a slot's state arrays whose buffer rotates with the
+// mesh (state: ctl.phase of 3, nu~: ctl.nphase of 2) or not (one buffer):
+// the device picks the buffer from the control block, so no host read of
+// it is needed.  Queued on the batch stream.
+enum class Rot { None, Phase, NutPhase };
+struct RotBufs {
+  unsigned char *b[3];
+  const int *sel;
+};
+RotBufs rot_bufs(fvm_batch *b, int32_t slot, Rot rot, void *single) {
+  RotBufs r;
+  const char *ctl = reinterpret_cast<const char *>(b->ctl + slot);
+  r.sel = reinterpret_cast<const int *>(ctl + (rot == Rot::NutPhase ? offsetof(MeshCtl, nphase)
+                                                                     : offsetof(MeshCtl, phase)));
+  if (rot == Rot::Phase) {
+    for (int i = 0; i < 3; i++) r.b[i] = static_cast<unsigned char *>(b->st[i]);
+  } else if (rot == Rot::NutPhase) {
+    r.b[0] = static_cast<unsigned char *>(b->nut[0]);
+    r.b[1] = r.b[2] = static_cast<unsigned char *>(b->nut[1]);
+  } else {
+    r.b[0] = r.b[1] = r.b[2] = static_cast<unsigned char *>(single);
+  }
+  return r;
+}
+
+int32_t put_vertex_rot(fvm_batch *b, int32_t slot, const Slot &s, Rot rot, void *single,
+                       const double *src, int k, size_t stride) {
+  const int np = s.L.np;
+  const size_t n = (size_t)np * k * sizeof(double);
+  cudaError_t e;
+  double *stage = dstaging(b, n, e);
+  FVM_TRY(b, e);
+  const RotBufs rb = rot_bufs(b, slot, rot, single);
+  FVM_TRY(b, cudaMemcpyAsync(stage, src, n, cudaMemcpyHostToDevice, b->stream));
+  FVM_TRY(b, launch_put_vertex_sel(b->rsz, rb.b, rb.sel, (size_t)s.off[P_V] * stride, stride,
+                                   stage, b->orig + s.off[P_V], np, k, b->stream));
+  return FVM_OK;
+}
+
+int32_t get_vertex_rot(fvm_batch *b, int32_t slot, const Slot &s, Rot rot, void *single,
+                       double *dst, int k, size_t stride, int c0 = 0) {
+  const int np = s.L.np;
+  const size_t n = (size_t)np * k * sizeof(double);
+  cudaError_t e;
+  double *stage = dstaging(b, n, e);
+  FVM_TRY(b, e);
+  const RotBufs rb = rot_bufs(b, slot, rot, single);
+  FVM_TRY(b, launch_get_vertex_sel(b->rsz, stage, rb.b, rb.sel, (size_t)s.off[P_V] * stride,
+                                   stride, b->orig + s.off[P_V], np, k, c0, b->stream));
+  FVM_TRY(b, cudaMemcpyAsync(dst, stage, n, cudaMemcpyDeviceToHost, b->stream));
   return FVM_OK;
 }
 
@@ -802,16 +856,17 @@ extern "C" int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *cap
   b->cfg.stencil = precision == FVM_PREC_FP32;
   b->cfg.any_inviscid = false;
   b->chains = std::min(std::max(c.overlap, 1), kMaxChains);
-  // gradient pass: in FP32 the pipelined form by default (launched as the
-  // bulk-copy form while the resident meshes' tiles leave no room for a
-  // stage ring), per-thread loads in FP64
+  // gradient pass (the triangle form, of viscous meshes in FP32): the
+  // bulk-copy form by default in FP32 (the pipelined form measured 1-4%
+  // slower on laminar and RANS batches and is a tuner candidate),
+  // per-thread loads in FP64
   const bool bulk_fits = grad_bulk_layout(c.max_tri, kTriLocMax, c.viscous != 0).total <= kMaxSmem;
   if (c.pipe_groups < 0 || c.pipe_groups > 2 || c.pipe_stages < 0 || c.pipe_stages > kPipeMaxStages)
     return fail(FVM_ERR_ARG);
   b->cfg.pipe_groups = c.pipe_groups == 1 ? 1 : 2;
   b->cfg.pipe_stages = c.pipe_stages;
   b->cfg.grad_mode = c.grad_mode > 0 ? c.grad_mode
-                                      : (precision == FVM_PREC_FP32 && bulk_fits ? 4 : 1);
+                                      : (precision == FVM_PREC_FP32 && bulk_fits ? 3 : 1);
   if (b->cfg.grad_mode < 1 || b->cfg.grad_mode > 4 ||
       (b->cfg.grad_mode >= 3 && (precision != FVM_PREC_FP32 || !bulk_fits)))
     return fail(FVM_ERR_ARG);
@@ -1280,22 +1335,16 @@ extern "C" int32_t fvm_batch_set_state(fvm_batch *b, int32_t slot, const double 
     if (cst) return cst;
   }
   Slot *S = slot_of(b, slot);
-  if (!S || !prim) return FVM_ERR_ARG;
-  MeshCtl c;
-  int32_t st = get_ctl(b, slot, c);
-  if (st) return st;
+  if (!S || !prim || iterlast < 0) return FVM_ERR_ARG;
   const size_t r = b->rsz;
-  if ((st = put_vertex(b, *S, b->st[c.phase], prim, 4, 4 * r))) return st;
-  if (nut && (st = put_vertex(b, *S, b->nut[c.nphase], nut, 1, r))) return st;
-  if (mul && (st = put_vertex(b, *S, b->mul, mul, 1, r))) return st;
-  if (mu && (st = put_vertex(b, *S, b->mu, mu, 1, r))) return st;
-  c.iter = iterlast;
-  c.iterlast = iterlast;
-  c.fres1 = 0.0;
-  c.err = 0;
-  c.err_point = INT_MAX;
-  c.active = 0;
-  return put_ctl(b, slot, c);
+  int32_t st;
+  if ((st = put_vertex_rot(b, slot, *S, Rot::Phase, nullptr, prim, 4, 4 * r))) return st;
+  if (nut && (st = put_vertex_rot(b, slot, *S, Rot::NutPhase, nullptr, nut, 1, r))) return st;
+  if (mul && (st = put_vertex_rot(b, slot, *S, Rot::None, b->mul, mul, 1, r))) return st;
+  if (mu && (st = put_vertex_rot(b, slot, *S, Rot::None, b->mu, mu, 1, r))) return st;
+  FVM_TRY(b, launch_ctl_update(b->ctl + slot, 0, iterlast, 0.0, b->stream));
+  // the caller's arrays have been read when the call returns
+  return sync_stream(b);
 }
 
 extern "C" int32_t fvm_batch_get_state(fvm_batch *b, int32_t slot, double *prim, double *nut,
@@ -1306,16 +1355,14 @@ extern "C" int32_t fvm_batch_get_state(fvm_batch *b, int32_t slot, double *prim,
   }
   Slot *S = slot_of(b, slot);
   if (!S) return FVM_ERR_ARG;
-  MeshCtl c;
-  int32_t st = get_ctl(b, slot, c);
-  if (st) return st;
   const size_t r = b->rsz;
-  if (prim && (st = get_vertex(b, *S, prim, b->st[c.phase], 4, 4 * r))) return st;
-  if (nut && (st = get_vertex(b, *S, nut, b->nut[c.nphase], 1, r))) return st;
-  if (mul && (st = get_vertex(b, *S, mul, b->mul, 1, r))) return st;
-  if (mu && (st = get_vertex(b, *S, mu, b->mu, 1, r))) return st;
-  if (qx && (st = get_vertex(b, *S, qx, b->grad, 4, 8 * r, 0))) return st;
-  if (qy && (st = get_vertex(b, *S, qy, b->grad, 4, 8 * r, 4))) return st;
+  int32_t st;
+  if (prim && (st = get_vertex_rot(b, slot, *S, Rot::Phase, nullptr, prim, 4, 4 * r))) return st;
+  if (nut && (st = get_vertex_rot(b, slot, *S, Rot::NutPhase, nullptr, nut, 1, r))) return st;
+  if (mul && (st = get_vertex_rot(b, slot, *S, Rot::None, b->mul, mul, 1, r))) return st;
+  if (mu && (st = get_vertex_rot(b, slot, *S, Rot::None, b->mu, mu, 1, r))) return st;
+  if (qx && (st = get_vertex_rot(b, slot, *S, Rot::None, b->grad, qx, 4, 8 * r, 0))) return st;
+  if (qy && (st = get_vertex_rot(b, slot, *S, Rot::None, b->grad, qy, 4, 8 * r, 4))) return st;
   return sync_stream(b);
 }
 
@@ -1326,16 +1373,9 @@ extern "C" int32_t fvm_batch_start(fvm_batch *b, int32_t slot, int32_t nmax, dou
   }
   Slot *S = slot_of(b, slot);
   if (!S || nmax < 0) return FVM_ERR_ARG;
-  MeshCtl c;
-  int32_t st = get_ctl(b, slot, c);
-  if (st) return st;
-  c.active = nmax > 0 ? 1 : 0;
-  c.n_done = 0;
-  c.n_max = nmax;
-  c.minres = minres;
-  c.err = 0;
-  c.err_point = INT_MAX;
-  return put_ctl(b, slot, c);
+  // on the device, in stream order before the next step (no host wait)
+  FVM_TRY(b, launch_ctl_update(b->ctl + slot, 1, nmax, minres, b->stream));
+  return FVM_OK;
 }
 
 extern "C" int32_t fvm_batch_step(fvm_batch *b, int32_t niter) {

@@ -82,5 +82,16 @@ cudaError_t launch_get_vertex(int rsz, double *dst, const unsigned char *src, si
                               const int *orig, int np, int k, int c0, cudaStream_t s);
 cudaError_t launch_fill_vertex(int rsz, unsigned char *dst, size_t stride, int np, int k,
                                const double *values, cudaStream_t s);
+// the same into / out of buffer b[*sel] (sel: a field of the mesh's control
+// block on the device), from byte offset off
+cudaError_t launch_put_vertex_sel(int rsz, unsigned char *const b[3], const int *sel, size_t off,
+                                  size_t stride, const double *src, const int *orig, int np,
+                                  int k, cudaStream_t s);
+cudaError_t launch_get_vertex_sel(int rsz, double *dst, unsigned char *const b[3], const int *sel,
+                                  size_t off, size_t stride, const int *orig, int np, int k,
+                                  int c0, cudaStream_t s);
+// a mesh's control block set on the device for a new state (what 0) or a
+// start (what 1)
+cudaError_t launch_ctl_update(MeshCtl *c, int what, int n, double minres, cudaStream_t s);
 
 }  // namespace fvm

@@ -1,5 +1,8 @@
 // fvm_setup.cu -- FP64 set-up kernels, run once per mesh.  Compiled with
 // --fmad=false so the results equal the serial FP64 arithmetic.
+#include <climits>
+#include <cstddef>
+
 #include <cuda_runtime.h>
 
 #include "fvm_launch.h"
@@ -137,6 +140,86 @@ __global__ void k_get_vertex(double *dst, const unsigned char *src, size_t strid
     double *d = dst + (size_t)(orig[v] - 1) * k;
     for (int c = 0; c < k; c++) d[c] = (double)q[c];
   }
+}
+
+// The same transfers into / out of one of three buffers chosen on the
+// device by *sel (a mesh's state phase or nu~ phase in its control block),
+// so the host need not read the control block first.  off: the mesh's
+// first row, in bytes.
+template <typename R>
+__global__ void k_put_vertex_sel(unsigned char *b0, unsigned char *b1, unsigned char *b2,
+                                 const int *sel, size_t off, size_t stride,
+                                 const double *__restrict__ src, const int *__restrict__ orig,
+                                 int np, int k) {
+  const int i = *sel;
+  unsigned char *dst = (i == 0 ? b0 : i == 1 ? b1 : b2) + off;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < np; v += gridDim.x * blockDim.x) {
+    const double *q = src + (size_t)(orig[v] - 1) * k;
+    R *d = reinterpret_cast<R *>(dst + (size_t)v * stride);
+    for (int c = 0; c < k; c++) d[c] = (R)q[c];
+  }
+}
+
+template <typename R>
+__global__ void k_get_vertex_sel(double *dst, const unsigned char *b0, const unsigned char *b1,
+                                 const unsigned char *b2, const int *sel, size_t off,
+                                 size_t stride, const int *__restrict__ orig, int np, int k,
+                                 int c0) {
+  const int i = *sel;
+  const unsigned char *src = (i == 0 ? b0 : i == 1 ? b1 : b2) + off;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < np; v += gridDim.x * blockDim.x) {
+    const R *q = reinterpret_cast<const R *>(src + (size_t)v * stride) + c0;
+    double *d = dst + (size_t)(orig[v] - 1) * k;
+    for (int c = 0; c < k; c++) d[c] = (double)q[c];
+  }
+}
+
+// A mesh's control block set for a new state (what 0: iteration and
+// iterlast = n, residual normaliser cleared, inactive) or for a start
+// (what 1: up to n iterations stopping at fres <= minres), on the device.
+__global__ void k_ctl_update(MeshCtl *c, int what, int n, double minres) {
+  if (what == 0) {
+    c->iter = n;
+    c->iterlast = n;
+    c->fres1 = 0.0;
+    c->active = 0;
+  } else {
+    c->active = n > 0 ? 1 : 0;
+    c->n_done = 0;
+    c->n_max = n;
+    c->minres = minres;
+  }
+  c->err = 0;
+  c->err_point = INT_MAX;
+}
+
+cudaError_t launch_put_vertex_sel(int rsz, unsigned char *const b[3], const int *sel, size_t off,
+                                  size_t stride, const double *src, const int *orig, int np,
+                                  int k, cudaStream_t s) {
+  if (np <= 0) return cudaSuccess;
+  const int g = (np + 255) / 256;
+  if (rsz == 8)
+    k_put_vertex_sel<double><<<g, 256, 0, s>>>(b[0], b[1], b[2], sel, off, stride, src, orig, np, k);
+  else
+    k_put_vertex_sel<float><<<g, 256, 0, s>>>(b[0], b[1], b[2], sel, off, stride, src, orig, np, k);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_get_vertex_sel(int rsz, double *dst, unsigned char *const b[3], const int *sel,
+                                  size_t off, size_t stride, const int *orig, int np, int k,
+                                  int c0, cudaStream_t s) {
+  if (np <= 0) return cudaSuccess;
+  const int g = (np + 255) / 256;
+  if (rsz == 8)
+    k_get_vertex_sel<double><<<g, 256, 0, s>>>(dst, b[0], b[1], b[2], sel, off, stride, orig, np, k, c0);
+  else
+    k_get_vertex_sel<float><<<g, 256, 0, s>>>(dst, b[0], b[1], b[2], sel, off, stride, orig, np, k, c0);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ctl_update(MeshCtl *c, int what, int n, double minres, cudaStream_t s) {
+  k_ctl_update<<<1, 1, 0, s>>>(c, what, n, minres);
+  return cudaGetLastError();
 }
 
 // every row of a mesh's per-vertex array set to the same k values

@@ -294,8 +294,10 @@ typedef struct fvm_batch_caps {
                                    bulk copies (FP32 only); 4 the same inputs
                                    streamed through a ring of shared-memory
                                    stages by a producer warp for consumer
-                                   groups (FP32 only); 0 (default): 4 in
-                                   FP32 (3 when no ring fits), 1 in FP64     */
+                                   groups (FP32 only); 0 (default): 3 in
+                                   FP32, 1 in FP64.  In FP32 this is the
+                                   pass of viscous meshes: inviscid meshes
+                                   take the vertex-stencil gradient        */
   int32_t overlap;              /* 2..8: the meshes run in that many chains
                                    of kernels on their own streams (parts of
                                    the work list split at mesh boundaries),
@@ -449,7 +451,7 @@ int32_t fvm_serve_release(fvm_server *s, int64_t ticket);
  * total viscosity (what the next iteration starts from) and its iteration
  * count.  FVM_ERR_STATE when the ticket is queued or done.
  * fvm_serve_checkpoint_read copies them out (driver order; prim(4,np),
- * nut/mul/mu(np); any output may be NULL); results.sol_conserved writes
+ * nut/mul/mu(np); any output may be NULL); results.write_sol writes
  * the SOL text from prim and nut.  fvm_serve_resume queues a solve that
  * starts from such a state at iteration iterlast: as in the reference's
  * restart, its first iteration sets the residual normaliser

@@ -179,9 +179,10 @@ def test_fused_pass_and_grid_give_identical_results(fvm_lib, prec):
     loads, per-vertex walks, bulk-copy staging) sum the same triangle terms
     in the same order; the grid only changes which CTA takes a block, and
     the two overlapped chains only when a mesh's blocks run: every variant
-    must give the same bits, Euler and laminar.  In FP32 the reference run
-    uses the default pipelined gradient pass (for the laminar mesh; the
-    Euler mesh takes the vertex-stencil pass in every form)."""
+    must give the same bits, Euler and laminar.  In FP32 the Euler mesh
+    takes the vertex-stencil gradient pass in every form; the variants
+    cover the triangle forms of the laminar mesh, the pipelined one
+    included."""
     g1, g2 = naca_ogrid(96, 40, jitter=0.1, seed=3), naca_ogrid(64, 24)
     ms = [fvm_lib.build_geometry(g.coord, g.elem, g.ptype) for g in (g1, g2)]
     flows = [dict(mach=0.8, aoa_deg=1.25),
