@@ -354,24 +354,6 @@ int32_t put_ctl(fvm_batch *b, int slot, const MeshCtl &c) {
   return FVM_OK;
 }
 
-// host double [np][k] (driver order) -> device [np][k] of the slot: the
-// array goes to the device as it is; a kernel permutes it into arena order
-// and converts it to the batch precision.  Queued on the batch stream (the
-// staging buffer is reused in stream order); the caller synchronises once
-// after its last transfer.
-int32_t put_vertex(fvm_batch *b, const Slot &s, void *dst_base, const double *src, int k,
-                   size_t stride) {
-  const int np = s.L.np;
-  const size_t n = (size_t)np * k * sizeof(double);
-  cudaError_t e;
-  double *stage = dstaging(b, n, e);
-  FVM_TRY(b, e);
-  unsigned char *dst = static_cast<unsigned char *>(dst_base) + (size_t)s.off[P_V] * stride;
-  FVM_TRY(b, cudaMemcpyAsync(stage, src, n, cudaMemcpyHostToDevice, b->stream));
-  FVM_TRY(b, launch_put_vertex(b->rsz, dst, stride, stage, b->orig + s.off[P_V], np, k, b->stream));
-  return FVM_OK;
-}
-
 // device [np][stride] of the slot, values c0..c0+k-1 -> host double [np][k]
 // in driver order (permuted and widened on the device); queued on the batch
 // stream, complete after the caller's synchronisation

@@ -76,8 +76,6 @@ cudaError_t launch_dtlength(int np, int nt, const double2 *coord, const int *ele
 cudaError_t launch_wall_dist(int np, int nsedge, const double2 *coord, const int2 *sedge,
                              const int *ptype, int bugcompat, double *wd, cudaStream_t s);
 // driver-order FP64 <-> arena-order per-vertex arrays of one mesh (fvm_setup.cu)
-cudaError_t launch_put_vertex(int rsz, unsigned char *dst, size_t stride, const double *src,
-                              const int *orig, int np, int k, cudaStream_t s);
 cudaError_t launch_get_vertex(int rsz, double *dst, const unsigned char *src, size_t stride,
                               const int *orig, int np, int k, int c0, cudaStream_t s);
 cudaError_t launch_fill_vertex(int rsz, unsigned char *dst, size_t stride, int np, int k,

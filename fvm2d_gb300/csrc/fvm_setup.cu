@@ -123,16 +123,6 @@ cudaError_t launch_wall_dist(int np, int nsedge, const double2 *coord, const int
 // Conversions round to nearest, as the host's would (this unit does not
 // flush subnormals).
 template <typename R>
-__global__ void k_put_vertex(unsigned char *dst, size_t stride, const double *__restrict__ src,
-                             const int *__restrict__ orig, int np, int k) {
-  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < np; v += gridDim.x * blockDim.x) {
-    const double *q = src + (size_t)(orig[v] - 1) * k;
-    R *d = reinterpret_cast<R *>(dst + (size_t)v * stride);
-    for (int c = 0; c < k; c++) d[c] = (R)q[c];
-  }
-}
-
-template <typename R>
 __global__ void k_get_vertex(double *dst, const unsigned char *src, size_t stride,
                              const int *__restrict__ orig, int np, int k, int c0) {
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < np; v += gridDim.x * blockDim.x) {
@@ -242,15 +232,6 @@ cudaError_t launch_fill_vertex(int rsz, unsigned char *dst, size_t stride, int n
   const int g = (np + 255) / 256;
   if (rsz == 8) k_fill_vertex<double><<<g, 256, 0, s>>>(dst, stride, np, k, a[0], a[1], a[2], a[3]);
   else k_fill_vertex<float><<<g, 256, 0, s>>>(dst, stride, np, k, a[0], a[1], a[2], a[3]);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_put_vertex(int rsz, unsigned char *dst, size_t stride, const double *src,
-                              const int *orig, int np, int k, cudaStream_t s) {
-  if (np <= 0) return cudaSuccess;
-  const int g = (np + 255) / 256;
-  if (rsz == 8) k_put_vertex<double><<<g, 256, 0, s>>>(dst, stride, src, orig, np, k);
-  else k_put_vertex<float><<<g, 256, 0, s>>>(dst, stride, src, orig, np, k);
   return cudaGetLastError();
 }
 
