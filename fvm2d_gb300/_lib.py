@@ -128,6 +128,8 @@ SIGNATURES = {
                                           C.POINTER(C.c_int64), _pi]),
     "fvm_batch_launch_count": (C.c_int64, [C.c_void_p]),
     "fvm_batch_test_wait_timeout": (C.c_int32, [C.c_void_p, C.c_int64]),
+    "fvm_gpu_gradient": (C.c_int32, [C.c_void_p]),
+    "fvm_gpu_shockind": (C.c_int32, [C.c_void_p]),
     "fvm_batch_tune": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, _pd, _pi]),
     "fvm_batch_set_form": (C.c_int32, [C.c_void_p, C.c_int32]),
     "fvm_abi_sizes": (None, [C.POINTER(C.c_int64)]),

@@ -120,6 +120,7 @@ struct fvm_batch {
   uint16_t *ve_list = nullptr, *vt_list = nullptr;
   int *va_list = nullptr;
   float2 *va_w = nullptr;   // FP32: Green-Gauss stencil weights per va_list entry
+  double *va_dsl = nullptr; // |ds| of each va_list entry's edge
   BlockInfo *blocks = nullptr;
   int2 *be_nodes = nullptr, *sw_nodes = nullptr;
   double2 *be_ds = nullptr;
@@ -237,6 +238,7 @@ ArenaPtrs<R> ptrs(const fvm_batch *b) {
   A.va_rng = b->va_rng;
   A.va_list = b->va_list;
   A.va_w = b->va_w;
+  A.va_dsl = b->va_dsl;
   A.mc = b->mc;
   A.ctl = b->ctl;
   A.part = b->part;
@@ -786,6 +788,7 @@ extern "C" int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *cap
   TRYB(dalloc(O, &b->ve_list, (size_t)c.edge_incidence));
   TRYB(dalloc(O, &b->vt_list, (size_t)c.tri_incidence + 16));   // slack: 16-byte copies
   TRYB(dalloc(O, &b->va_list, (size_t)c.all_incidence));
+  TRYB(dalloc(O, &b->va_dsl, (size_t)c.all_incidence));
   TRYB(dalloc(O, &b->blocks, (size_t)c.blocks));
   TRYB(dalloc(O, &b->part, (size_t)c.blocks));
   TRYB(dalloc(O, &b->work, (size_t)c.blocks));
@@ -898,6 +901,7 @@ struct fvm_prepared {
   std::vector<double2> be_ds;
   std::vector<EdgeGeo32> be_g32;   // FP32 batches (mesh-local vertex ids)
   std::vector<float2> va_w;        // FP32 batches: Green-Gauss weights per va_list entry
+  std::vector<double> va_dsl;      // |ds| of each va_list entry's edge (shockind.f:36)
   std::vector<TriGeo32> tri_g32;   // FP32 batches
 };
 
@@ -1007,6 +1011,19 @@ extern "C" int32_t fvm_batch_prepare(const fvm_params *par, const fvm_mesh *m, f
       for (int j = L.va_ptr[v]; j < L.va_ptr[v + 1]; j++)
         P->va_w[j] = make_float2((float)(P->ais[v] * wx[j]), (float)(P->ais[v] * wy[j]));
   }
+  // |ds| per all-edge incidence entry, in the order build_layout lists them
+  // (edge order, both ends of each edge); dsqrt(ds(1)**2 + ds(2)**2)
+  P->va_dsl.resize(L.va_list.size());
+  {
+    std::vector<int> cur(L.va_ptr.begin(), L.va_ptr.end() - 1);
+    for (int e = 0; e < m->netot; e++) {
+      const int a = L.iperm[m->edge[2 * e] - 1], c = L.iperm[m->edge[2 * e + 1] - 1];
+      const double dsx = m->ds[2 * e], dsy = m->ds[2 * e + 1];
+      const double dl = std::sqrt(dsx * dsx + dsy * dsy);
+      P->va_dsl[cur[a]++] = dl;
+      P->va_dsl[cur[c]++] = dl;
+    }
+  }
   P->tri_g32.resize(L.bt_nodes.size());
   for (size_t k = 0; k < L.bt_nodes.size(); k++) {
     const int t = L.bt_nodes[k].w;   // driver triangle of this block entry
@@ -1043,7 +1060,7 @@ extern "C" int64_t fvm_prepared_bytes(const fvm_prepared *prep, int32_t precisio
   bytes += (int64_t)L.be_nodes.size() * (8 + 16 + 32);
   bytes += (int64_t)L.bb_nodes.size() * 16 + (int64_t)L.bt_nodes.size() * (16 + (r == 4 ? 32 : 0));
   bytes += (int64_t)L.nt * 8 + (int64_t)L.ve_list.size() * 2 + (int64_t)L.vt_list.size() * 2;
-  bytes += (int64_t)L.va_list.size() * (4 + (r == 4 ? 8 : 0)) + (int64_t)L.sw_nodes.size() * 8;
+  bytes += (int64_t)L.va_list.size() * (12 + (r == 4 ? 8 : 0)) + (int64_t)L.sw_nodes.size() * 8;
   bytes += (int64_t)L.nblk * (sizeof(BlockInfo) + sizeof(BlockPartial) + 4);
   bytes += (int64_t)L.be_loc.size() * 4 + (int64_t)L.halo_ids.size() * 4;
   bytes += (int64_t)L.hl_ptr.size() * 4 + (int64_t)L.hl_list.size() * 2;
@@ -1214,6 +1231,7 @@ static int32_t add_prepared(fvm_batch *b, fvm_prepared *prep, int32_t *slot_out,
   }
   if (b->tri_g32) PUT(put_range(b, b->tri_g32, S.off[P_BT], prep->tri_g32, us));
   if (b->va_w) PUT(put_range(b, b->va_w, S.off[P_VA], prep->va_w, us));
+  PUT(put_range(b, b->va_dsl, S.off[P_VA], prep->va_dsl, us));
   PUT(put_range(b, b->sw_nodes, S.off[P_SW], sw, us));
   PUT(cudaMemcpyAsync(b->mc + sid, &mc, sizeof(mc), cudaMemcpyHostToDevice, us));
   PUT(cudaMemcpyAsync(b->ctl + sid, &ctl, sizeof(ctl), cudaMemcpyHostToDevice, us));
@@ -1476,7 +1494,10 @@ extern "C" int32_t fvm_batch_tune(fvm_batch *b, int32_t iters, int32_t max, doub
   b->tune_calls++;
   for (int i = 0; i < kForms && st == FVM_OK; i++) {
     const Form f = form_of(b, i);
-    if (!form_fits(b, f)) {
+    // FP32: the per-thread-load and per-vertex triangle passes are not
+    // timed (they only serve viscous meshes there and were never fastest);
+    // set_form still accepts them
+    if (!form_fits(b, f) || (b->prec == FVM_PREC_FP32 && (f.grad == 1 || f.grad == 2))) {
       b->tune_last[i] = 0.0;
       continue;
     }
@@ -1859,6 +1880,26 @@ extern "C" int32_t fvm_gpu_limitgrad(fvm_handle *h) {
   fvm_batch *b = h->b;
   if (b->prec == FVM_PREC_FP64) FVM_TRY(b, launch_limitgrad(ptrs<double>(b), b->cfg));
   else FVM_TRY(b, launch_limitgrad(ptrs<float>(b), b->cfg));
+  b->launches++;
+  FVM_TRY(b, cudaStreamSynchronize(b->stream));
+  return FVM_OK;
+}
+
+extern "C" int32_t fvm_gpu_gradient(fvm_handle *h) {
+  if (!h) return FVM_ERR_ARG;
+  fvm_batch *b = h->b;
+  if (b->prec == FVM_PREC_FP64) FVM_TRY(b, launch_gradient_edge(ptrs<double>(b), b->cfg));
+  else FVM_TRY(b, launch_gradient_edge(ptrs<float>(b), b->cfg));
+  b->launches++;
+  FVM_TRY(b, cudaStreamSynchronize(b->stream));
+  return FVM_OK;
+}
+
+extern "C" int32_t fvm_gpu_shockind(fvm_handle *h) {
+  if (!h) return FVM_ERR_ARG;
+  fvm_batch *b = h->b;
+  if (b->prec == FVM_PREC_FP64) FVM_TRY(b, launch_shockind(ptrs<double>(b), b->cfg));
+  else FVM_TRY(b, launch_shockind(ptrs<float>(b), b->cfg));
   b->launches++;
   FVM_TRY(b, cudaStreamSynchronize(b->stream));
   return FVM_OK;

@@ -262,6 +262,7 @@ struct ArenaPtrs {
   const int2 *va_rng;
   const int *va_list;     // other vertex | (is n2) << 31
   const float2 *va_w;     // FP32: Green-Gauss stencil weight of each va_list entry
+  const double *va_dsl;   // |ds| of the edge of each va_list entry (shockind.f:36)
   // per mesh
   const MeshConst *mc;
   MeshCtl *ctl;

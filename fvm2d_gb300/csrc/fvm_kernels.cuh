@@ -1866,6 +1866,143 @@ __global__ void __launch_bounds__(256) k_routine_monitor(ArenaPtrs<R> A, int mes
 
 // limitgrad.f:14-75 on the current gradients, one thread per vertex over
 // all of its edges in edge order.
+// ---------------------------------------------------------------------------
+// gradient.f:1-63 (never called by the reference: main.f:29 comments it
+// out), routine mode: edge-based Green-Gauss over the dual cells.  Each
+// interior edge contributes +-(qa*ds) with qa the mean of its ends' states;
+// each boundary edge contributes (5 p1 + p2)/6 and (p1 + 5 p2)/6 times half
+// its rotated edge vector to its two ends; each vertex sums its interior
+// edges in iedge order, then its boundary edges in beindx order (the flux
+// pass's incidence lists), and divides by its dual-cell area.  The
+// reference's print of every vertex (gradient.f:60) is left out.
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(kBlockVerts) k_gradient_edge(ArenaPtrs<R> A) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  Grad<R> *s_g = reinterpret_cast<Grad<R> *>(smem_raw);   // [max_slots]
+  int w0, nwork;
+  work_range(A, w0, nwork);
+  for (int w = w0 + blockIdx.x; w < nwork; w += gridDim.x) {
+    const BlockInfo bi = A.blocks[A.work[w]];
+    const MeshCtl &ctl = A.ctl[bi.mesh];
+    const R4<R> *P = A.st[ctl.phase];
+    for (int k = threadIdx.x; k < bi.ne; k += blockDim.x) {
+      const int2 nn = A.be_nodes[bi.e0 + k];
+      const double2 ds = A.be_ds[bi.e0 + k];
+      const R4<R> p1 = P[nn.x], p2 = P[nn.y];
+      Grad<R> g;
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const R qa = R(0.5) * (comp(p1, q) + comp(p2, q));
+        g.qx[q] = qa * R(ds.x);
+        g.qy[q] = qa * R(ds.y);
+      }
+      s_g[k] = g;
+    }
+    for (int k = threadIdx.x; k < bi.nb; k += blockDim.x) {
+      const int4 b = A.bb_nodes[bi.b0 + k];
+      const double2 x1 = A.coord[b.x], x2 = A.coord[b.y];
+      const R dx = R(x2.x - x1.x), dy = R(x2.y - x1.y);
+      const R nx = R(0.5) * dy, ny = -R(0.5) * dx;
+      const R4<R> p1 = P[b.x], p2 = P[b.y];
+      Grad<R> g1, g2;
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const R qa1 = (R(5) * comp(p1, q) + comp(p2, q)) / R(6);
+        const R qa2 = (comp(p1, q) + R(5) * comp(p2, q)) / R(6);
+        g1.qx[q] = qa1 * nx;
+        g1.qy[q] = qa1 * ny;
+        g2.qx[q] = qa2 * nx;
+        g2.qy[q] = qa2 * ny;
+      }
+      s_g[bi.ne + 2 * k] = g1;
+      s_g[bi.ne + 2 * k + 1] = g2;
+    }
+    __syncthreads();
+    if (threadIdx.x < bi.nv) {
+      const int v = bi.v0 + threadIdx.x;
+      R qx[4] = {R(0), R(0), R(0), R(0)}, qy[4] = {R(0), R(0), R(0), R(0)};
+      const int2 jr = A.ve_rng[v];
+      for (int j = jr.x; j < jr.y; j++) {
+        const uint16_t e = A.ve_list[j];
+        const Grad<R> g = s_g[e & kSlotMask];
+        if (e & kNegBit) {      // n2 of an interior edge
+#pragma unroll
+          for (int q = 0; q < 4; q++) {
+            qx[q] = qx[q] - g.qx[q];
+            qy[q] = qy[q] - g.qy[q];
+          }
+        } else {
+#pragma unroll
+          for (int q = 0; q < 4; q++) {
+            qx[q] = qx[q] + g.qx[q];
+            qy[q] = qy[q] + g.qy[q];
+          }
+        }
+      }
+      const R ai = R(1) / v_cvarea(A, v);
+      Grad<R> g;
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        g.qx[q] = ai * qx[q];
+        g.qy[q] = ai * qy[q];
+      }
+      A.grad[v] = g;
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// shockind.f:1-52 (never called by the reference), routine mode: the
+// density-jump indicator of every vertex from all its edges (edge order),
+// ind/drmin/cvarea**0.75; the gradients of vertices where it exceeds 1 are
+// set to zero.  One thread per vertex; each edge's term is formed by both
+// of its ends with the same operations, so both add the same value.
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(kBlockVerts) k_shockind(ArenaPtrs<R> A) {
+  int w0, nwork;
+  work_range(A, w0, nwork);
+  for (int w = w0 + blockIdx.x; w < nwork; w += gridDim.x) {
+    const BlockInfo bi = A.blocks[A.work[w]];
+    if (threadIdx.x >= bi.nv) continue;
+    const MeshCtl &ctl = A.ctl[bi.mesh];
+    const MeshConst &mc = A.mc[bi.mesh];
+    const int v = bi.v0 + threadIdx.x;
+    const R4<R> *P = A.st[ctl.phase];
+    const R a11 = MCR(R, albada11), a12 = MCR(R, albada12);
+    R ind = R(0);
+    const int2 r = A.va_rng[v];
+    for (int j = r.x; j < r.y; j++) {
+      const int raw = A.va_list[j];
+      const int o = raw & 0x7fffffff;
+      const bool is_n2 = raw < 0;
+      const int n1 = is_n2 ? o : v, n2 = is_n2 ? v : o;
+      const double2 c1 = A.coord[n1], c2 = A.coord[n2];
+      const R dx = R(c2.x - c1.x), dy = R(c2.y - c1.y);
+      const R r1 = P[n1].x, r2 = P[n2].x;
+      const Grad<R> g1 = A.grad[n1], g2 = A.grad[n2];
+      const R dvc = r2 - r1;
+      R dvt = dx * g1.qx[0] + dy * g1.qy[0];
+      const R dvl = a11 * dvt + a12 * dvc;
+      const R vl = r1 + dvl;
+      dvt = dx * g2.qx[0] + dy * g2.qy[0];
+      const R dvr = a11 * dvt + a12 * dvc;
+      const R vr = r2 - dvr;
+      const R li = sq(vr - vl) * R(A.va_dsl[j]);
+      ind = ind + li;
+    }
+    ind = ind / v_drmin(A, v) / mpow(v_cvarea(A, v), R(0.75));
+    if (ind > R(1)) {
+      Grad<R> z;
+#pragma unroll
+      for (int q = 0; q < 4; q++) z.qx[q] = z.qy[q] = R(0);
+      A.grad[v] = z;
+    }
+  }
+}
+
 template <typename R>
 __global__ void __launch_bounds__(kBlockVerts) k_limitgrad(ArenaPtrs<R> A) {
   int w0, nwork;

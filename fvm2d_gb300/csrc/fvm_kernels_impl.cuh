@@ -156,6 +156,16 @@ inline int fit_grid(const LaunchCfg &c, K kern, size_t smem, int threads = kBloc
     k_routine_monitor<R><<<1, 256, 0, c.stream>>>(A, mesh, 1, 0, serial);                   \
     return cudaGetLastError();                                                             \
   }                                                                                        \
+  cudaError_t launch_gradient_edge(const ArenaPtrs<R> &A, const LaunchCfg &c) {             \
+    const size_t sm = size_t(c.max_slots) * sizeof(Grad<R>);                                 \
+    if (sm > kMaxSmem) return cudaErrorInvalidConfiguration;                              \
+    k_gradient_edge<R><<<c.grid, kBlockVerts, sm, c.stream>>>(A);                          \
+    return cudaGetLastError();                                                             \
+  }                                                                                        \
+  cudaError_t launch_shockind(const ArenaPtrs<R> &A, const LaunchCfg &c) {                  \
+    k_shockind<R><<<c.grid, kBlockVerts, 0, c.stream>>>(A);                                \
+    return cudaGetLastError();                                                             \
+  }                                                                                        \
   cudaError_t launch_limitgrad(const ArenaPtrs<R> &A, const LaunchCfg &c) {                 \
     k_limitgrad<R><<<c.grid, kBlockVerts, 0, c.stream>>>(A);                               \
     return cudaGetLastError();                                                             \
@@ -189,6 +199,9 @@ inline int fit_grid(const LaunchCfg &c, K kern, size_t smem, int threads = kBloc
     const size_t gb = grad_bulk_layout(c.max_tri, kTriLocMax, c.viscous).total;            \
     if (e == cudaSuccess && sizeof(R) == 4 && gb <= kMaxSmem)                              \
       e = cudaFuncSetAttribute(k_grad_bulk<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gb); \
+    const size_t ge = size_t(c.max_slots) * sizeof(Grad<R>);                                 \
+    if (e == cudaSuccess && ge <= kMaxSmem)                                                \
+      e = cudaFuncSetAttribute(k_gradient_edge<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ge); \
     const int pmax = (int)(kMaxSmem - kPipeStaticSmem);                                    \
     if (e == cudaSuccess && sizeof(R) == 4)                                                \
       e = cudaFuncSetAttribute(k_grad_pipe<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, pmax); \

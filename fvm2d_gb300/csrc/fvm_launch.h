@@ -61,6 +61,8 @@ inline int pipe_stage_count(uint32_t stage_bytes, int groups, int want) {
   cudaError_t launch_conres(const ArenaPtrs<R> &A, const LaunchCfg &c, int mesh, int first);\
   cudaError_t launch_clcd(const ArenaPtrs<R> &A, const LaunchCfg &c, int mesh, int serial);\
   cudaError_t launch_limitgrad(const ArenaPtrs<R> &A, const LaunchCfg &c);                 \
+  cudaError_t launch_gradient_edge(const ArenaPtrs<R> &A, const LaunchCfg &c);             \
+  cudaError_t launch_shockind(const ArenaPtrs<R> &A, const LaunchCfg &c);                  \
   size_t smem_grad(const LaunchCfg &c, R *);                                              \
   size_t smem_flux(const LaunchCfg &c, R *);                                              \
   size_t smem_sa(const LaunchCfg &c, R *);                                                \

@@ -209,6 +209,14 @@ class Solver:
     def sa_model(self):
         check(L.lib().fvm_gpu_sa_model(self.h), "sa_model")
 
+    def gradient(self):
+        """gradient.f: edge-based Green-Gauss gradients (read with get_state)."""
+        check(L.lib().fvm_gpu_gradient(self.h), "fvm_gpu_gradient")
+
+    def shockind(self):
+        """shockind.f: zero the gradients where the shock indicator exceeds 1."""
+        check(L.lib().fvm_gpu_shockind(self.h), "fvm_gpu_shockind")
+
     def limitgrad(self):
         check(L.lib().fvm_gpu_limitgrad(self.h), "limitgrad")
 

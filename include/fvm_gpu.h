@@ -190,6 +190,17 @@ int32_t fvm_gpu_residu(fvm_handle *h);                   /* residu.f:2-91     */
 int32_t fvm_gpu_update(fvm_handle *h, int32_t irk);      /* update.f:5-38     */
 int32_t fvm_gpu_sa_model(fvm_handle *h);                 /* sa_model.f:3-25   */
 int32_t fvm_gpu_limitgrad(fvm_handle *h);                /* limitgrad.f:1-78  */
+/* gradient.f:1-63, never called by the reference (main.f:29 comments it
+ * out): edge-based Green-Gauss gradients over the dual cells (interior edges
+ * in iedge order, then boundary edges in beindx order with the 5/6, 1/6
+ * closure), divided by cvarea; they replace the handle's gradients (read
+ * them with fvm_gpu_get_state).  Boundary edges other than solid and
+ * farfield are not represented (the reference's grids have none). */
+int32_t fvm_gpu_gradient(fvm_handle *h);
+/* shockind.f:1-52, never called by the reference: the density-jump
+ * indicator over all edges from the handle's current gradients; the
+ * gradients of vertices where it exceeds 1 are set to zero. */
+int32_t fvm_gpu_shockind(fvm_handle *h);
 int32_t fvm_gpu_check_positivity(fvm_handle *h,
                                  int32_t *bad_point);    /* check_positivity.f */
 int32_t fvm_gpu_clcd(fvm_handle *h, double *cl, double *cd);   /* clcd.f:4-49 */

@@ -1201,6 +1201,90 @@ void orc_limitgrad(orc_t *o) {
 }
 
 /* ------------------------------------------------------------------ */
+/* gradient.f:1-63 (never called by the reference: main.f:29 comments   */
+/* it out).  The print of every vertex (gradient.f:60) is left out.     */
+/* ------------------------------------------------------------------ */
+void orc_gradient(orc_t *o) {
+  int np = o->s.np;
+  for (int i = 1; i <= np; i++)
+    for (int j = 1; j <= NVAR; j++) {
+      QX(j, i) = 0.0;
+      QY(j, i) = 0.0;
+    }
+  for (int i = 1; i <= o->s.ne; i++) {            /* interior non-zero edges */
+    int ie = V1(o->iedge, i);
+    int n1 = EDGE(1, ie), n2 = EDGE(2, ie);
+    for (int j = 1; j <= NVAR; j++) {
+      double qa = 0.5 * (PRIM(j, n1) + PRIM(j, n2));
+      double tmpx = qa * DS(1, ie);
+      double tmpy = qa * DS(2, ie);
+      QX(j, n1) = QX(j, n1) + tmpx;
+      QY(j, n1) = QY(j, n1) + tmpy;
+      QX(j, n2) = QX(j, n2) - tmpx;
+      QY(j, n2) = QY(j, n2) - tmpy;
+    }
+  }
+  for (int i = 1; i <= o->s.nbe; i++) {           /* all boundary edges */
+    int ie = V1(o->beindx, i);
+    int n1 = EDGE(1, ie), n2 = EDGE(2, ie);
+    double dx = COORD(1, n2) - COORD(1, n1);
+    double dy = COORD(2, n2) - COORD(2, n1);
+    double nx = 0.5 * dy;
+    double ny = -0.5 * dx;
+    for (int j = 1; j <= NVAR; j++) {
+      double qa1 = (5.0 * PRIM(j, n1) + PRIM(j, n2)) / 6.0;
+      double qa2 = (PRIM(j, n1) + 5.0 * PRIM(j, n2)) / 6.0;
+      QX(j, n1) = QX(j, n1) + qa1 * nx;
+      QY(j, n1) = QY(j, n1) + qa1 * ny;
+      QX(j, n2) = QX(j, n2) + qa2 * nx;
+      QY(j, n2) = QY(j, n2) + qa2 * ny;
+    }
+  }
+  for (int i = 1; i <= np; i++) {                 /* divide by area */
+    double ai = 1.0 / V1(o->cvarea, i);
+    for (int j = 1; j <= NVAR; j++) {
+      QX(j, i) = ai * QX(j, i);
+      QY(j, i) = ai * QY(j, i);
+    }
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* shockind.f:1-52 (never called by the reference)                      */
+/* ------------------------------------------------------------------ */
+void orc_shockind(orc_t *o, double *ind_out) {
+  int np = o->s.np;
+  double *ind = (double *)malloc(sizeof(double) * (size_t)np);
+  for (int i = 1; i <= np; i++) V1(ind, i) = 0.0;
+  for (int i = 1; i <= o->s.netot; i++) {
+    int n1 = EDGE(1, i), n2 = EDGE(2, i);
+    double dx = COORD(1, n2) - COORD(1, n1);
+    double dy = COORD(2, n2) - COORD(2, n1);
+    double dvc = PRIM(1, n2) - PRIM(1, n1);
+    double dvt = dx * QX(1, n1) + dy * QY(1, n1);
+    double dvl = o->s.albada11 * dvt + o->s.albada12 * dvc;
+    double vl = PRIM(1, n1) + dvl;
+    dvt = dx * QX(1, n2) + dy * QY(1, n2);
+    double dvr = o->s.albada11 * dvt + o->s.albada12 * dvc;
+    double vr = PRIM(1, n2) - dvr;
+    double ln = sqrt(sq(DS(1, i)) + sq(DS(2, i)));
+    double li = sq(vr - vl) * ln;
+    V1(ind, n1) = V1(ind, n1) + li;
+    V1(ind, n2) = V1(ind, n2) + li;
+  }
+  for (int i = 1; i <= np; i++) {
+    V1(ind, i) = V1(ind, i) / V1(o->drmin, i) / pow(V1(o->cvarea, i), 0.75);
+    if (V1(ind, i) > 1.0)
+      for (int j = 1; j <= NVAR; j++) {
+        QX(j, i) = 0.0;
+        QY(j, i) = 0.0;
+      }
+  }
+  if (ind_out) memcpy(ind_out, ind, sizeof(double) * (size_t)np);
+  free(ind);
+}
+
+/* ------------------------------------------------------------------ */
 /* monitors: check_positivity.f, clcd.f, conres.f                       */
 /* ------------------------------------------------------------------ */
 int32_t orc_check_positivity(orc_t *o) {

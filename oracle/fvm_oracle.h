@@ -86,6 +86,12 @@ void orc_residu(orc_t *o);
 void orc_update(orc_t *o, int32_t irk);
 void orc_sa_model(orc_t *o);
 void orc_limitgrad(orc_t *o);
+/* gradient.f and shockind.f (both uncalled by the reference): edge-based
+ * Green-Gauss gradients with the boundary closure into qx, qy; the shock
+ * indicator, zeroing the gradients where it exceeds 1 (ind, length np,
+ * may be NULL). */
+void orc_gradient(orc_t *o);
+void orc_shockind(orc_t *o, double *ind);
 int32_t orc_check_positivity(orc_t *o);      /* first bad point or 0 */
 void orc_clcd(orc_t *o);
 int32_t orc_conres(orc_t *o);                /* ORC_OK or ZERO_FIRST_RES */

@@ -80,8 +80,9 @@ def lib():
         L.orc_iarray.restype = pi
         L.orc_iarray.argtypes = [vp, C.c_char_p, C.POINTER(C.c_int64)]
         for n in ["orc_save_old", "orc_time_step", "orc_residu", "orc_sa_model",
-                  "orc_limitgrad", "orc_clcd"]:
+                  "orc_limitgrad", "orc_clcd", "orc_gradient"]:
             getattr(L, n).argtypes = [vp]
+        L.orc_shockind.argtypes = [vp, pd]
         L.orc_update.argtypes = [vp, i32]
         L.orc_check_positivity.argtypes = [vp]
         L.orc_check_positivity.restype = i32
@@ -191,6 +192,17 @@ class Oracle:
 
     def limitgrad(self):
         lib().orc_limitgrad(self.h)
+
+    def gradient(self):
+        """gradient.f: edge-based Green-Gauss gradients into qx, qy."""
+        lib().orc_gradient(self.h)
+
+    def shockind(self):
+        """shockind.f: returns the indicator per vertex; zeroes qx, qy where
+        it exceeds 1."""
+        ind = np.zeros(self.scalars()["np"])
+        lib().orc_shockind(self.h, ind.ctypes.data_as(C.POINTER(C.c_double)))
+        return ind
 
     def check_positivity(self) -> int:
         return lib().orc_check_positivity(self.h)

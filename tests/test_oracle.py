@@ -220,3 +220,46 @@ def test_whole_scheme_rotational_invariance(oracle_lib):
     np.testing.assert_allclose(hb["fres"], ha["fres"], rtol=1e-8)
     np.testing.assert_allclose(hb["cl"], ha["cl"], rtol=1e-8, atol=1e-12)
     np.testing.assert_allclose(hb["cd"], ha["cd"], rtol=1e-8, atol=1e-12)
+
+
+def test_edge_gradient_linear(oracle_lib, small_grid):
+    """gradient.f (edge-based Green-Gauss over the dual cells with the 5/6,
+    1/6 boundary closure) is exact for linear fields at every vertex,
+    boundary vertices included."""
+    g = naca_ogrid(64, 24, jitter=0.1, seed=3)
+    o = oracle_lib.Oracle(g.coord, g.elem, g.ptype)
+    c = o.d("coord")
+    prim = o.d("prim")
+    a = np.array([0.3, -1.2, 0.7, 2.0])
+    bx = np.array([1.5, 0.2, -0.4, 0.9])
+    by = np.array([-0.6, 1.1, 0.3, -2.0])
+    prim[:] = a + np.outer(c[:, 0], bx) + np.outer(c[:, 1], by)
+    o.gradient()
+    assert np.abs(o.d("qx") - bx).max() < 1e-9
+    assert np.abs(o.d("qy") - by).max() < 1e-9
+
+
+def test_shock_indicator(oracle_lib):
+    """shockind.f: a uniform state gives an indicator at rounding level
+    (the edge gradients of a constant are rounding noise) and keeps every
+    gradient; a density step gives an indicator above 1 next to the step,
+    where the gradients are then zero, and leaves them elsewhere."""
+    g = naca_ogrid(64, 24, jitter=0.1, seed=3)
+    o = oracle_lib.Oracle(g.coord, g.elem, g.ptype)
+    o.gradient()
+    qx0 = o.d("qx").copy()
+    ind = o.shockind()
+    assert np.all(ind < 1e-12)
+    np.testing.assert_array_equal(o.d("qx"), qx0)
+    prim = o.d("prim")
+    c = o.d("coord")
+    prim[:, 0] = np.where(c[:, 0] > 0.5, 1.5, 1.0)          # a density step at x = 0.5
+    o.gradient()
+    qx0 = o.d("qx").copy()
+    ind = o.shockind()
+    assert np.all(ind >= 0.0)
+    hit = ind > 1.0
+    near = np.abs(c[:, 0] - 0.5) < 0.2
+    assert hit.any() and np.all(near[hit])
+    np.testing.assert_array_equal(o.d("qx")[hit], 0.0)
+    np.testing.assert_array_equal(o.d("qx")[~hit], qx0[~hit])
