@@ -62,13 +62,18 @@ __device__ __forceinline__ R limit_albada(R ul, R ur, R eps) {
   return top / bot;
 }
 // FP32: the same value without a branch (bot >= 2 eps > 0), so the warp
-// does not diverge on the sign test
+// does not diverge on the sign test, and with the numerator factored:
+// (ul^2 + eps) ur + (ur^2 + eps) ul = (ul + ur)(ul ur + eps), the same value
+// in fewer operations, the product reused for the sign test (the flux pass
+// 0.206 -> 0.200 ms on 8 x 1024x384).  Its FP32 rounding differs from the
+// written order, which the FP64 form keeps.
 template <>
 __device__ __forceinline__ float limit_albada<float>(float ul, float ur, float eps) {
-  const float top = (sq(ul) + eps) * ur + (sq(ur) + eps) * ul;
-  const float bot = sq(ul) + sq(ur) + 2.0f * eps;
+  const float p = ul * ur;
+  const float top = (ul + ur) * (p + eps);
+  const float bot = fmaf(ul, ul, fmaf(ur, ur, 2.0f * eps));
   const float r = __fdividef(top, bot);
-  return (ul * ur <= 0.0f) ? 0.0f : r;
+  return (p <= 0.0f) ? 0.0f : r;
 }
 
 // recon.f:4-50 for one variable
