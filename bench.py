@@ -795,7 +795,7 @@ def main():
     ap.add_argument("--rate", type=float, default=20.0)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--arena-vertices", type=int, default=6_000_000)
-    ap.add_argument("--chunk", type=int, default=50)
+    ap.add_argument("--chunk", type=int, default=100)
     ap.add_argument("--workers", type=int, default=8)
     ap.add_argument("--max-iter", type=int, default=5000)
     ap.add_argument("--minres", type=float, default=1e-6)
