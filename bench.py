@@ -637,7 +637,7 @@ def run_serve(args):
 
 
 ACCURACY_CASES = [
-    # (name, workload grid, flow, iterations)
+    # (name, workload grid, flow, iterations; see STOP_RULES for --stop-rules)
     ("config1 euler 160x48 roe", "euler_160x48", dict(mach=0.8, aoa_deg=1.25, cfl=1.0, iflux=1), 2000),
     ("config2 euler 1024x384 roe", "euler_1024x384", dict(mach=0.8, aoa_deg=1.25, cfl=1.0, iflux=1), 2000),
     ("config2 euler 1024x384 kfvs", "euler_1024x384", dict(mach=0.8, aoa_deg=1.25, cfl=1.0, iflux=2), 2000),
@@ -647,6 +647,13 @@ ACCURACY_CASES = [
     ("config4 rans-sa 768x256 hllc", "rans_768x256",
      dict(iflow=3, mach=0.7, aoa_deg=2.0, rey=6.5e6, cfl=0.5, iflux=3, nut_ratio=3.0), 1000),
 ]
+
+
+# The single-mesh workloads' own stop rules, as (iteration cap, residual drop):
+# 160x48 2000 iterations; 1024x384 5000 iterations or a drop of 1e-8; 512x192
+# laminar a drop of 1e-7 (no cap given: 5000 here); 768x256 RANS-SA 20000
+# iterations or a drop of 1e-6.
+STOP_RULES = [(2000, 0.0), (5000, 1e-8), (5000, 1e-8), (5000, 1e-8), (5000, 1e-7), (20000, 1e-6)]
 
 
 def run_accuracy(args):
@@ -672,9 +679,14 @@ def run_accuracy(args):
         b = Batch(prec, vertices=sum(m.np for m in meshes), meshes=len(meshes), viscous=True)
         pars = [F.make_params(precision=prec, bugcompat=0, **f) for f in flows]
         slots = [b.add(p, m) for p, m in zip(pars, meshes)]
-        nmax = [c[3] for c in ACCURACY_CASES]
-        for s, n in zip(slots, nmax):
-            b.start(s, n)
+        if args.stop_rules:
+            nmax = [r[0] for r in STOP_RULES]
+            drops = [r[1] for r in STOP_RULES]
+        else:
+            nmax = [c[3] for c in ACCURACY_CASES]
+            drops = [0.0] * len(nmax)
+        for s, n, dr in zip(slots, nmax, drops):
+            b.start(s, n, dr)
         hist = [dict(fres=[], cl=[], cd=[]) for _ in slots]
         done = [0] * len(slots)
         t0 = time.perf_counter()
@@ -707,6 +719,7 @@ def run_accuracy(args):
         tail = min(256, k)
         cases.append({
             "case": name, "vertices": meshes[j].np, "iterations": k,
+            "iterations_fp64_fp32": [len(r64["hist"]["fres"]), len(r32["hist"]["fres"])],
             "status": [r64["poll"]["status"], r32["poll"]["status"]],
             "fres_final": [float(f64[-1]), float(f32[-1])] if k else None,
             "fres_max_rel_err": float(np.max(np.abs(f32 - f64) / np.abs(f64))) if k else None,
@@ -722,7 +735,9 @@ def run_accuracy(args):
         })
     out.update({"mode": "accuracy", "targets": {"cl": 1e-4, "cd": 2e-5},
                 "what": "FP32 batch vs FP64 batch (bitwise the serial FP64 oracle's arithmetic), "
-                        "same grids, same iteration counts", "cases": cases})
+                        "same grids; " + ("each run to its workload's stop rule (STOP_RULES)"
+                                          if args.stop_rules else "the same iteration counts"),
+                "cases": cases})
     print(json.dumps(out), flush=True)
 
 
@@ -806,6 +821,8 @@ def main():
     ap.add_argument("--fp64-sample", type=int, default=4,
                     help="serving: requests re-solved on the plain FP64 path")
     ap.add_argument("--rids", default="", help="fp64-solves: request ids")
+    ap.add_argument("--stop-rules", action="store_true",
+                    help="accuracy: run each case to its workload's stop rule (STOP_RULES)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
