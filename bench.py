@@ -727,6 +727,10 @@ def run_accuracy(args):
             "cl": [r64["poll"]["cl"], r32["poll"]["cl"]], "cd": [r64["poll"]["cd"], r32["poll"]["cd"]],
             "abs_err_cl": abs(r64["poll"]["cl"] - r32["poll"]["cl"]),
             "abs_err_cd": abs(r64["poll"]["cd"] - r32["poll"]["cd"]),
+            "cl_tail": [float(np.mean(r64["hist"]["cl"][k - tail:k])),
+                        float(np.mean(r32["hist"]["cl"][k - tail:k]))] if k else None,
+            "cd_tail": [float(np.mean(r64["hist"]["cd"][k - tail:k])),
+                        float(np.mean(r32["hist"]["cd"][k - tail:k]))] if k else None,
             "abs_err_cl_tail_mean": float(abs(np.mean(r64["hist"]["cl"][k - tail:k]) -
                                               np.mean(r32["hist"]["cl"][k - tail:k]))) if k else None,
             "abs_err_cd_tail_mean": float(abs(np.mean(r64["hist"]["cd"][k - tail:k]) -
