@@ -163,3 +163,25 @@ def test_converged_naca0012_transonic_lift_and_drag(fvm_lib):
     cl32, cd32 = out[L.FP32]
     assert abs(cl64 - 0.3214) < 2e-3 and abs(cd64 - 0.02234) < 2e-4
     assert abs(cl32 - cl64) < 1e-3 and abs(cd32 - cd64) < 2e-4
+
+
+def test_amdba_grid_file_through_the_gpu_path(oracle_lib, fvm_lib, tmp_path):
+    """The grid input path (read_grid.f:19-94 layout): a jittered O-grid
+    written as an amdba text file and read back drives the host geometry
+    chain and the FP64 GPU solve to the oracle's history and state, bit for
+    bit, as the in-memory grid does."""
+    from fvm2d_gb300.ogrid import naca_ogrid, read_amdba, write_amdba
+    g = naca_ogrid(96, 40, jitter=0.1, seed=11)
+    p = tmp_path / "grid.amdba"
+    write_amdba(str(p), g)
+    h = read_amdba(str(p))
+    np.testing.assert_array_equal(h.coord, g.coord)
+    mesh = fvm_lib.build_geometry(h.coord, h.elem, h.ptype)
+    s = fvm_lib.Solver(fvm_lib.make_params(precision=L.FP64, iflux=L.ROE, **EULER), mesh)
+    st, hist = s.iterate(30)
+    o = oracle_lib.Oracle(g.coord, g.elem, g.ptype, iflux=L.ROE, **EULER)
+    ost, ohist = o.iterate(30)
+    assert st == ost == 0
+    np.testing.assert_array_equal(hist["iresi"], ohist["iresi"])
+    assert rel_err(hist["fres"], ohist["fres"]) <= REDUCTION_RTOL
+    np.testing.assert_array_equal(s.get_state()["prim"], o.d("prim"))
