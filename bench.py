@@ -789,6 +789,7 @@ def run_probe(args):
 
 
 def main():
+    from fvm2d_gb300.batch import Batch   # form names only: loads no library
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=1000)
@@ -798,9 +799,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--quick", action="store_true", help="skip the side measurements")
     ap.add_argument("--form", default=None,
-                    choices=["bulk", "loads", "vertex", "fused", "split+overlap", "fused+overlap",
-                             "split+overlap4", "split+overlap8", "pipe", "pipe+overlap",
-                             "pipe+overlap4"],
+                    choices=list(Batch.TUNE_CANDIDATES),
                     help="use this form of the iteration instead of the autotuner's choice")
     ap.add_argument("--mode", choices=["throughput", "serve", "accuracy", "probe", "fp64-solves"],
                     default="throughput")

@@ -926,6 +926,120 @@ __device__ __forceinline__ void edge_flux(const ArenaPtrs<R> &A, const FluxConst
   }
 }
 
+// Phase 1b of the flux pass: boundary edges, two slots each (contribution
+// to n1, to n2) after the block's ne interior slots.
+template <typename R>
+__device__ __forceinline__ void flux_boundary(const ArenaPtrs<R> &A, const MeshConst &mc,
+                                              const MeshCtl &ctl, const BlockInfo &bi,
+                                              const R4<R> *P, R4<R> *s_flux) {
+  for (int k = threadIdx.x; k < bi.nb; k += blockDim.x) {
+    const int4 b = A.bb_nodes[bi.b0 + k];
+    const double2 x1 = A.coord[b.x], x2 = A.coord[b.y];
+    const R4<R> p1 = P[b.x], p2 = P[b.y];
+    R4<R> o1, o2;
+    if (b.z == 1) {
+      // solid_flux.f:10-17
+      const R sx = R(0.5) * R(x2.y - x1.y);
+      const R sy = -R(0.5) * R(x2.x - x1.x);
+      const R pp1 = R(0.75) * p1.w + R(0.25) * p2.w;
+      const R pp2 = R(0.25) * p1.w + R(0.75) * p2.w;
+      o1.x = R(0);
+      o1.y = pp1 * sx;
+      o1.z = pp1 * sy;
+      o1.w = R(0);
+      o2.x = R(0);
+      o2.y = pp2 * sx;
+      o2.z = pp2 * sy;
+      o2.w = R(0);
+    } else {
+      R f1[4], f2[4];
+      farfield_flux<R>(mc, ctl.cl, x1, x2, p1, p2, f1, f2);
+      o1.x = f1[0];
+      o1.y = f1[1];
+      o1.z = f1[2];
+      o1.w = f1[3];
+      o2.x = f2[0];
+      o2.y = f2[1];
+      o2.z = f2[2];
+      o2.w = f2[3];
+    }
+    s_flux[bi.ne + 2 * k] = o1;
+    s_flux[bi.ne + 2 * k + 1] = o2;
+  }
+}
+
+// Phase 2 of the flux pass: one thread per vertex sums its edge slots in
+// Fortran order, then writes the residual (MODE_RESIDUAL) or applies the RK
+// stage (MODE_UPDATE); at stage 3 the block's conres partial follows.
+template <typename R>
+__device__ __forceinline__ void flux_gather(const ArenaPtrs<R> &A, const MeshConst &mc,
+                                            MeshCtl &ctl, const BlockInfo &bi, const R4<R> *P,
+                                            const R4<R> *s_flux, int p, int stage, int mode,
+                                            int irk, int routine, double *s_red, double *s_max,
+                                            int *s_arg) {
+  bool have = false;
+  R rho_new = R(0), rho_old = R(0);
+  int org = 0;
+  if (threadIdx.x < bi.nv) {
+    const int v = bi.v0 + threadIdx.x;
+    R acc[4];
+    if (mc.iflow != 1) {
+      const R4<R> rv = A.resv[v];
+      acc[0] = R(0);
+      acc[1] = rv.y;
+      acc[2] = rv.z;
+      acc[3] = rv.w;
+    } else {
+      acc[0] = acc[1] = acc[2] = acc[3] = R(0);
+    }
+    const int2 jr = A.ve_rng[v];
+    for (int j = jr.x; j < jr.y; j++) {
+      const uint16_t e = A.ve_list[j];
+      const R4<R> f = s_flux[e & kSlotMask];
+      if (e & kSolidBit) {
+        acc[1] = acc[1] + f.y;
+        acc[2] = acc[2] + f.z;
+      } else if (e & kNegBit) {
+        acc[0] = acc[0] - f.x;
+        acc[1] = acc[1] - f.y;
+        acc[2] = acc[2] - f.z;
+        acc[3] = acc[3] - f.w;
+      } else {
+        acc[0] = acc[0] + f.x;
+        acc[1] = acc[1] + f.y;
+        acc[2] = acc[2] + f.z;
+        acc[3] = acc[3] + f.w;
+      }
+    }
+    if (mode == MODE_RESIDUAL) {
+      R4<R> r;
+      r.x = acc[0];
+      r.y = acc[1];
+      r.z = acc[2];
+      r.w = acc[3];
+      A.res[v] = r;
+    } else {
+      const R4<R> po = A.st[old_buf(p, stage)][v];
+      const R4<R> pc = P[v];
+      const bool noslip = (mc.iflow != 1) && (A.vflag[v] & kVtxSolid);
+      const R4<R> pn = rk_update<R>(mc, irk, po, pc, A.dt[v], v_cvarea(A, v), acc, noslip);
+      A.st[out_buf(p, stage)][v] = pn;
+      // iterate mode: stages 2 and 3 start from the viscosity computed here
+      if (!routine && stage < 3 && mc.iflow != 1) next_viscosity<R>(A, mc, ctl, v, pn);
+      if (stage == 3) {
+        // conres.f:14-22 partials and check_positivity.f:13-14 (rho, p)
+        have = true;
+        rho_new = pn.x;
+        rho_old = po.x;
+        org = A.orig[v];
+        if (pn.x <= R(0) || pn.w <= R(0)) atomicMin(&ctl.err_point, org);
+      }
+    }
+  }
+  if (mode == MODE_UPDATE && stage == 3)
+    block_conres_partial<R>(have, rho_new, rho_old, org, s_red, s_max, s_arg, A.part + bi.part);
+}
+
 template <typename R, int FLUX>
 __global__ void __launch_bounds__(sizeof(R) == 4 ? kFluxThreads : kBlockVerts,
                                   sizeof(R) == 4 ? FVM_FLUX_MINB32 : 2)
@@ -977,105 +1091,12 @@ __global__ void __launch_bounds__(sizeof(R) == 4 ? kFluxThreads : kBlockVerts,
       o.w = f[3];
       s_flux[k] = o;
     }
-    // phase 1b: boundary edges, two slots each (contribution to n1, to n2)
-    for (int k = threadIdx.x; k < bi.nb; k += blockDim.x) {
-      const int4 b = A.bb_nodes[bi.b0 + k];
-      const double2 x1 = A.coord[b.x], x2 = A.coord[b.y];
-      const R4<R> p1 = P[b.x], p2 = P[b.y];
-      R4<R> o1, o2;
-      if (b.z == 1) {
-        // solid_flux.f:10-17
-        const R sx = R(0.5) * R(x2.y - x1.y);
-        const R sy = -R(0.5) * R(x2.x - x1.x);
-        const R pp1 = R(0.75) * p1.w + R(0.25) * p2.w;
-        const R pp2 = R(0.25) * p1.w + R(0.75) * p2.w;
-        o1.x = R(0);
-        o1.y = pp1 * sx;
-        o1.z = pp1 * sy;
-        o1.w = R(0);
-        o2.x = R(0);
-        o2.y = pp2 * sx;
-        o2.z = pp2 * sy;
-        o2.w = R(0);
-      } else {
-        R f1[4], f2[4];
-        farfield_flux<R>(mc, ctl.cl, x1, x2, p1, p2, f1, f2);
-        o1.x = f1[0];
-        o1.y = f1[1];
-        o1.z = f1[2];
-        o1.w = f1[3];
-        o2.x = f2[0];
-        o2.y = f2[1];
-        o2.z = f2[2];
-        o2.w = f2[3];
-      }
-      s_flux[bi.ne + 2 * k] = o1;
-      s_flux[bi.ne + 2 * k + 1] = o2;
-    }
+    // phase 1b: boundary edges
+    flux_boundary<R>(A, mc, ctl, bi, P, s_flux);
     if (err) atomicCAS(&ctl.err, 0, 4 /* FVM_ERR_ROE_SONIC */);
     __syncthreads();
     // phase 2: gather per vertex in Fortran order
-    bool have = false;
-    R rho_new = R(0), rho_old = R(0);
-    int org = 0;
-    if (threadIdx.x < bi.nv) {
-      const int v = bi.v0 + threadIdx.x;
-      R acc[4];
-      if (mc.iflow != 1) {
-        const R4<R> rv = A.resv[v];
-        acc[0] = R(0);
-        acc[1] = rv.y;
-        acc[2] = rv.z;
-        acc[3] = rv.w;
-      } else {
-        acc[0] = acc[1] = acc[2] = acc[3] = R(0);
-      }
-      const int2 jr = A.ve_rng[v];
-      for (int j = jr.x; j < jr.y; j++) {
-        const uint16_t e = A.ve_list[j];
-        const R4<R> f = s_flux[e & kSlotMask];
-        if (e & kSolidBit) {
-          acc[1] = acc[1] + f.y;
-          acc[2] = acc[2] + f.z;
-        } else if (e & kNegBit) {
-          acc[0] = acc[0] - f.x;
-          acc[1] = acc[1] - f.y;
-          acc[2] = acc[2] - f.z;
-          acc[3] = acc[3] - f.w;
-        } else {
-          acc[0] = acc[0] + f.x;
-          acc[1] = acc[1] + f.y;
-          acc[2] = acc[2] + f.z;
-          acc[3] = acc[3] + f.w;
-        }
-      }
-      if (mode == MODE_RESIDUAL) {
-        R4<R> r;
-        r.x = acc[0];
-        r.y = acc[1];
-        r.z = acc[2];
-        r.w = acc[3];
-        A.res[v] = r;
-      } else {
-        const R4<R> po = A.st[old_buf(p, stage)][v];
-        const R4<R> pc = P[v];
-        const bool noslip = (mc.iflow != 1) && (A.vflag[v] & kVtxSolid);
-        const R4<R> pn = rk_update<R>(mc, irk, po, pc, A.dt[v], v_cvarea(A, v), acc, noslip);
-        A.st[out_buf(p, stage)][v] = pn;
-        // iterate mode: stages 2 and 3 start from the viscosity computed here
-        if (!routine && stage < 3 && mc.iflow != 1) next_viscosity<R>(A, mc, ctl, v, pn);
-        if (stage == 3) {
-          // conres.f:14-22 partials and check_positivity.f:13-14 (rho, p)
-          have = true;
-          rho_new = pn.x;
-          rho_old = po.x;
-          org = A.orig[v];
-          if (pn.x <= R(0) || pn.w <= R(0)) atomicMin(&ctl.err_point, org);
-        }
-      }
-    }
-    if (mode == MODE_UPDATE && stage == 3)
-      block_conres_partial<R>(have, rho_new, rho_old, org, s_red, s_max, s_arg, A.part + bi.part);
+    flux_gather<R>(A, mc, ctl, bi, P, s_flux, p, stage, mode, irk, routine, s_red, s_max, s_arg);
     __syncthreads();
   }
 }
