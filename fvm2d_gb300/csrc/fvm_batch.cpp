@@ -899,7 +899,7 @@ struct fvm_prepared {
   std::vector<double> ais, cvarea, drmin, wd, elarea;
   std::vector<int> orig;
   std::vector<double2> be_ds;
-  std::vector<EdgeGeo32> be_g32;   // FP32 batches (mesh-local vertex ids)
+  std::vector<EdgeGeo32> be_g32;   // FP32 batches
   std::vector<float2> va_w;        // FP32 batches: Green-Gauss weights per va_list entry
   std::vector<double> va_dsl;      // |ds| of each va_list entry's edge (shockind.f:36)
   std::vector<TriGeo32> tri_g32;   // FP32 batches
@@ -949,16 +949,10 @@ extern "C" int32_t fvm_batch_prepare(const fvm_params *par, const fvm_mesh *m, f
     P->be_ds[k] = make_double2(dsx, dsy);
     // FP32 copies of FP64 quantities, rounded once
     const int n1 = m->edge[2 * e] - 1, n2 = m->edge[2 * e + 1] - 1;
-    const double len = std::sqrt(dsx * dsx + dsy * dsy);   // flux.f:10-13
     EdgeGeo32 g;
-    g.n1 = L.be_nodes[k].x;
-    g.n2 = L.be_nodes[k].y;
-    g.dx = (float)(m->coord[2 * n2] - m->coord[2 * n1]);
-    g.dy = (float)(m->coord[2 * n2 + 1] - m->coord[2 * n1 + 1]);
-    g.ct = (float)(dsx / len);
-    g.st = (float)(dsy / len);
-    g.len = (float)len;
-    g.loc = L.be_loc[k];
+    g.v = make_float4((float)(m->coord[2 * n2] - m->coord[2 * n1]),
+                      (float)(m->coord[2 * n2 + 1] - m->coord[2 * n1 + 1]), (float)dsx,
+                      (float)dsy);
     P->be_g32[k] = g;
   }
   // Green-Gauss as a vertex stencil (FP32 batches).  green_gauss.f:23-39
@@ -1057,7 +1051,7 @@ extern "C" int64_t fvm_prepared_bytes(const fvm_prepared *prep, int32_t precisio
   const int64_t r = precision == FVM_PREC_FP64 ? 8 : 4;
   const int64_t V = L.np;
   int64_t bytes = V * (3 * 4 * r + 8 * r + 4 * r + 4 * r + 5 * r + 16 + 4 * 8 + 4 + 1 + 3 * 8);
-  bytes += (int64_t)L.be_nodes.size() * (8 + 16 + 32);
+  bytes += (int64_t)L.be_nodes.size() * (8 + 16 + (r == 4 ? 16 : 32));
   bytes += (int64_t)L.bb_nodes.size() * 16 + (int64_t)L.bt_nodes.size() * (16 + (r == 4 ? 32 : 0));
   bytes += (int64_t)L.nt * 8 + (int64_t)L.ve_list.size() * 2 + (int64_t)L.vt_list.size() * 2;
   bytes += (int64_t)L.va_list.size() * (12 + (r == 4 ? 8 : 0)) + (int64_t)L.sw_nodes.size() * 8;
@@ -1221,14 +1215,7 @@ static int32_t add_prepared(fvm_batch *b, fvm_prepared *prep, int32_t *slot_out,
   PUT(put_range(b, b->bb_nodes, S.off[P_BB], bb, us));
   PUT(put_range(b, b->bt_nodes, S.off[P_BT], bt, us));
   PUT(put_range(b, b->elarea, S.off[P_TRI], prep->elarea, us));
-  if (b->be_g32) {
-    std::vector<EdgeGeo32> g(prep->be_g32);
-    for (EdgeGeo32 &x : g) {
-      x.n1 += v0;
-      x.n2 += v0;
-    }
-    PUT(put_range(b, b->be_g32, S.off[P_BE], g, us));
-  }
+  if (b->be_g32) PUT(put_range(b, b->be_g32, S.off[P_BE], prep->be_g32, us));
   if (b->tri_g32) PUT(put_range(b, b->tri_g32, S.off[P_BT], prep->tri_g32, us));
   if (b->va_w) PUT(put_range(b, b->va_w, S.off[P_VA], prep->va_w, us));
   PUT(put_range(b, b->va_dsl, S.off[P_VA], prep->va_dsl, us));

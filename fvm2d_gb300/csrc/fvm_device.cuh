@@ -156,6 +156,71 @@ __device__ __forceinline__ bool roe_flux(R ct, R st, R length, const R pl4[4], c
   return ok;
 }
 
+// FP32: the same flux with fewer special-function operations.  The four
+// divisions by the Roe-average sound speed (and its square) become products
+// with one reciprocal square root, which also gives the sound speed
+// (aa = aa2 / sqrt(aa2)); the divisions by gamma - 1 become products with
+// its reciprocal, formed once per call (loop-invariant in the edge loops).
+// Same operations otherwise; FP32 rounding differs from the written order,
+// which the FP64 form keeps.
+template <>
+__device__ __forceinline__ bool roe_flux<float>(float ct, float st, float length,
+                                                const float pl4[4], const float pr4[4],
+                                                float GAMMA, float GAMMA1, float flux[4]) {
+  const float ig1 = __fdividef(1.0f, GAMMA1);
+  const float rl = pl4[0], ul = pl4[1], vl = pl4[2], pl = pl4[3];
+  const float al2 = __fdividef(GAMMA * pl, rl);
+  const float ql2 = ul * ul + vl * vl;
+  const float hl = al2 * ig1 + 0.5f * ql2;
+  const float rr = pr4[0], ur = pr4[1], vr = pr4[2], pr = pr4[3];
+  const float ar2 = __fdividef(GAMMA * pr, rr);
+  const float qr2 = ur * ur + vr * vr;
+  const float hr = ar2 * ig1 + 0.5f * qr2;
+  const float unl = ul * ct + vl * st;
+  const float Fc0 = rl * unl;
+  const float Fc1 = pl * ct + rl * ul * unl;
+  const float Fc2 = pl * st + rl * vl * unl;
+  const float Fc3 = rl * hl * unl;
+  const float rl12 = sqrtf(rl), rr12 = sqrtf(rr);
+  const float rd = __fdividef(1.0f, rl12 + rr12);
+  const float ua = (ul * rl12 + ur * rr12) * rd;
+  const float va = (vl * rl12 + vr * rr12) * rd;
+  const float ha = (hl * rl12 + hr * rr12) * rd;
+  const float qa2 = ua * ua + va * va;
+  const float aa2 = GAMMA1 * (ha - 0.5f * qa2);
+  const bool ok = aa2 > 0.0f;
+  const float iaa = rsqrtf(aa2);
+  const float aa = aa2 * iaa;
+  const float una = ua * ct + va * st;
+  const float vna = -ua * st + va * ct;
+  const float l1 = dmin1(una - aa, 0.0f);
+  const float l2 = dmin1(una, 0.0f);
+  const float l3 = l2;
+  const float l4 = dmin1(una + aa, 0.0f);
+  const float du1 = rr - rl;
+  const float du2 = rr * ur - rl * ul;
+  const float du3 = rr * vr - rl * vl;
+  const float du4 = (pr - pl) * ig1 + 0.5f * (rr * qr2 - rl * ql2);
+  const float m1 = (ct * du2 + st * du3 - una * du1) * iaa;
+  const float m2 = GAMMA1 * (du4 - ua * du2 - va * du3 + qa2 * du1) * (iaa * iaa);
+  const float a4 = 0.5f * (m1 + m2);
+  const float a1 = 0.5f * (m2 - m1);
+  const float a3 = du1 - a1 - a4;
+  const float a2 = (st * du2 - ct * du3 + vna * du1) * iaa;
+  const float a1l1 = a1 * l1, a2l2 = a2 * l2, a3l3 = a3 * l3, a4l4 = a4 * l4;
+  const float aact = aa * ct, aast = aa * st;
+  const float Fd0 = a1l1 + a3l3 + a4l4;
+  const float Fd1 = a1l1 * (ua - aact) + a2l2 * aa * st + a3l3 * ua + a4l4 * (ua + aact);
+  const float Fd2 = a1l1 * (va - aast) - a2l2 * aa * ct + a3l3 * va + a4l4 * (va + aast);
+  const float Fd3 = a1l1 * (ha - una * aa) + a2l2 * aa * vna + a3l3 * 0.5f * qa2 +
+                    a4l4 * (ha + una * aa);
+  flux[0] = (Fc0 + Fd0) * length;
+  flux[1] = (Fc1 + Fd1) * length;
+  flux[2] = (Fc2 + Fd2) * length;
+  flux[3] = (Fc3 + Fd3) * length;
+  return ok;
+}
+
 // --------------------------------------------------------- kfvs_flux.f
 template <typename R>
 __device__ __forceinline__ void kfvs_flux(R ct, R st, R length, const R pl4[4], const R pr4[4],

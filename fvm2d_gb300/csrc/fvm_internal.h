@@ -208,15 +208,12 @@ constexpr int kTriLocBits = 10;
 constexpr int kTriLocMax = 1 << kTriLocBits;
 constexpr uint32_t kTriNoLoc = 0xffffffffu;
 
-// One interior edge entry of a block for the FP32 kernels: its ends, the
-// FP64 edge vector and dual-face normal rounded once to FP32 (flux.f:10-13
-// computes ct, st, len from ds), and the ends' local slots; 32 bytes, read
-// with two 16-byte loads.
+// One interior edge entry of a block for the FP32 kernels (its ends are
+// be_nodes): the FP64 edge vector and dual-face normal ds rounded once to
+// FP32; 16 bytes, one load.  The flux pass forms ct, st, len from ds
+// (flux.f:10-13) itself.
 struct alignas(16) EdgeGeo32 {
-  int n1, n2;          // arena vertex ids
-  float dx, dy;        // x(n2)-x(n1), y(n2)-y(n1)
-  float ct, st, len;   // ds/|ds| and |ds|
-  uint32_t loc;        // local slots of n1 (low half) and n2 (high half)
+  float4 v;            // x(n2)-x(n1), y(n2)-y(n1), ds (flength.f:38-39)
 };
 
 // Device pointers of an arena (all arena-global indices).
@@ -247,7 +244,7 @@ struct ArenaPtrs {
   const int4 *bb_nodes;   // boundary entries (n1, n2, type, -)
   const int4 *bt_nodes;   // triangle entries (n1, n2, n3, arena triangle)
   const double *elarea;   // per arena triangle
-  const EdgeGeo32 *be_g32; // FP32 path: ends, geometry and local slots of each edge entry
+  const EdgeGeo32 *be_g32; // FP32 path: edge vector and ds of each edge entry (ends: be_nodes)
   const float *ais32, *cvarea32, *drmin32, *wd32;   // FP32 path: per-vertex copies
   const TriGeo32 *tri_g32; // FP32 path: per triangle entry of the blocks (bt_* order)
   // solid edges per mesh for clcd (n1, n2) in beindx order

@@ -878,6 +878,45 @@ __device__ __forceinline__ FluxConst<R> flux_const(const MeshConst &mc) {
   return c;
 }
 
+// FP32: the edge's unit normal and length from its ds (flux.f:10-13) with
+// one reciprocal square root.
+__device__ __forceinline__ void edge_normal_f32(float dsx, float dsy, float &ct, float &st,
+                                                float &len) {
+  const float d2 = fmaf(dsx, dsx, dsy * dsy);
+  const float il = rsqrtf(d2);
+  ct = dsx * il;
+  st = dsy * il;
+  len = d2 * il;
+}
+
+// FP32: recon.f:4-50 for the four variables of an edge.  With the limiter,
+// albada21 scales the edge vector once per edge instead of each projected
+// gradient, and albada22 * dq serves both sides; the same values as recon1
+// up to FP32 rounding.
+__device__ __forceinline__ void recon_edge_f32(const R4<float> &p1, const R4<float> &p2,
+                                               const Grad<float> &g1, const Grad<float> &g2,
+                                               float dx, float dy, const FluxConst<float> &fc,
+                                               float pl[4], float pr[4]) {
+  if (fc.ilimit == 1) {
+    const float dxa = fc.a21 * dx, dya = fc.a21 * dy;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const float a = comp(p1, q), b = comp(p2, q);
+      const float dqp = b - a;
+      const float c = fc.a22 * dqp;
+      const float dql = fmaf(dxa, g1.qx[q], fmaf(dya, g1.qy[q], c));
+      const float dqr = fmaf(dxa, g2.qx[q], fmaf(dya, g2.qy[q], c));
+      pl[q] = fmaf(0.5f, limit_albada<float>(dql, dqp, fc.eps), a);
+      pr[q] = fmaf(-0.5f, limit_albada<float>(dqr, dqp, fc.eps), b);
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+      recon1<float>(comp(p1, q), comp(p2, q), g1.qx[q], g1.qy[q], g2.qx[q], g2.qy[q], dx, dy,
+                    fc.ilimit, fc.a11, fc.a12, fc.a21, fc.a22, fc.eps, pl[q], pr[q]);
+  }
+}
+
 // FLUX = 1/2/3 compiles one Riemann solver only (every resident mesh uses
 // it); FLUX = 0 dispatches on the mesh's iflux.
 template <typename R, int FLUX>
@@ -885,13 +924,16 @@ __device__ __forceinline__ void edge_flux(const ArenaPtrs<R> &A, const FluxConst
                                           const R4<R> *P, int e, R f[4], int &err) {
   int2 nn;
   R dx, dy, ct, st, len;
+  float dsx = 0.f, dsy = 0.f;
   if constexpr (sizeof(R) == 4) {
-    // first half of the entry (ends, edge vector) now, the normal after the
-    // reconstruction: fewer values live across it
-    const int4 h = reinterpret_cast<const int4 *>(A.be_g32 + e)[0];
-    nn = make_int2(h.x, h.y);
-    dx = __int_as_float(h.z);
-    dy = __int_as_float(h.w);
+    // ends, edge vector and ds (24 bytes per entry); ds/|ds| and |ds| are
+    // formed after the reconstruction
+    nn = A.be_nodes[e];
+    const float4 h = A.be_g32[e].v;
+    dx = h.x;
+    dy = h.y;
+    dsx = h.z;
+    dsy = h.w;
   } else {
     nn = A.be_nodes[e];
     const double2 c1 = A.coord[nn.x], c2 = A.coord[nn.y];
@@ -901,15 +943,16 @@ __device__ __forceinline__ void edge_flux(const ArenaPtrs<R> &A, const FluxConst
   const R4<R> p1 = P[nn.x], p2 = P[nn.y];
   const Grad<R> g1 = A.grad[nn.x], g2 = A.grad[nn.y];
   R pl[4], pr[4];
-#pragma unroll
-  for (int q = 0; q < 4; q++)
-    recon1<R>(comp(p1, q), comp(p2, q), g1.qx[q], g1.qy[q], g2.qx[q], g2.qy[q], dx, dy,
-              fc.ilimit, fc.a11, fc.a12, fc.a21, fc.a22, fc.eps, pl[q], pr[q]);
   if constexpr (sizeof(R) == 4) {
-    const float4 h = reinterpret_cast<const float4 *>(A.be_g32 + e)[1];
-    ct = h.x;
-    st = h.y;
-    len = h.z;
+    recon_edge_f32(p1, p2, g1, g2, dx, dy, fc, pl, pr);
+  } else {
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+      recon1<R>(comp(p1, q), comp(p2, q), g1.qx[q], g1.qy[q], g2.qx[q], g2.qy[q], dx, dy,
+                fc.ilimit, fc.a11, fc.a12, fc.a21, fc.a22, fc.eps, pl[q], pr[q]);
+  }
+  if constexpr (sizeof(R) == 4) {
+    edge_normal_f32(dsx, dsy, ct, st, len);
   } else {
     const D4 csl = A.be_csl[e];
     ct = R(csl.x);
@@ -1148,6 +1191,7 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_FLUX_MINB32 
         if (sizeof(R) == 4) {
           prefetch_l2(A.tri_g32 + n.t0, sizeof(TriGeo32) * n.nt2);
           prefetch_l2(A.be_g32 + n.e0, sizeof(EdgeGeo32) * n.ne);
+          prefetch_l2(A.be_nodes + n.e0, sizeof(int2) * n.ne);
         } else {
           prefetch_l2(A.coord + n.v0, sizeof(double2) * n.nv);
           prefetch_l2(A.be_csl + n.e0, sizeof(D4) * n.ne);
@@ -1252,14 +1296,12 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_FLUX_MINB32 
       uint32_t ll;
       R dx, dy, ct, st, len;
       if constexpr (sizeof(R) == 4) {
-        const EdgeGeo32 g = A.be_g32[e];
-        nn = make_int2(g.n1, g.n2);
-        ll = g.loc;
-        dx = g.dx;
-        dy = g.dy;
-        ct = g.ct;
-        st = g.st;
-        len = g.len;
+        const float4 g = A.be_g32[e].v;
+        nn = A.be_nodes[e];
+        ll = A.be_loc[e];
+        dx = g.x;
+        dy = g.y;
+        edge_normal_f32(g.z, g.w, ct, st, len);
       } else {
         nn = A.be_nodes[e];
         ll = A.be_loc[e];
@@ -1449,11 +1491,11 @@ __global__ void __launch_bounds__(kBlockVerts) k_sa(ArenaPtrs<R> A, int stage, i
       const int e = bi.e0 + k;
       int2 nn;
       R d1, d2;
-      if constexpr (sizeof(R) == 4) {   // ds = (cos, sin) |ds| from the FP32 record
-        const EdgeGeo32 g = A.be_g32[e];
-        nn = make_int2(g.n1, g.n2);
-        d1 = g.ct * g.len;
-        d2 = g.st * g.len;
+      if constexpr (sizeof(R) == 4) {   // ds from the FP32 record
+        const float4 g = A.be_g32[e].v;
+        nn = A.be_nodes[e];
+        d1 = g.z;
+        d2 = g.w;
       } else {
         nn = A.be_nodes[e];
         const double2 ds = A.be_ds[e];
