@@ -109,6 +109,8 @@ SIGNATURES = {
     "fvm_geom_build": (C.c_int32, [C.c_int32, C.c_int32, _pd, _pi, _pi, C.c_int32,
                                    C.POINTER(C.POINTER(FvmGeom))]),
     "fvm_geom_free": (C.c_int32, [C.POINTER(FvmGeom)]),
+    "fvm_gpu_geom_build": (C.c_int32, [C.c_int32, C.c_int32, _pd, _pi, _pi, C.c_int32,
+                                       C.POINTER(C.POINTER(FvmGeom))]),
     "fvm_batch_create": (C.c_int32, [C.c_int32, C.POINTER(FvmBatchCaps), C.POINTER(C.c_void_p)]),
     "fvm_batch_destroy": (C.c_int32, [C.c_void_p]),
     "fvm_batch_add": (C.c_int32, [C.c_void_p, C.POINTER(FvmParams), C.POINTER(FvmMesh), _pi]),

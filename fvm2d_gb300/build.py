@@ -53,6 +53,7 @@ UNITS = [
         "FVM_FP32_FLAGS", "-prec-div=false -prec-sqrt=false -ftz=true").split()),
     ("fvm_setup.cu", "nvcc", ["--fmad=false"]),
     ("fvm_noalloc.cu", "nvcc", ["--fmad=false"]),
+    ("fvm_geom_gpu.cu", "nvcc", ["--fmad=false"]),
     ("fvm_batch.cpp", "cxx", []),
     ("fvm_serve.cpp", "cxx", []),
     ("fvm_layout.cpp", "cxx", []),

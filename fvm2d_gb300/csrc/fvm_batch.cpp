@@ -89,6 +89,14 @@ struct Slot {
   int64_t len[P_COUNT] = {0};
 };
 
+// math.f:8-40's values of the constants the flux pass uses (as
+// fvm_params_init sets them; pi compared with its correctly rounded double)
+bool standard_constants(const fvm_params &p) {
+  return p.gamma == 1.4 && p.gamma1 == 1.4 - 1.0 && p.albada11 == 2.0 / 3.0 &&
+         p.albada12 == 1.0 - 2.0 / 3.0 && p.albada21 == 4.0 / 3.0 &&
+         p.albada22 == 1.0 - 4.0 / 3.0 && p.epsilon == 1.0e-16 && p.pi == 3.141592653589793;
+}
+
 const char *kKernelNames[] = {"visc", "grad", "flux", "sa", "monitor", "step"};
 enum { K_VISC, K_GRAD, K_FLUX, K_SA, K_MON, K_STEP, K_COUNT };
 
@@ -455,9 +463,10 @@ int32_t update_work(fvm_batch *b) {
   // capacities: smaller tiles let more CTAs share an SM.
   int tile[4] = {0, 0, 0, 0};
   int max_halo = 0;
-  bool any_visc = false, any_turb = false, any_inv = false, tri_loc = true;
+  bool any_visc = false, any_turb = false, any_inv = false, tri_loc = true, std_const = true;
   for (const Slot &s : b->slots)
     if (s.used && !s.staged) {
+      std_const &= standard_constants(s.par);
       any_visc |= s.par.iflow != FVM_INVISCID;
       any_inv |= s.par.iflow == FVM_INVISCID;
       any_turb |= s.par.iflow == FVM_TURBULENT;
@@ -477,7 +486,8 @@ int32_t update_work(fvm_batch *b) {
   b->cfg.tri_loc = tri_loc;
   const int cap[4] = {b->caps.max_tri, b->caps.max_slots, b->caps.max_tri2, b->caps.max_loc};
   int *cur[4] = {&b->cfg.max_tri, &b->cfg.max_slots, &b->cfg.max_tri2, &b->cfg.max_loc};
-  bool changed = flux != b->cfg.flux || changed_halo;
+  bool changed = flux != b->cfg.flux || changed_halo || std_const != b->cfg.std_const;
+  b->cfg.std_const = std_const;
   b->cfg.flux = flux;
   for (int i = 0; i < 4; i++) {
     if (!tile[i]) continue;             // empty batch: keep the current tiles
@@ -856,6 +866,7 @@ extern "C" int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *cap
       (b->cfg.grad_mode >= 3 && (precision != FVM_PREC_FP32 || !bulk_fits)))
     return fail(FVM_ERR_ARG);
   b->cfg.viscous = c.viscous != 0;
+  b->cfg.std_const = false;   // set when meshes are admitted
   b->cfg.stream = b->stream;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);

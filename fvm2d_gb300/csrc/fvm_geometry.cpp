@@ -11,17 +11,26 @@
 // point operation follow those files, so the arrays are identical to the
 // driver's.  Compiled with -ffp-contract=off.
 #include <cmath>
+#include <cstdint>
 #include <cstdlib>
 #include <cstring>
 #include <new>
+#include <utility>
 #include <vector>
 
 #include "../../include/fvm_gpu.h"
+#include "fvm_geom_gpu.h"
 
 namespace {
 
 inline double sqr(double x) { return x * x; }
 inline double maxd(double a, double b) { return b > a ? b : a; }
+
+// flength.f:52 and make_bdedges.f:12 test edneigh(1,i)*edneigh(2,i) .eq. 0:
+// the 32-bit product, formed here in unsigned arithmetic (defined wrap-around)
+inline int boundary_edge(const int32_t *edneigh, int i) {
+  return (uint32_t)edneigh[2 * i] * (uint32_t)edneigh[2 * i + 1] == 0u;
+}
 
 template <typename T>
 T *dup(const std::vector<T> &v) {
@@ -117,6 +126,49 @@ struct GeomOwned {
   std::vector<int32_t> edge, edneigh, iedge, beindx, spts;
   std::vector<double> ds, dsb, elarea, cvarea, mcarea, drmin, wd;
 };
+
+// Points the fvm_geom struct (and its fvm_mesh) at G's arrays.
+static fvm_geom *publish(GeomOwned *G, int32_t np, int32_t nt, int nswe, const double *coord,
+                         int32_t *elem, const int32_t *ptype) {
+  fvm_geom &g = G->g;
+  g.edge = G->edge.data();
+  g.edneigh = G->edneigh.data();
+  g.iedge = G->iedge.data();
+  g.beindx = G->beindx.data();
+  g.spts = G->spts.data();
+  g.ds = G->ds.data();
+  g.dsb = G->dsb.data();
+  g.elarea = G->elarea.data();
+  g.cvarea = G->cvarea.data();
+  g.mcarea = G->mcarea.data();
+  g.drmin = G->drmin.data();
+  g.wd = G->wd.data();
+  fvm_mesh &m = g.mesh;
+  m.np = np;
+  m.nt = nt;
+  m.ne = (int)G->iedge.size();
+  m.netot = (int)(G->edge.size() / 2);
+  m.nsp = (int)G->spts.size();
+  m.nbe = (int)G->beindx.size();
+  m.nswe1 = 1;
+  m.nswe2 = nswe;
+  m.nffe1 = nswe + 1;
+  m.nffe2 = m.nbe;
+  m.coord = coord;
+  m.elem = elem;
+  m.ptype = ptype;
+  m.spts = g.spts;
+  m.edge = g.edge;
+  m.iedge = g.iedge;
+  m.beindx = g.beindx;
+  m.ds = g.ds;
+  m.elarea = g.elarea;
+  m.cvarea = g.cvarea;
+  m.mcarea = g.mcarea;
+  m.drmin = g.drmin;
+  m.wd = g.wd;
+  return &G->g;
+}
 
 extern "C" int32_t fvm_geom_build(int32_t np, int32_t nt, const double *coord, int32_t *elem,
                                   const int32_t *ptype, int32_t cell_type, fvm_geom **out) {
@@ -293,7 +345,7 @@ extern "C" int32_t fvm_geom_build(int32_t np, int32_t nt, const double *coord, i
     G->ds[2 * i + 1] = (x2 - x1);
   }
   for (int i = 0; i < ne_all; i++) {
-    if (G->edneigh[2 * i] * G->edneigh[2 * i + 1] != 0) continue;
+    if (boundary_edge(G->edneigh.data(), i) == 0) continue;
     const int n1 = G->edge[2 * i] - 1, n2 = G->edge[2 * i + 1] - 1;
     const double nx = Y(n2) - Y(n1);
     const double ny = -(X(n2) - X(n1));
@@ -313,7 +365,7 @@ extern "C" int32_t fvm_geom_build(int32_t np, int32_t nt, const double *coord, i
   // make_bdedges.f:9-44: solid edges, then farfield edges
   std::vector<int32_t> ff;
   for (int i = 0; i < ne_all; i++) {
-    if (G->edneigh[2 * i] * G->edneigh[2 * i + 1] != 0) continue;
+    if (boundary_edge(G->edneigh.data(), i) == 0) continue;
     const int t1 = ptype[G->edge[2 * i] - 1], t2 = ptype[G->edge[2 * i + 1] - 1];
     if (t1 == FVM_PT_SOLID && t2 == FVM_PT_SOLID) G->beindx.push_back(i + 1);
     if (t1 == FVM_PT_FARFIELD && t2 == FVM_PT_FARFIELD) ff.push_back(i + 1);
@@ -333,44 +385,39 @@ extern "C" int32_t fvm_geom_build(int32_t np, int32_t nt, const double *coord, i
   G->drmin.assign(np, 0.0);
   G->wd.assign(np, 0.0);
 
-  fvm_geom &g = G->g;
-  g.edge = G->edge.data();
-  g.edneigh = G->edneigh.data();
-  g.iedge = G->iedge.data();
-  g.beindx = G->beindx.data();
-  g.spts = G->spts.data();
-  g.ds = G->ds.data();
-  g.dsb = G->dsb.data();
-  g.elarea = G->elarea.data();
-  g.cvarea = G->cvarea.data();
-  g.mcarea = G->mcarea.data();
-  g.drmin = G->drmin.data();
-  g.wd = G->wd.data();
-  fvm_mesh &m = g.mesh;
-  m.np = np;
-  m.nt = nt;
-  m.ne = (int)G->iedge.size();
-  m.netot = ne_all;
-  m.nsp = (int)G->spts.size();
-  m.nbe = (int)G->beindx.size();
-  m.nswe1 = 1;
-  m.nswe2 = nswe;
-  m.nffe1 = nswe + 1;
-  m.nffe2 = m.nbe;
-  m.coord = coord;
-  m.elem = elem;
-  m.ptype = ptype;
-  m.spts = g.spts;
-  m.edge = g.edge;
-  m.iedge = g.iedge;
-  m.beindx = g.beindx;
-  m.ds = g.ds;
-  m.elarea = g.elarea;
-  m.cvarea = g.cvarea;
-  m.mcarea = g.mcarea;
-  m.drmin = g.drmin;
-  m.wd = g.wd;
-  *out = &G->g;
+  *out = publish(G, np, nt, nswe, coord, elem, ptype);
+  return FVM_OK;
+}
+
+// The same chain on the GPU (fvm_geom_gpu.cu): identical arrays, and drmin
+// (dtlength.f) from the same device arrays.
+extern "C" int32_t fvm_gpu_geom_build(int32_t np, int32_t nt, const double *coord,
+                                      int32_t *elem, const int32_t *ptype, int32_t cell_type,
+                                      fvm_geom **out) {
+  if (!out || np < 3 || nt < 1 || !coord || !elem || !ptype) return FVM_ERR_ARG;
+  if (cell_type != FVM_CELL_MEDIAN && cell_type != FVM_CELL_BARTH) return FVM_ERR_ARG;
+  *out = nullptr;
+  for (int64_t k = 0; k < 3 * (int64_t)nt; k++)
+    if (elem[k] < 1 || elem[k] > np) return FVM_ERR_ARG;
+  fvm::GeomChainOut R;
+  const int32_t st = fvm::geom_chain_gpu(np, nt, coord, elem, ptype, cell_type, R);
+  if (st != FVM_OK) return st;
+  GeomOwned *G = new (std::nothrow) GeomOwned();
+  if (!G) return FVM_ERR_NOMEM;
+  std::memcpy(elem, R.elem.data(), sizeof(int32_t) * 3 * (size_t)nt);
+  G->edge = std::move(R.edge);
+  G->edneigh = std::move(R.edneigh);
+  G->iedge = std::move(R.iedge);
+  G->beindx = std::move(R.beindx);
+  G->spts = std::move(R.spts);
+  G->ds = std::move(R.ds);
+  G->dsb = std::move(R.dsb);
+  G->elarea = std::move(R.elarea);
+  G->cvarea = std::move(R.cvarea);
+  G->mcarea = std::move(R.mcarea);
+  G->drmin = std::move(R.drmin);
+  G->wd.assign(np, 0.0);
+  *out = publish(G, np, nt, R.nswe, coord, elem, ptype);
   return FVM_OK;
 }
 

@@ -878,6 +878,30 @@ __device__ __forceinline__ FluxConst<R> flux_const(const MeshConst &mc) {
   return c;
 }
 
+// The same constants when every resident mesh has math.f:8-40's values
+// (fvm_params_init; the host checks): compile-time values, each the FP32
+// rounding of the double the driver computes, so the edge loop keeps none
+// of them in registers.
+__device__ __forceinline__ FluxConst<float> flux_const_std(const MeshConst &mc) {
+  FluxConst<float> c;
+  c.a11 = (float)(2.0 / 3.0);
+  c.a12 = (float)(1.0 - 2.0 / 3.0);
+  c.a21 = (float)(4.0 / 3.0);
+  c.a22 = (float)(1.0 - 4.0 / 3.0);
+  c.eps = (float)1.0e-16;
+  c.gamma = (float)1.4;
+  c.gamma1 = (float)(1.4 - 1.0);
+  c.pi = (float)3.141592653589793;
+  c.ilimit = mc.ilimit;
+  c.iflux = mc.iflux;
+  c.rotate_back = mc.bugcompat ? 0 : 1;
+  return c;
+}
+
+// Flux-pass template code: the Riemann solver (1/2/3; 0 dispatches on the
+// mesh's iflux) plus kFluxStd when the FP32 constants are the standard ones.
+constexpr int kFluxStd = 4;
+
 // FP32: the edge's unit normal and length from its ds (flux.f:10-13) with
 // one reciprocal square root.
 __device__ __forceinline__ void edge_normal_f32(float dsx, float dsy, float &ct, float &st,
@@ -959,7 +983,8 @@ __device__ __forceinline__ void edge_flux(const ArenaPtrs<R> &A, const FluxConst
     st = R(csl.y);
     len = R(csl.z);
   }
-  const int which = FLUX ? FLUX : fc.iflux;
+  constexpr int FL = FLUX & 3;
+  const int which = FL ? FL : fc.iflux;
   if (which == 1) {
     if (!roe_flux<R>(ct, st, len, pl, pr, fc.gamma, fc.gamma1, f)) err = 1;
   } else if (which == 2) {
@@ -1122,7 +1147,9 @@ __global__ void __launch_bounds__(sizeof(R) == 4 ? kFluxThreads : kBlockVerts,
       }
     }
     int err = 0;
-    const FluxConst<R> fc = flux_const<R>(mc);
+    FluxConst<R> fc;
+    if constexpr (sizeof(R) == 4 && (FLUX & kFluxStd) != 0) fc = flux_const_std(mc);
+    else fc = flux_const<R>(mc);
     // phase 1a: interior edges
     for (int k = threadIdx.x; k < bi.ne; k += blockDim.x) {
       R f[4];

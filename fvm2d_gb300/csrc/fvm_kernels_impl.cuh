@@ -22,6 +22,50 @@ inline int fit_grid(const LaunchCfg &c, K kern, size_t smem, int threads = kBloc
   return g < c.grid ? g : c.grid;
 }
 
+// The flux pass for template code F (Riemann solver | kFluxStd).
+template <typename R, int F>
+inline void launch_flux_code(const ArenaPtrs<R> &A, const LaunchCfg &c, size_t sm, int nt,
+                             int stage, int mode, int irk, int routine) {
+  k_flux<R, F><<<fit_grid(c, k_flux<R, F>, sm, nt), nt, sm, c.stream>>>(A, stage, mode, irk,
+                                                                         routine);
+}
+template <typename R>
+inline void launch_flux_any(const ArenaPtrs<R> &A, const LaunchCfg &c, size_t sm, int nt,
+                            int stage, int mode, int irk, int routine) {
+  if constexpr (sizeof(R) == 4) {
+    if (c.std_const) {
+      switch (c.flux) {
+        case 1: launch_flux_code<R, 1 | kFluxStd>(A, c, sm, nt, stage, mode, irk, routine); return;
+        case 2: launch_flux_code<R, 2 | kFluxStd>(A, c, sm, nt, stage, mode, irk, routine); return;
+        case 3: launch_flux_code<R, 3 | kFluxStd>(A, c, sm, nt, stage, mode, irk, routine); return;
+        default: launch_flux_code<R, kFluxStd>(A, c, sm, nt, stage, mode, irk, routine); return;
+      }
+    }
+  }
+  switch (c.flux) {
+    case 1: launch_flux_code<R, 1>(A, c, sm, nt, stage, mode, irk, routine); return;
+    case 2: launch_flux_code<R, 2>(A, c, sm, nt, stage, mode, irk, routine); return;
+    case 3: launch_flux_code<R, 3>(A, c, sm, nt, stage, mode, irk, routine); return;
+    default: launch_flux_code<R, 0>(A, c, sm, nt, stage, mode, irk, routine); return;
+  }
+}
+// dynamic shared memory attribute of every flux-pass instantiation
+template <typename R>
+inline cudaError_t flux_attributes(size_t f) {
+  const int b = (int)f;
+  cudaError_t e = cudaFuncSetAttribute(k_flux<R, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_flux<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_flux<R, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_flux<R, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+  if constexpr (sizeof(R) == 4) {
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_flux<R, kFluxStd>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_flux<R, 1 | kFluxStd>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_flux<R, 2 | kFluxStd>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_flux<R, 3 | kFluxStd>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+  }
+  return e;
+}
+
 #define FVM_DEFINE_LAUNCHERS(R)                                                            \
   size_t smem_grad(const LaunchCfg &c, R *) {                                              \
     return size_t(c.max_tri) * (sizeof(TriSmem<R>) + (c.viscous ? 9 * sizeof(R) : 0));     \
@@ -97,12 +141,7 @@ inline int fit_grid(const LaunchCfg &c, K kern, size_t smem, int threads = kBloc
     size_t sm = smem_flux(c, (R *)nullptr);                                                \
     if (sm > kMaxSmem) return cudaErrorInvalidConfiguration;                              \
     const int nt = sizeof(R) == 4 ? kFluxThreads : kBlockVerts;                           \
-    switch (c.flux) {                                                                      \
-      case 1: k_flux<R, 1><<<fit_grid(c, k_flux<R, 1>, sm, nt), nt, sm, c.stream>>>(A, stage, mode, irk, routine); break; \
-      case 2: k_flux<R, 2><<<fit_grid(c, k_flux<R, 2>, sm, nt), nt, sm, c.stream>>>(A, stage, mode, irk, routine); break; \
-      case 3: k_flux<R, 3><<<fit_grid(c, k_flux<R, 3>, sm, nt), nt, sm, c.stream>>>(A, stage, mode, irk, routine); break; \
-      default: k_flux<R, 0><<<fit_grid(c, k_flux<R, 0>, sm, nt), nt, sm, c.stream>>>(A, stage, mode, irk, routine); \
-    }                                                                                      \
+    launch_flux_any<R>(A, c, sm, nt, stage, mode, irk, routine);                           \
     return cudaGetLastError();                                                             \
   }                                                                                        \
   size_t smem_step(const LaunchCfg &c, R *) {                                              \
@@ -186,14 +225,7 @@ inline int fit_grid(const LaunchCfg &c, K kern, size_t smem, int threads = kBloc
     }                                                                                      \
     cudaError_t e = cudaFuncSetAttribute(k_grad<R>,                                        \
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g); \
-    if (e == cudaSuccess)                                                                  \
-      e = cudaFuncSetAttribute(k_flux<R, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f); \
-    if (e == cudaSuccess)                                                                  \
-      e = cudaFuncSetAttribute(k_flux<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f); \
-    if (e == cudaSuccess)                                                                  \
-      e = cudaFuncSetAttribute(k_flux<R, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f); \
-    if (e == cudaSuccess)                                                                  \
-      e = cudaFuncSetAttribute(k_flux<R, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f); \
+    if (e == cudaSuccess) e = flux_attributes<R>(f);                                       \
     if (e == cudaSuccess)                                                                  \
       e = cudaFuncSetAttribute(k_sa<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s); \
     const size_t gb = grad_bulk_layout(c.max_tri, kTriLocMax, c.viscous).total;            \

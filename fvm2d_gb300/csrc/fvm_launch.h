@@ -28,6 +28,7 @@ struct LaunchCfg {
   bool any_inviscid; // an inviscid mesh is resident
   int pipe_groups;   // consumer groups of a pipelined kernel's CTA (1 or 2)
   int pipe_stages;   // stages of its ring (0: as many as fit, at most kPipeMaxStages)
+  bool std_const;    // every resident mesh has math.f's constants (FP32 flux pass folds them)
   cudaStream_t stream;
 };
 

@@ -71,17 +71,20 @@ class MeshArrays:
 
 
 def build_geometry(coord, elem, ptype, *, cell_type=L.MEDIAN, wall_distance=False,
-                   bugcompat=1, setup_on_gpu=True) -> MeshArrays:
+                   bugcompat=1, setup_on_gpu=True, chain_on_gpu=False) -> MeshArrays:
     """geometric.f:15-60 for a grid: host chain + GPU dtlength / wall_dist.
 
     With ``setup_on_gpu=False`` drmin and wd stay zero (host-only callers).
+    With ``chain_on_gpu=True`` the chain itself runs on the GPU
+    (fvm_gpu_geom_build: the same arrays bit for bit, drmin included).
     """
     coord = np.ascontiguousarray(coord, dtype=np.float64)
     elem = np.array(elem, dtype=np.int32, order="C", copy=True)   # oriented in place
     ptype = np.ascontiguousarray(ptype, dtype=np.int32)
     gp = C.POINTER(L.FvmGeom)()
-    check(L.lib().fvm_geom_build(coord.shape[0], elem.shape[0], dptr(coord), iptr(elem),
-                                 iptr(ptype), cell_type, C.byref(gp)), "fvm_geom_build")
+    fn = "fvm_gpu_geom_build" if chain_on_gpu else "fvm_geom_build"
+    check(getattr(L.lib(), fn)(coord.shape[0], elem.shape[0], dptr(coord), iptr(elem),
+                               iptr(ptype), cell_type, C.byref(gp)), fn)
     try:
         g = gp.contents
         m = g.mesh
@@ -99,11 +102,13 @@ def build_geometry(coord, elem, ptype, *, cell_type=L.MEDIAN, wall_distance=Fals
                  iedge=iarr(g.iedge, m.ne), beindx=iarr(g.beindx, m.nbe),
                  ds=darr(g.ds, 2 * netot).reshape(-1, 2), dsb=darr(g.dsb, 2 * npt).reshape(-1, 2),
                  elarea=darr(g.elarea, nt), cvarea=darr(g.cvarea, npt),
-                 mcarea=darr(g.mcarea, npt), drmin=np.zeros(npt), wd=np.zeros(npt))
+                 mcarea=darr(g.mcarea, npt),
+                 drmin=darr(g.drmin, npt) if chain_on_gpu else np.zeros(npt), wd=np.zeros(npt))
     finally:
         L.lib().fvm_geom_free(gp)
     if setup_on_gpu:
-        d["drmin"] = dtlength(d["coord"], d["elem"], d["elarea"])
+        if not chain_on_gpu:
+            d["drmin"] = dtlength(d["coord"], d["elem"], d["elarea"])
         if wall_distance:
             d["wd"] = wall_dist(d["coord"], d["edge"], d["ptype"], bugcompat)
     return MeshArrays(d)

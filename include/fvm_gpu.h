@@ -242,6 +242,15 @@ int32_t fvm_geom_build(int32_t np, int32_t nt, const double *coord,
                        int32_t *elem, const int32_t *ptype,
                        int32_t cell_type, fvm_geom **out);
 int32_t fvm_geom_free(fvm_geom *g);
+/* The same chain on the GPU, for callers that build many grids (the
+ * serving path's request preparation): every array equal to
+ * fvm_geom_build's, bit for bit (same numbering, same floating-point
+ * operations in the same order), and drmin filled as fvm_gpu_dtlength
+ * fills it.  elem is oriented in place on success and left untouched on
+ * error.  Release with fvm_geom_free(). */
+int32_t fvm_gpu_geom_build(int32_t np, int32_t nt, const double *coord,
+                           int32_t *elem, const int32_t *ptype,
+                           int32_t cell_type, fvm_geom **out);
 
 /* ---- allocation-free entry point ----------------------------------------- */
 /* No counterpart in the reference.  conres.f:11-31 (RMS and first argmax of
