@@ -772,7 +772,7 @@ def run_probe(args):
     par = F.make_params(precision=prec, bugcompat=0, **flow)
     slots = [b.add(par, m) for m in meshes]
     for s in slots:
-        b.start(s, args.warmup + args.steps)
+        b.start(s, args.warmup + args.steps + 25)
     b.set_form(args.form or "bulk")
     b.step(args.warmup)
     b.sync()
@@ -780,10 +780,23 @@ def run_probe(args):
     b.step(args.steps)
     b.sync()
     dt = (time.perf_counter() - t0) / max(args.steps, 1)
+    # per-kernel CUDA events over a few more iterations (one kernel at a
+    # time: the events need a host sync after every iteration)
+    b.timing(True)
+    b.step(1)
+    b.sync()
+    b.timing(True)
+    nk = min(args.steps, 20)
+    b.step(nk)
+    b.sync()
+    kt = b.timing_read()
+    b.timing(False)
     polls = [b.poll(s) for s in slots]
     out = {"mode": "probe", "flow": args.flow, "precision": args.precision,
            "meshes": args.meshes, "vertices_per_mesh": meshes[0].np, "form": args.form or "bulk",
-           "iters": args.steps, "ms_per_iter": dt * 1e3, "status": [p["status"] for p in polls]}
+           "iters": args.steps, "ms_per_iter": dt * 1e3, "status": [p["status"] for p in polls],
+           "kernel_ms_per_iter": {k: round(v[0] / nk, 4) for k, v in kt.items() if v[1]},
+           "kernel_launches_per_iter": {k: v[1] / nk for k, v in kt.items() if v[1]}}
     b.close()
     print(json.dumps(out), flush=True)
 
