@@ -29,6 +29,9 @@
 #ifndef FVM_STENCIL_MINB
 #define FVM_STENCIL_MINB 1  // resident CTAs per SM asked of the stencil gradient kernel
 #endif
+#ifndef FVM_STENCIL_PIPE
+#define FVM_STENCIL_PIPE 1  // stencil pass: next trip's neighbour ids in flight with this trip's states
+#endif
 #ifndef FVM_STENCIL_BATCH
 #define FVM_STENCIL_BATCH 4 // edges whose loads are in flight at once per thread
 #endif
@@ -594,18 +597,35 @@ __global__ void __launch_bounds__(kBlockVerts, FVM_STENCIL_MINB)
       const R4<R> pv = P[v];
       const int2 r = A.va_rng[v];
       R qx[4] = {R(0), R(0), R(0), R(0)}, qy[4] = {R(0), R(0), R(0), R(0)};
+#if FVM_STENCIL_PIPE
+      // the next trip's neighbour ids are loaded while this trip's states
+      // are in flight: one dependent load latency per trip instead of two
+      int un[B];
+#pragma unroll
+      for (int k = 0; k < B; k++)
+        un[k] = k < r.y - r.x ? (A.va_list[r.x + k] & 0x7fffffff) : v;
+#endif
       for (int j = r.x; j < r.y; j += B) {
         const int n = r.y - j;
         int u[B];
         float2 wt[B];
 #pragma unroll
         for (int k = 0; k < B; k++) {
+#if FVM_STENCIL_PIPE
+          u[k] = un[k];
+#else
           u[k] = k < n ? (A.va_list[j + k] & 0x7fffffff) : v;
+#endif
           wt[k] = k < n ? A.va_w[j + k] : make_float2(0.f, 0.f);
         }
         R4<R> pu[B];
 #pragma unroll
         for (int k = 0; k < B; k++) pu[k] = k < n ? P[u[k]] : pv;
+#if FVM_STENCIL_PIPE
+#pragma unroll
+        for (int k = 0; k < B; k++)
+          un[k] = k < n - B ? (A.va_list[j + B + k] & 0x7fffffff) : v;
+#endif
 #pragma unroll
         for (int k = 0; k < B; k++) {
           if (k < n) {
