@@ -29,6 +29,12 @@
 #ifndef FVM_STENCIL_MINB
 #define FVM_STENCIL_MINB 1  // resident CTAs per SM asked of the stencil gradient kernel
 #endif
+#ifndef FVM_GATHER_BATCH
+#define FVM_GATHER_BATCH 1  // FP32 flux pass: incidences loaded together in the per-vertex gather
+#endif
+#ifndef FVM_FLUX_PIPE
+#define FVM_FLUX_PIPE 1     // FP32 flux pass: the next edge entry's ends in flight with this entry's gathers
+#endif
 #ifndef FVM_STENCIL_PIPE
 #define FVM_STENCIL_PIPE 1  // stencil pass: next trip's neighbour ids in flight with this trip's states
 #endif
@@ -963,16 +969,19 @@ __device__ __forceinline__ void recon_edge_f32(const R4<float> &p1, const R4<flo
 
 // FLUX = 1/2/3 compiles one Riemann solver only (every resident mesh uses
 // it); FLUX = 0 dispatches on the mesh's iflux.
+// nn_in: the entry's ends when the caller has loaded them (FP32 edge loop),
+// else nullptr
 template <typename R, int FLUX>
 __device__ __forceinline__ void edge_flux(const ArenaPtrs<R> &A, const FluxConst<R> &fc,
-                                          const R4<R> *P, int e, R f[4], int &err) {
+                                          const R4<R> *P, int e, R f[4], int &err,
+                                          const int2 *nn_in = nullptr) {
   int2 nn;
   R dx, dy, ct, st, len;
   float dsx = 0.f, dsy = 0.f;
   if constexpr (sizeof(R) == 4) {
     // ends, edge vector and ds (24 bytes per entry); ds/|ds| and |ds| are
     // formed after the reconstruction
-    nn = A.be_nodes[e];
+    nn = nn_in ? *nn_in : A.be_nodes[e];
     const float4 h = A.be_g32[e].v;
     dx = h.x;
     dy = h.y;
@@ -1081,22 +1090,36 @@ __device__ __forceinline__ void flux_gather(const ArenaPtrs<R> &A, const MeshCon
       acc[0] = acc[1] = acc[2] = acc[3] = R(0);
     }
     const int2 jr = A.ve_rng[v];
-    for (int j = jr.x; j < jr.y; j++) {
-      const uint16_t e = A.ve_list[j];
-      const R4<R> f = s_flux[e & kSlotMask];
-      if (e & kSolidBit) {
-        acc[1] = acc[1] + f.y;
-        acc[2] = acc[2] + f.z;
-      } else if (e & kNegBit) {
-        acc[0] = acc[0] - f.x;
-        acc[1] = acc[1] - f.y;
-        acc[2] = acc[2] - f.z;
-        acc[3] = acc[3] - f.w;
-      } else {
-        acc[0] = acc[0] + f.x;
-        acc[1] = acc[1] + f.y;
-        acc[2] = acc[2] + f.z;
-        acc[3] = acc[3] + f.w;
+    // FVM_GATHER_BATCH incidences' slots and fluxes loaded together, then
+    // added in list order
+    constexpr int GB = sizeof(R) == 4 ? FVM_GATHER_BATCH : 1;
+    for (int j = jr.x; j < jr.y; j += GB) {
+      uint16_t es[GB];
+      R4<R> fs[GB];
+#pragma unroll
+      for (int u = 0; u < GB; u++) es[u] = j + u < jr.y ? A.ve_list[j + u] : uint16_t(0);
+#pragma unroll
+      for (int u = 0; u < GB; u++)
+        if (j + u < jr.y) fs[u] = s_flux[es[u] & kSlotMask];
+#pragma unroll
+      for (int u = 0; u < GB; u++) {
+        if (j + u >= jr.y) break;
+        const uint16_t e = es[u];
+        const R4<R> f = fs[u];
+        if (e & kSolidBit) {
+          acc[1] = acc[1] + f.y;
+          acc[2] = acc[2] + f.z;
+        } else if (e & kNegBit) {
+          acc[0] = acc[0] - f.x;
+          acc[1] = acc[1] - f.y;
+          acc[2] = acc[2] - f.z;
+          acc[3] = acc[3] - f.w;
+        } else {
+          acc[0] = acc[0] + f.x;
+          acc[1] = acc[1] + f.y;
+          acc[2] = acc[2] + f.z;
+          acc[3] = acc[3] + f.w;
+        }
       }
     }
     if (mode == MODE_RESIDUAL) {
@@ -1170,10 +1193,25 @@ __global__ void __launch_bounds__(sizeof(R) == 4 ? kFluxThreads : kBlockVerts,
     FluxConst<R> fc;
     if constexpr (sizeof(R) == 4 && (FLUX & kFluxStd) != 0) fc = flux_const_std(mc);
     else fc = flux_const<R>(mc);
-    // phase 1a: interior edges
+    // phase 1a: interior edges.  FP32: the next entry's ends are loaded
+    // while this entry's states and gradients are in flight
+#if FVM_FLUX_PIPE
+    int2 nn_next = make_int2(0, 0);
+    if (sizeof(R) == 4 && threadIdx.x < bi.ne) nn_next = A.be_nodes[bi.e0 + threadIdx.x];
+#endif
     for (int k = threadIdx.x; k < bi.ne; k += blockDim.x) {
       R f[4];
+#if FVM_FLUX_PIPE
+      if constexpr (sizeof(R) == 4) {
+        const int2 nn = nn_next;
+        if (k + (int)blockDim.x < bi.ne) nn_next = A.be_nodes[bi.e0 + k + blockDim.x];
+        edge_flux<R, FLUX>(A, fc, P, bi.e0 + k, f, err, &nn);
+      } else {
+        edge_flux<R, FLUX>(A, fc, P, bi.e0 + k, f, err);
+      }
+#else
       edge_flux<R, FLUX>(A, fc, P, bi.e0 + k, f, err);
+#endif
       R4<R> o;
       o.x = f[0];
       o.y = f[1];
