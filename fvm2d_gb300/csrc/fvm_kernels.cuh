@@ -27,7 +27,7 @@
 #define FVM_GRADV_MINB32 4  // the same for its per-vertex form
 #endif
 #ifndef FVM_STENCIL_MINB
-#define FVM_STENCIL_MINB 1  // resident CTAs per SM asked of the stencil gradient kernel
+#define FVM_STENCIL_MINB 6  // resident CTAs per SM asked of the stencil gradient kernel
 #endif
 #ifndef FVM_GATHER_BATCH
 #define FVM_GATHER_BATCH 1  // FP32 flux pass: incidences loaded together in the per-vertex gather
@@ -39,7 +39,7 @@
 #define FVM_STENCIL_PIPE 1  // stencil pass: next trip's neighbour ids in flight with this trip's states
 #endif
 #ifndef FVM_STENCIL_BATCH
-#define FVM_STENCIL_BATCH 4 // edges whose loads are in flight at once per thread
+#define FVM_STENCIL_BATCH 2 // edges whose loads are in flight at once per thread
 #endif
 
 namespace fvm {
