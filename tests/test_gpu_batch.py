@@ -315,3 +315,31 @@ def test_fp32_stencil_gradient_matches_triangle_sums(fvm_lib, oracle_lib):
         scale = np.abs(ref).max(axis=0)
         err = np.abs(got[k] - ref).max(axis=0) / scale
         assert np.all(err < 2e-5), f"{k}: {err}"
+
+
+def test_fp32_runtime_constants_build(fvm_lib):
+    """A mesh whose constants differ from math.f's (here the limiter's
+    epsilon) sends the FP32 flux pass to its build with runtime constants,
+    for every resident mesh.  A standard mesh in such a mix stays within
+    FP32 rounding of its solve alone (the builds differ only in what the
+    compiler rounds ahead), and the other mesh's solve (epsilon only keeps
+    the limiter's quotient defined) within the same tolerance of it."""
+    from fvm2d_gb300.batch import Batch
+    m = mesh(fvm_lib, 96, 40, seed=3)
+    flow = dict(mach=0.8, aoa_deg=1.25)
+    n = 30
+    h0, st0 = alone(fvm_lib, L.FP32, m, flow, n)
+    b = Batch(L.FP32, vertices=2 * m.np + 5000, meshes=2)
+    pa = fvm_lib.make_params(precision=L.FP32, **flow)
+    pb = fvm_lib.make_params(precision=L.FP32, **flow)
+    pb.epsilon = 2.0e-16
+    slots = [b.add(pa, m), b.add(pb, m)]
+    for s in slots:
+        b.start(s, n)
+    b.step(n)
+    for s in slots:
+        p = b.poll(s)
+        assert p["status"] == 0 and p["niter"] == n
+        np.testing.assert_allclose(b.get_state(s)["prim"], st0["prim"], rtol=1e-4, atol=1e-6)
+        np.testing.assert_allclose(b.history(s, 0, n)["fres"], h0["fres"], rtol=1e-3)
+    b.close()
