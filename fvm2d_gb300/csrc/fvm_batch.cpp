@@ -130,6 +130,7 @@ struct fvm_batch {
   float2 *va_w = nullptr;   // FP32: Green-Gauss stencil weights per va_list entry
   double *va_dsl = nullptr; // |ds| of each va_list entry's edge
   BlockInfo *blocks = nullptr;
+  BlockInfo *wblocks = nullptr;   // blocks[work[w]], refreshed with the work list
   int2 *be_nodes = nullptr, *sw_nodes = nullptr;
   double2 *be_ds = nullptr;
   D4 *be_csl = nullptr;
@@ -230,6 +231,7 @@ ArenaPtrs<R> ptrs(const fvm_batch *b) {
   A.vt_rng = b->vt_rng;
   A.vt_list = b->vt_list;
   A.blocks = b->blocks;
+  A.wblocks = b->wblocks;
   A.be_nodes = b->be_nodes;
   A.be_ds = b->be_ds;
   A.be_csl = b->be_csl;
@@ -540,6 +542,7 @@ int32_t update_work(fvm_batch *b) {
   }
   b->mesh_part_h = part;
   if (n) FVM_TRY(b, cudaMemcpyAsync(b->work, work.data(), n * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+  FVM_TRY(b, launch_gather_blocks(b->work, b->blocks, b->wblocks, n, b->stream));
   FVM_TRY(b, cudaMemcpyAsync(b->nwork, head, sizeof(head), cudaMemcpyHostToDevice, b->stream));
   FVM_TRY(b, cudaMemcpyAsync(b->mesh_part, b->mesh_part_h.data(), part.size() * sizeof(int),
                              cudaMemcpyHostToDevice, b->stream));
@@ -800,6 +803,7 @@ extern "C" int32_t fvm_batch_create(int32_t precision, const fvm_batch_caps *cap
   TRYB(dalloc(O, &b->va_list, (size_t)c.all_incidence));
   TRYB(dalloc(O, &b->va_dsl, (size_t)c.all_incidence));
   TRYB(dalloc(O, &b->blocks, (size_t)c.blocks));
+  TRYB(dalloc(O, &b->wblocks, (size_t)c.blocks));
   TRYB(dalloc(O, &b->part, (size_t)c.blocks));
   TRYB(dalloc(O, &b->work, (size_t)c.blocks));
   TRYB(dalloc(O, &b->nwork, 1 + kMaxChains));

@@ -238,6 +238,7 @@ struct ArenaPtrs {
   const uint16_t *vt_list;
   // block entries
   const BlockInfo *blocks;
+  const BlockInfo *wblocks;  // blocks[work[w]] for each w (copies in work-list order)
   const int2 *be_nodes;   // interior edge entries (n1, n2)
   const double2 *be_ds;   // ds of the edge (flength.f:38-39)
   const D4 *be_csl;       // (ct, st, length) precomputed in FP64

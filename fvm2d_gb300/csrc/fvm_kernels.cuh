@@ -99,10 +99,18 @@ __device__ __forceinline__ void work_range(const ArenaPtrs<R> &A, int &w0, int &
   }
 }
 
-__device__ __forceinline__ const BlockInfo *next_block(const BlockInfo *blocks, const int *work,
-                                                       int w, int nwork) {
+// Block w of the work list: its copy in work-list order (one load, not an
+// index load followed by the block's; the host refreshes the copies with
+// the work list)
+template <typename R>
+__device__ __forceinline__ const BlockInfo &work_block(const ArenaPtrs<R> &A, int w) {
+  return A.wblocks[w];
+}
+
+template <typename R>
+__device__ __forceinline__ const BlockInfo *next_block(const ArenaPtrs<R> &A, int w, int nwork) {
   const int nw = w + gridDim.x;
-  return nw < nwork ? blocks + work[nw] : nullptr;
+  return nw < nwork ? &work_block(A, nw) : nullptr;
 }
 
 // ---------------------------------------------------------------------------
@@ -200,7 +208,7 @@ __global__ void __launch_bounds__(kBlockVerts) k_visc(ArenaPtrs<R> A, int stage,
   int w0, nwork;
   work_range(A, w0, nwork);
   for (int w = w0 + blockIdx.x; w < nwork; w += gridDim.x) {
-    const BlockInfo bi = A.blocks[A.work[w]];
+    const BlockInfo bi = work_block(A, w);
     const MeshCtl &ctl = A.ctl[bi.mesh];
     if (!routine && !ctl.active) continue;
     const MeshConst &mc = A.mc[bi.mesh];
@@ -376,7 +384,7 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRAD_MINB32 
   int w0, nwork;
   work_range(A, w0, nwork);
   for (int w = w0 + blockIdx.x; w < nwork; w += gridDim.x) {
-    const BlockInfo bi = A.blocks[A.work[w]];
+    const BlockInfo bi = work_block(A, w);
     const MeshCtl &ctl = A.ctl[bi.mesh];
     if (!routine && !ctl.active) continue;
     const MeshConst &mc = A.mc[bi.mesh];
@@ -384,7 +392,7 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRAD_MINB32 
     const bool visc = mc.iflow != 1;
     const R4<R> *P = A.st[cur_buf(ctl.phase, stage)];
     if (threadIdx.x == 0) {
-      const BlockInfo *nb = next_block(A.blocks, A.work, w, nwork);
+      const BlockInfo *nb = next_block(A, w, nwork);
       if (nb) {
         const BlockInfo n = *nb;
         prefetch_l2(A.bt_nodes + n.t0, sizeof(int4) * n.nt);
@@ -472,7 +480,7 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRAD_MINB32 
     int w0, nwork;
   work_range(A, w0, nwork);
     for (int w = w0 + blockIdx.x; w < nwork; w += gridDim.x) {
-      const BlockInfo bi = A.blocks[A.work[w]];
+      const BlockInfo bi = work_block(A, w);
       const MeshCtl &ctl = A.ctl[bi.mesh];
       if (!routine && !ctl.active) continue;
       const MeshConst &mc = A.mc[bi.mesh];
@@ -493,7 +501,7 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRAD_MINB32 
         bulk_g2s(s_vtr, A.vt_rng + bi.v0, nvtr, &bar);
         if (nvtl) bulk_g2s(s_vtl, A.vt_list + vt_a, nvtl, &bar);
         bulk_g2s(s_pv, P + bi.v0, npv, &bar);
-        const BlockInfo *nb = next_block(A.blocks, A.work, w, nwork);
+        const BlockInfo *nb = next_block(A, w, nwork);
         if (nb) {
           const BlockInfo n = *nb;
           prefetch_l2(A.tri_g32 + n.t0, sizeof(TriGeo32) * n.nt);
@@ -593,7 +601,7 @@ __global__ void __launch_bounds__(kBlockVerts, FVM_STENCIL_MINB)
     int w0, nwork;
     work_range(A, w0, nwork);
     for (int w = w0 + blockIdx.x; w < nwork; w += gridDim.x) {
-      const BlockInfo bi = A.blocks[A.work[w]];
+      const BlockInfo bi = work_block(A, w);
       const MeshCtl &ctl = A.ctl[bi.mesh];
       if (!routine && !ctl.active) continue;
       const MeshConst &mc = A.mc[bi.mesh];
@@ -667,7 +675,7 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRADV_MINB32
   int w0, nwork;
   work_range(A, w0, nwork);
   for (int w = w0 + blockIdx.x; w < nwork; w += gridDim.x) {
-    const BlockInfo bi = A.blocks[A.work[w]];
+    const BlockInfo bi = work_block(A, w);
     const MeshCtl &ctl = A.ctl[bi.mesh];
     if (!routine && !ctl.active) continue;
     const MeshConst &mc = A.mc[bi.mesh];
@@ -675,7 +683,7 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_GRADV_MINB32
     const bool visc = mc.iflow != 1;
     const R4<R> *P = A.st[cur_buf(ctl.phase, stage)];
     if (threadIdx.x == 0) {
-      const BlockInfo *nb = next_block(A.blocks, A.work, w, nwork);
+      const BlockInfo *nb = next_block(A, w, nwork);
       if (nb) {
         const BlockInfo n = *nb;
         prefetch_l2(A.bt_nodes + n.t0, sizeof(int4) * n.nt);
@@ -1163,7 +1171,7 @@ __global__ void __launch_bounds__(sizeof(R) == 4 ? kFluxThreads : kBlockVerts,
   int w0, nwork;
   work_range(A, w0, nwork);
   for (int w = w0 + blockIdx.x; w < nwork; w += gridDim.x) {
-    const BlockInfo bi = A.blocks[A.work[w]];
+    const BlockInfo bi = work_block(A, w);
     MeshCtl &ctl = A.ctl[bi.mesh];
     if (!routine && !ctl.active) continue;
     const MeshConst &mc = A.mc[bi.mesh];
@@ -1173,7 +1181,7 @@ __global__ void __launch_bounds__(sizeof(R) == 4 ? kFluxThreads : kBlockVerts,
     // prefetches made the pass slower (0.206 -> 0.216 ms on 8 meshes of
     // 1024 x 384 timed alone; whole iterations 1.025 -> 1.040 ms).
     if (sizeof(R) == 8 && threadIdx.x == 0) {
-      const BlockInfo *nb = next_block(A.blocks, A.work, w, nwork);
+      const BlockInfo *nb = next_block(A, w, nwork);
       if (nb) {
         const BlockInfo n = *nb;
         prefetch_l2(A.be_nodes + n.e0, sizeof(int2) * n.ne);
@@ -1261,7 +1269,7 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_FLUX_MINB32 
   int w0, nwork;
   work_range(A, w0, nwork);
   for (int w = w0 + blockIdx.x; w < nwork; w += gridDim.x) {
-    const BlockInfo bi = A.blocks[A.work[w]];
+    const BlockInfo bi = work_block(A, w);
     MeshCtl &ctl = A.ctl[bi.mesh];
     if (!ctl.active) continue;
     const MeshConst &mc = A.mc[bi.mesh];
@@ -1269,7 +1277,7 @@ __global__ void __launch_bounds__(kBlockVerts, sizeof(R) == 4 ? FVM_FLUX_MINB32 
     const int p = ctl.phase;
     const R4<R> *P = A.st[cur_buf(p, stage)];
     if (threadIdx.x == 0) {
-      const BlockInfo *nb = next_block(A.blocks, A.work, w, nwork);
+      const BlockInfo *nb = next_block(A, w, nwork);
       if (nb) {
         const BlockInfo n = *nb;
         prefetch_l2(A.bt_nodes + n.t0, sizeof(int4) * n.nt2);
@@ -1522,7 +1530,7 @@ __global__ void __launch_bounds__(kBlockVerts) k_sa(ArenaPtrs<R> A, int stage, i
   int w0, nwork;
   work_range(A, w0, nwork);
   for (int w = w0 + blockIdx.x; w < nwork; w += gridDim.x) {
-    const BlockInfo bi = A.blocks[A.work[w]];
+    const BlockInfo bi = work_block(A, w);
     MeshCtl &ctl = A.ctl[bi.mesh];
     if (!routine && !ctl.active) continue;
     const MeshConst &mc = A.mc[bi.mesh];
@@ -1879,7 +1887,7 @@ __global__ void __launch_bounds__(kBlockVerts) k_update(ArenaPtrs<R> A, int irk)
   int w0, nwork;
   work_range(A, w0, nwork);
   for (int w = w0 + blockIdx.x; w < nwork; w += gridDim.x) {
-    const BlockInfo bi = A.blocks[A.work[w]];
+    const BlockInfo bi = work_block(A, w);
     if (threadIdx.x >= bi.nv) continue;
     const MeshCtl &ctl = A.ctl[bi.mesh];
     const MeshConst &mc = A.mc[bi.mesh];
@@ -1898,7 +1906,7 @@ __global__ void __launch_bounds__(kBlockVerts) k_time_step(ArenaPtrs<R> A) {
   int w0, nwork;
   work_range(A, w0, nwork);
   for (int w = w0 + blockIdx.x; w < nwork; w += gridDim.x) {
-    const BlockInfo bi = A.blocks[A.work[w]];
+    const BlockInfo bi = work_block(A, w);
     if (threadIdx.x >= bi.nv) continue;
     const MeshCtl &ctl = A.ctl[bi.mesh];
     const int v = bi.v0 + threadIdx.x;
@@ -1911,7 +1919,7 @@ __global__ void __launch_bounds__(kBlockVerts) k_positivity(ArenaPtrs<R> A) {
   int w0, nwork;
   work_range(A, w0, nwork);
   for (int w = w0 + blockIdx.x; w < nwork; w += gridDim.x) {
-    const BlockInfo bi = A.blocks[A.work[w]];
+    const BlockInfo bi = work_block(A, w);
     if (threadIdx.x >= bi.nv) continue;
     MeshCtl &ctl = A.ctl[bi.mesh];
     const int v = bi.v0 + threadIdx.x;
@@ -1929,7 +1937,7 @@ __global__ void __launch_bounds__(kBlockVerts) k_conres_part(ArenaPtrs<R> A) {
   int w0, nwork;
   work_range(A, w0, nwork);
   for (int w = w0 + blockIdx.x; w < nwork; w += gridDim.x) {
-    const BlockInfo bi = A.blocks[A.work[w]];
+    const BlockInfo bi = work_block(A, w);
     const MeshCtl &ctl = A.ctl[bi.mesh];
     double d2 = 0.0, dabs = 0.0;
     int darg = INT_MAX;
@@ -2031,7 +2039,7 @@ __global__ void __launch_bounds__(kBlockVerts) k_gradient_edge(ArenaPtrs<R> A) {
   int w0, nwork;
   work_range(A, w0, nwork);
   for (int w = w0 + blockIdx.x; w < nwork; w += gridDim.x) {
-    const BlockInfo bi = A.blocks[A.work[w]];
+    const BlockInfo bi = work_block(A, w);
     const MeshCtl &ctl = A.ctl[bi.mesh];
     const R4<R> *P = A.st[ctl.phase];
     for (int k = threadIdx.x; k < bi.ne; k += blockDim.x) {
@@ -2113,7 +2121,7 @@ __global__ void __launch_bounds__(kBlockVerts) k_shockind(ArenaPtrs<R> A) {
   int w0, nwork;
   work_range(A, w0, nwork);
   for (int w = w0 + blockIdx.x; w < nwork; w += gridDim.x) {
-    const BlockInfo bi = A.blocks[A.work[w]];
+    const BlockInfo bi = work_block(A, w);
     if (threadIdx.x >= bi.nv) continue;
     const MeshCtl &ctl = A.ctl[bi.mesh];
     const MeshConst &mc = A.mc[bi.mesh];
@@ -2156,7 +2164,7 @@ __global__ void __launch_bounds__(kBlockVerts) k_limitgrad(ArenaPtrs<R> A) {
   int w0, nwork;
   work_range(A, w0, nwork);
   for (int w = w0 + blockIdx.x; w < nwork; w += gridDim.x) {
-    const BlockInfo bi = A.blocks[A.work[w]];
+    const BlockInfo bi = work_block(A, w);
     if (threadIdx.x >= bi.nv) continue;
     const MeshCtl &ctl = A.ctl[bi.mesh];
     const MeshConst &mc = A.mc[bi.mesh];

@@ -94,5 +94,7 @@ cudaError_t launch_get_vertex_sel(int rsz, double *dst, unsigned char *const b[3
 // a mesh's control block set on the device for a new state (what 0) or a
 // start (what 1)
 cudaError_t launch_ctl_update(MeshCtl *c, int what, int n, double minres, cudaStream_t s);
+cudaError_t launch_gather_blocks(const int *work, const BlockInfo *blocks, BlockInfo *out, int n,
+                                 cudaStream_t s);
 
 }  // namespace fvm

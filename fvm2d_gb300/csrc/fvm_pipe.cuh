@@ -89,7 +89,7 @@ __device__ __forceinline__ PipeLook<R> pipe_look(const ArenaPtrs<R> &A, int w, i
   for (int k = 0; k < 16; k++) z[k] = 0;
   c.ok = c.phase = c.nphase = c.iflow = 0;
   if (w < nwork) {
-    c.bi = A.blocks[A.work[w]];
+    c.bi = work_block(A, w);
     const MeshCtl &ctl = A.ctl[c.bi.mesh];
     c.phase = ctl.phase;
     c.nphase = ctl.nphase;
@@ -105,7 +105,7 @@ __device__ __forceinline__ PipeLook<R> pipe_look(const ArenaPtrs<R> &A, int w, i
 template <typename R>
 __device__ __forceinline__ void pipe_timeout(const ArenaPtrs<R> &A, int mesh, int w_first,
                                              int nwork, volatile int *abort) {
-  if (mesh < 0 && w_first < nwork) mesh = A.blocks[A.work[w_first]].mesh;
+  if (mesh < 0 && w_first < nwork) mesh = work_block(A, w_first).mesh;
   if (mesh >= 0) atomicCAS(&A.ctl[mesh].err, 0, 6 /* FVM_ERR_TIMEOUT */);
   *abort = 1;
   __threadfence_block();
