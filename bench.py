@@ -247,8 +247,10 @@ def run_gpu(args):
                  "flux + gather + RK stage)")
     else:
         alg_stage = sum(sweep_fu_bytes(m.np, m.ne) for m in meshes)
-        kname = (f"k_flux<float, {FLUX_CODES[args.flux]}> (recon + {args.flux} flux + gather "
-                 "+ RK stage)")
+        # the workload's meshes have math.f's constants: the build with them
+        # compiled in (template code + 4)
+        kname = (f"k_flux<float, {FLUX_CODES[args.flux] + 4}> (recon + {args.flux} flux + gather "
+                 "+ RK stage; math.f constants compiled in)")
     # all launches of the pass together moved alg_stage bytes per stage (with
     # the overlapped chains each launch covers part of the meshes)
     alg_flux = alg_stage * 3 * args.steps / max(flux_n, 1)
